@@ -1,0 +1,373 @@
+"""Benchmark: full SVD of a 4096 x 4096 FP32 graded-spectrum matrix on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: A = Q1 diag(sigma) Q2^T, Q1/Q2 Haar (QR of seeded Gaussians,
+sign-fixed by diag(R)), sigma_i = 10^(-6 i / 4095) (cond 1e6), formed in
+FP64 and rounded to FP32 -- synthetic data with the shape and spectrum of
+the precision configuration.  A step is one complete SVD (U 4096x4096,
+sigma, V 4096x4096) through the library's device entry point with the
+input resident in HBM; L2 is flushed (a 256 MiB write) between timed steps.
+`value` is the mean ms per SVD (lower is better).  Under torchrun every rank
+runs its own replica on its own GPU (the path does not shard); value is the
+job-level ms per SVD (max-over-ranks time / SVDs completed).
+
+Other keys: plain FP32 and blocked FP32 modes timed on the same input
+(`modes`), accuracy of each mode against the known FP64 spectrum, stage and
+kernel-class times, the roofline of the dominant kernel class, e2e through
+the FP32 host API (pinned host buffers, copies inside the timed region), and
+the CPU baseline (the FP64 CPU restatement of the reference pipeline timed on
+a bounded sample of the same workload).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "ddc-svd_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+M = N = 4096
+SEED = 1
+METRIC = "4096^2 full-SVD ms (graded cond 1e6, FP32)"
+
+
+def graded_matrix(torch, n, seed, device):
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    G1 = torch.randn((n, n), dtype=torch.float64, device=device, generator=g)
+    G2 = torch.randn((n, n), dtype=torch.float64, device=device, generator=g)
+    Q1, R1 = torch.linalg.qr(G1)
+    Q1 = Q1 * torch.sign(torch.diagonal(R1))
+    Q2, R2 = torch.linalg.qr(G2)
+    Q2 = Q2 * torch.sign(torch.diagonal(R2))
+    s = 10.0 ** (-6.0 * torch.arange(n, dtype=torch.float64, device=device) / (n - 1))
+    A64 = (Q1 * s) @ Q2.T
+    return A64, s
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.out = ""
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(",") for r in self.out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def gemv_bytes(m, n):
+    """Algorithmic bytes of the memory-bound half of the bidiagonalisation:
+    every column step reads the trailing block twice (y = A^T u, x = A v),
+    2 * 4 * sum_i (m-i)(n-i) bytes in FP32."""
+    i = np.arange(n, dtype=np.float64)
+    return float(8.0 * np.sum((m - i) * (n - i)))
+
+
+def svd_flops(m, n):
+    return 8.0 * m * n * n - 4.0 / 3.0 * n ** 3
+
+
+def accuracy(torch, A64, s_true, s, U, V):
+    s64, U64, V64 = s.double(), U.double(), V.double()
+    R = A64 - (U64 * s64) @ V64.T
+    k = s.shape[0]
+    eye = torch.eye(k, dtype=torch.float64, device=A64.device)
+    st = torch.sort(s_true).values
+    return {
+        "resid": float(torch.linalg.norm(R) / torch.linalg.norm(A64)),
+        "orth_u": float(torch.linalg.norm(U64.T @ U64 - eye) / k ** 0.5),
+        "orth_v": float(torch.linalg.norm(V64.T @ V64 - eye) / k ** 0.5),
+        "sig_abs": float(torch.max(torch.abs(torch.sort(s64).values - st)) / st[-1]),
+    }
+
+
+def time_mode(torch, lib, h, Ac, bufs, mode, steps, warmup, flush):
+    m, n = M, N
+    s, Ut, Vt = bufs
+    for _ in range(warmup):
+        lib.svd_device_colmajor(h, m, n, Ac, s, Ut, Vt, mode=mode)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.svd_device_colmajor(h, m, n, Ac, s, Ut, Vt, mode=mode)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / steps
+
+
+def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
+    """FP64 CPU restatement of the reference pipeline (bidiag.c + host stages) on a
+    bounded sample of the 4096^2 workload, extrapolated to the full SVD."""
+    from oracle import oracle
+    oracle.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    m, n = A64_host.shape
+    # (1) bidiagonalisation: the first k Householder steps of the 4096^2 matrix
+    A = np.asfortranarray(A64_host.copy())
+    k = 2
+    t0 = time.perf_counter()
+    oracle.bidiag_steps(A, k)
+    t1 = time.perf_counter() - t0
+    k2 = int(max(k, min(n - 1, k * (0.45 * budget_s) / max(t1, 1e-3))))
+    A = np.asfortranarray(A64_host.copy())
+    t0 = time.perf_counter()
+    oracle.bidiag_steps(A, k2)
+    tb = time.perf_counter() - t0
+    i = np.arange(n - 1, dtype=np.float64)
+    work = (m - i) * (n - i)
+    bidiag_full = tb * work.sum() / work[:k2].sum()
+    # (2) the remaining stages on a 1024^2 slice, scaled by the O(n^3) cost
+    ns = 1024
+    B = np.asfortranarray(A64_host[:ns, :ns])
+    t0 = time.perf_counter()
+    oracle.svd(B)
+    tfull = time.perf_counter() - t0
+    Bb = np.asfortranarray(B.copy())
+    t0 = time.perf_counter()
+    oracle.bidiag_steps(Bb, ns)
+    tbb = time.perf_counter() - t0
+    rest_full = max(tfull - tbb, 0.0) * (n / ns) ** 3
+    total_ms = 1e3 * (bidiag_full + rest_full)
+    return {"value": round(total_ms, 1), "unit": "ms", "cores": threads, "kind": "port",
+            "sample": (f"FP64 CPU port of bidiag.c + host stages: first {k2} of {n - 1} Householder steps of the "
+                       f"4096^2 input ({tb:.1f} s, scaled by the step work sum (m-i)(n-i)), plus the other "
+                       f"stages on its leading 1024^2 block ({max(tfull - tbb, 0):.2f} s, scaled by (4096/1024)^3)")}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (FP64 port) timed on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rng = np.random.default_rng(SEED)
+    Q1, R1 = np.linalg.qr(rng.standard_normal((M, M)))
+    Q1 *= np.sign(np.diag(R1))
+    Q2, R2 = np.linalg.qr(rng.standard_normal((N, N)))
+    Q2 *= np.sign(np.diag(R2))
+    s = 10.0 ** (-6.0 * np.arange(N) / (N - 1))
+    A64 = ((Q1 * s) @ Q2.T).astype(np.float32).astype(np.float64)
+    budget = max(4.0, 150.0 / max(args.steps + args.warmup, 1))
+    vals = []
+    cb = None
+    for it in range(args.warmup + args.steps):
+        cb = cpu_baseline(A64, budget_s=budget)
+        if it >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = round(v, 1)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "svd_graded_4096x4096", "m": M, "n": N, "cond": 1e6, "l2": "n/a (CPU)"},
+            "cpu_baseline": cb, "e2e": {"value": round(v, 1), "unit": "ms", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the secondary mode timings")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import ddcsvd as lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    A64, s_true = graded_matrix(torch, N, SEED + rank, dev)
+    A32 = A64.float()
+    A64r = A32.double()
+    Ac = A32.t().contiguous()  # column-major buffer
+    h = lib.Handle(local)
+    bufs = (torch.empty(N, device=dev), torch.empty((N, M), device=dev), torch.empty((N, N), device=dev))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # accuracy + stage / kernel times of each mode (one extra untimed run each)
+    modes = ["tf32x3", "blocked", "plain"] if not args.quick else ["tf32x3"]
+    avail = []
+    info = {}
+    for mode in modes:
+        try:
+            lib.svd_device_colmajor(h, M, N, Ac, *bufs, mode=mode)
+        except lib.DdcsvdError as e:
+            if e.status == 8:
+                continue
+            raise
+        avail.append(mode)
+        torch.cuda.synchronize()
+        s, Ut, Vt = bufs
+        acc = accuracy(torch, A64r, torch.linalg.svdvals(A64r) if False else s_true, s, Ut.t(), Vt.t())
+        h.stage_timing(True)
+        lib.svd_device_colmajor(h, M, N, Ac, *bufs, mode=mode)
+        torch.cuda.synchronize()
+        st = h.stage_times()
+        kms, kn = h.kernel_times(5)
+        h.stage_timing(False)
+        info[mode] = {"accuracy": {k: float(f"{v:.3e}") for k, v in acc.items()},
+                      "stage_ms": dict(zip(["bidiag", "sigma", "vectors", "backxform"], [round(x, 3) for x in st])),
+                      "kernel_ms": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform"],
+                                            [round(x, 3) for x in kms])),
+                      "kernel_launches": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform"],
+                                                  kn))}
+    head = avail[0]
+
+    # timed region of the headline mode
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    phys = local
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd:
+        try:
+            phys = int(cvd.split(",")[local])
+        except ValueError:
+            phys = local
+    n_launch0 = lib.launch_count()
+    with ClockSampler(phys) as clk:
+        ms = time_mode(torch, lib, h, Ac, bufs, head, args.steps, args.warmup, flush)
+    launches = (lib.launch_count() - n_launch0) // max(args.steps + args.warmup, 1) * args.steps
+    t = torch.tensor([ms], device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = ms_max / world
+
+    # secondary modes (same input, fewer steps)
+    mode_ms = {head: round(ms, 3)}
+    for mode in avail[1:]:
+        mode_ms[mode] = round(time_mode(torch, lib, h, Ac, bufs, mode, max(2, args.steps // 2), 1, flush), 3)
+
+    # e2e through the FP32 host API: pinned host input, copies inside the timed region
+    Ah = torch.empty((N, M), dtype=torch.float32, pin_memory=True)
+    Ah.copy_(Ac.cpu())
+    Sh = torch.empty(N, dtype=torch.float32, pin_memory=True)
+    Uh = torch.empty((N, M), dtype=torch.float32, pin_memory=True)
+    Vh = torch.empty((N, N), dtype=torch.float32, pin_memory=True)
+    L = lib.load()
+    mcode = lib.MODES[head]
+
+    def host_call():
+        rc = L.ddcsvd_svd_f32(M, N, Ah.data_ptr(), M, Sh.data_ptr(), Uh.data_ptr(), M, Vh.data_ptr(), N, mcode)
+        lib.check(rc, "ddcsvd_svd_f32")
+
+    host_call()
+    e2e = []
+    for _ in range(max(2, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_call()
+        e2e.append(1e3 * (time.perf_counter() - t0))
+    e2e_ms = float(np.mean(e2e))
+
+    # roofline of the dominant kernel class (bidiagonalisation GEMV kernels)
+    hbm, peak_kind = measured_peaks()
+    kinfo = info[head]
+    bid_ms = kinfo["kernel_ms"]["bidiag_kernels"]
+    nl = max(kinfo["kernel_launches"]["bidiag_kernels"], 1)
+    bytes_total = gemv_bytes(M, N)
+    achieved = bytes_total / (bid_ms * 1e-3) / 1e9 if bid_ms > 0 else None
+    roof = {"bound": "hbm", "kernel": "bidiag_panel_kernel", "achieved": round(achieved, 1) if achieved else None,
+            "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(achieved / hbm, 3) if achieved else None, "traffic": None,
+            "bytes_per_launch": round(bytes_total / nl), "launches": nl,
+            "avg_launch_ms": round(bid_ms / nl, 4)}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    cb = None
+    if world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(A64r.cpu().numpy())
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 sigma/vector stages)", "data": "synthetic",
+        "config": {"workload": "svd_graded_4096x4096", "m": M, "n": N, "cond": 1e6, "mode": head,
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}"},
+        "modes_ms": mode_ms, "modes": info,
+        "gflops": round(svd_flops(M, N) / (ms * 1e-3) / 1e9, 1),
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": M * N * 4,
+                "d2h_bytes_per_step": (N + M * N + N * N) * 4, "api": "ddcsvd_svd_f32 (pinned host buffers)"},
+        "roofline": roof, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cb,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,774 @@
+// api.cu -- handles, workspace, the five-stage pipeline and the C ABI.
+//
+// Pipeline (svd_gpu.c:99-121 order), m >= n (m < n runs on A^T):
+//   1. bidiagonalisation (FP32)                      bidiag.cu
+//   2. singular values by double D&C (FP64)          dc.cu
+//   3-4. right/left vectors of B (FP64 core)         twisted.cu
+//   5. back-transformation U = Q [Y;0], V = P X      backxform.cu
+// All stages are enqueued on the handle's stream; the only host sync is the
+// final read of the device status word.
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+
+#include "internal.hpp"
+
+namespace ddcsvd {
+
+long long g_launch_count = 0;
+static thread_local std::string t_last_error;
+
+void set_last_error(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+}
+
+void ktimer_begin(ddcsvd_context* ctx, int cls) {
+  if (!ctx->timing) return;
+  if ((size_t)(2 * ctx->kused + 2) > ctx->kev.size()) {
+    for (int k = 0; k < 64; k++) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      ctx->kev.push_back(e);
+    }
+  }
+  if ((int)ctx->kcat.size() <= ctx->kused) ctx->kcat.resize(ctx->kused + 1);
+  ctx->kcat[ctx->kused] = cls;
+  cudaEventRecord(ctx->kev[2 * ctx->kused], ctx->stream);
+}
+
+void ktimer_end(ddcsvd_context* ctx) {
+  if (!ctx->timing || (size_t)(2 * ctx->kused + 2) > ctx->kev.size()) return;
+  cudaEventRecord(ctx->kev[2 * ctx->kused + 1], ctx->stream);
+  ctx->kused++;
+}
+
+void ktimer_collect(ddcsvd_context* ctx) {
+  if (!ctx->timing) return;
+  for (int c = 0; c < 8; c++) { ctx->kern_ms[c] = 0.f; ctx->kern_n[c] = 0; }
+  for (int i = 0; i < ctx->kused; i++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->kev[2 * i], ctx->kev[2 * i + 1]) == cudaSuccess) {
+      ctx->kern_ms[ctx->kcat[i]] += ms;
+      ctx->kern_n[ctx->kcat[i]] += 1;
+    }
+  }
+  ctx->kused = 0;
+}
+
+int ensure_workspace(ddcsvd_context* ctx, size_t bytes) {
+  if (bytes <= ctx->ws_bytes) return DDCSVD_OK;
+  if (ctx->ws) {
+    DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->ws);
+    ctx->ws = nullptr;
+    ctx->ws_bytes = 0;
+  }
+  size_t want = (size_t)round_up((long long)bytes, 1 << 21);
+  if (cudaMalloc(&ctx->ws, want) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("device workspace of %zu bytes could not be allocated", want);
+    return DDCSVD_ERR_ALLOC;
+  }
+  ctx->ws_bytes = want;
+  return DDCSVD_OK;
+}
+
+int ensure_pinned(ddcsvd_context* ctx, size_t bytes) {
+  if (bytes <= ctx->pinned_bytes) return DDCSVD_OK;
+  if (ctx->pinned) {
+    DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->pinned);
+    ctx->pinned = nullptr;
+    ctx->pinned_bytes = 0;
+  }
+  size_t want = (size_t)round_up((long long)bytes, 1 << 20);
+  if (cudaMallocHost(&ctx->pinned, want) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("pinned host buffer of %zu bytes could not be allocated", want);
+    return DDCSVD_ERR_ALLOC;
+  }
+  ctx->pinned_bytes = want;
+  return DDCSVD_OK;
+}
+
+int reset_status(ddcsvd_context* ctx) {
+  DDC_CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, sizeof(DevStatus), ctx->stream));
+  return DDCSVD_OK;
+}
+
+int check_status(ddcsvd_context* ctx, const char* stage) {
+  DDC_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (ctx->h_status->code != 0) {
+    set_last_error("%s: device status %d (detail %d)", stage, ctx->h_status->code, ctx->h_status->detail);
+    return ctx->h_status->code;
+  }
+  return DDCSVD_OK;
+}
+
+static GemmKind kind_of(int mode) {
+  switch (mode) {
+    case DDCSVD_MODE_BLOCKED_TF32X3: return GEMM_TF32X3;
+    case DDCSVD_MODE_BLOCKED_BF16X3: return GEMM_BF16X3;
+    default: return GEMM_SIMT;
+  }
+}
+
+static int resolve_mode(int mode) {
+  if (mode != DDCSVD_MODE_AUTO) return mode;
+  const char* e = getenv("DDCSVD_MODE");
+  if (e) {
+    if (!strcmp(e, "plain")) return DDCSVD_MODE_PLAIN_FP32;
+    if (!strcmp(e, "blocked")) return DDCSVD_MODE_BLOCKED_FP32;
+    if (!strcmp(e, "tf32x3")) return DDCSVD_MODE_BLOCKED_TF32X3;
+    if (!strcmp(e, "bf16x3")) return DDCSVD_MODE_BLOCKED_BF16X3;
+  }
+  return DDCSVD_MODE_BLOCKED_TF32X3;
+}
+
+// ---------------------------------------------------------------- small kernels
+__global__ void copy_pad_kernel(int m, int n, const float* __restrict__ A, int lda, float* W, int ldw) {
+  const int c = blockIdx.y;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ldw; r += gridDim.x * blockDim.x)
+    W[r + (size_t)c * ldw] = (r < m) ? A[r + (size_t)c * lda] : 0.f;
+}
+
+__global__ void sigma_out_kernel(int n, const double* s, float* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)s[i];
+}
+
+__global__ void zero_rows_kernel(int r0, int r1, int ncols, float* C, int ldc) {
+  const int c = blockIdx.y;
+  for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < r1; r += gridDim.x * blockDim.x)
+    C[r + (size_t)c * ldc] = 0.f;
+}
+
+__global__ void finite_check_kernel(int m, int n, const float* A, int lda, DevStatus* st) {
+  const size_t tot = (size_t)m * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = A[(i % m) + (i / m) * (size_t)lda];
+    if (!isfinite(v)) {
+      set_error(st, DDCSVD_ERR_NONFINITE, (int)(i % 2147483647));
+      return;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- pipeline
+struct Plan {
+  float *W, *d, *e, *tauq, *taup;
+  double *sig_slot, *sig;
+  char* blob;  // device copy of the bidiagonal preparation (see BdBlob)
+  BidiagWork bw;
+};
+
+// Prepared bidiagonal: split FP64 copy, block bounds per row and the D&C
+// node table, laid out identically in pinned host memory and on the device.
+struct BdBlob {
+  size_t off_b1, off_b2, off_lo, off_hi, off_ints, bytes;
+  static BdBlob layout(int N) {
+    BdBlob L;
+    size_t o = 0;
+    auto take = [&](size_t b) { o = (size_t)round_up((long long)o, 256); size_t r = o; o += b; return r; };
+    L.off_b1 = take(sizeof(double) * N);
+    L.off_b2 = take(sizeof(double) * N);
+    L.off_lo = take(sizeof(int) * N);
+    L.off_hi = take(sizeof(int) * N);
+    L.off_ints = take(sizeof(int) * dc_max_ints(N));
+    L.bytes = (size_t)round_up((long long)o, 256);
+    return L;
+  }
+};
+
+// Fills the pinned blob from host copies of the bidiagonal (a, b: N each; b is
+// split in place), builds the D&C forest and uploads the blob.  `eps` is the
+// precision the bidiagonal was computed in.
+static int prepare_bidiagonal(ddcsvd_context* ctx, int N, char* hblob, char* dblob, double eps, DcHost* H) {
+  const BdBlob L = BdBlob::layout(N);
+  double* a = (double*)(hblob + L.off_b1);
+  double* b = (double*)(hblob + L.off_b2);
+  int* lo = (int*)(hblob + L.off_lo);
+  int* hi = (int*)(hblob + L.off_hi);
+  std::vector<int> starts;
+  split_bidiagonal(N, a, b, eps, starts, lo, hi);
+  dc_build_host(N, starts, *H);
+  if (H->ints.size() > dc_max_ints(N)) {
+    set_last_error("D&C node table larger than its bound");
+    return DDCSVD_ERR_ARG;
+  }
+  memcpy(hblob + L.off_ints, H->ints.data(), sizeof(int) * H->ints.size());
+  const size_t used = L.off_ints + sizeof(int) * H->ints.size();
+  DDC_CUDA_TRY(cudaMemcpyAsync(dblob, hblob, used, cudaMemcpyHostToDevice, ctx->stream));
+  return DDCSVD_OK;
+}
+
+static int stage_event(ddcsvd_context* ctx, int k) {
+  if (ctx->timing) DDC_CUDA_TRY(cudaEventRecord(ctx->ev[k], ctx->stream));
+  return DDCSVD_OK;
+}
+
+// Full SVD of the m x n (m >= n) device matrix dA.  Workspace: region A
+// (matrix, bidiagonal, sigma) persists through the call; region B is scratch
+// reused by each stage in turn.
+static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
+                    int ldu, float* dV, int ldv, int mode, bool check_finite) {
+  const bool plain = (mode == DDCSVD_MODE_PLAIN_FP32);
+  const GemmKind kind = kind_of(mode);
+  const int P = bidiag_coop_ctas(ctx, m, n);
+  const int ldw = (int)round_up(m, 32);
+  const size_t gsc = gemm_scratch_bytes(kind, m, n, 2 * kPanel);
+  auto region_a = [&](Arena& a, Plan& pl) {
+    pl.W = a.take<float>((size_t)ldw * n);
+    pl.d = a.take<float>(n + 4);
+    pl.e = a.take<float>(n + 4);
+    pl.tauq = a.take<float>(n + 4);
+    pl.taup = a.take<float>(n + 4);
+    pl.sig_slot = a.take<double>(n + 4);
+    pl.sig = a.take<double>(n + 4);
+    pl.blob = a.take<char>(BdBlob::layout(n).bytes);
+  };
+  // ---- size
+  Plan pl;
+  size_t need;
+  {
+    Arena a;
+    region_a(a, pl);
+    Arena b1 = a;
+    plan_bidiag(b1, m, n, ldw, P, kind, &pl.bw);
+    b1.take<char>(gsc);
+    Arena b2 = a;
+    DDC_TRY(dc_sigma(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, b2, true));
+    Arena b3 = a;
+    DDC_TRY(bd_vectors(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, dV, ldv, dU, ldu, nullptr, b3, true));
+    Arena b4 = a;
+    DDC_TRY(apply_left_reflectors(ctx, m, n, nullptr, ldw, nullptr, dU, ldu, n, kind, plain, b4, true));
+    Arena b5 = a;
+    DDC_TRY(apply_right_reflectors(ctx, n, std::max(0, n - 2), nullptr, ldw, nullptr, dV, ldv, n, kind, plain, b5, true));
+    need = std::max(std::max(b1.off, b2.off), std::max(std::max(b3.off, b4.off), b5.off));
+  }
+  DDC_TRY(ensure_workspace(ctx, need + 4096));
+  Arena a;
+  a.plan = false;
+  a.base = (char*)ctx->ws;
+  region_a(a, pl);
+  // ---- stage 1
+  DDC_TRY(reset_status(ctx));
+  ctx->kused = 0;
+  DDC_TRY(stage_event(ctx, 0));
+  if (check_finite) {
+    finite_check_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(m, n, dA, lda, ctx->d_status);
+    count_launch();
+  }
+  copy_pad_kernel<<<dim3(ceil_div(ldw, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, pl.W, ldw);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  {
+    Arena b = a;
+    plan_bidiag(b, m, n, ldw, P, kind, &pl.bw);
+    Arena sc;
+    sc.base = b.take<char>(gsc);
+    sc.plan = false;
+    sc.cap = gsc;
+    if (plain) DDC_TRY(bidiag_plain(ctx, m, n, pl.W, ldw, pl.d, pl.e, pl.tauq, pl.taup, pl.bw));
+    else DDC_TRY(bidiag_blocked(ctx, m, n, pl.W, ldw, pl.d, pl.e, pl.tauq, pl.taup, pl.bw, kind, &sc));
+  }
+  DDC_TRY(stage_event(ctx, 1));
+  // ---- bidiagonal read-back: split at negligible superdiagonal entries and
+  //      build the D&C forest on the host (2n floats down, one blob up)
+  const BdBlob L = BdBlob::layout(n);
+  DcHost H;
+  {
+    const size_t rb = (size_t)round_up(sizeof(float) * 2 * (n + 4), 256);
+    DDC_TRY(ensure_pinned(ctx, rb + L.bytes));
+    float* hd = (float*)ctx->pinned;
+    float* he = hd + n + 4;
+    DDC_CUDA_TRY(cudaMemcpyAsync(hd, pl.d, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (n > 1)
+      DDC_CUDA_TRY(cudaMemcpyAsync(he, pl.e, sizeof(float) * (n - 1), cudaMemcpyDeviceToHost, ctx->stream));
+    DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    char* hb = (char*)ctx->pinned + rb;
+    double* a64 = (double*)(hb + L.off_b1);
+    double* b64 = (double*)(hb + L.off_b2);
+    for (int i = 0; i < n; i++) {
+      a64[i] = hd[i];
+      b64[i] = (i < n - 1) ? (double)he[i] : 0.0;  // beta[N-1] := 0 (square case)
+    }
+    DDC_TRY(prepare_bidiagonal(ctx, n, hb, pl.blob, FLT_EPSILON, &H));
+  }
+  const double* b1 = (const double*)(pl.blob + L.off_b1);
+  const double* b2 = (const double*)(pl.blob + L.off_b2);
+  const int* blo = (const int*)(pl.blob + L.off_lo);
+  const int* bhi = (const int*)(pl.blob + L.off_hi);
+  const int* dints = (const int*)(pl.blob + L.off_ints);
+  // ---- stage 2
+  {
+    Arena b = a;
+    DDC_TRY(dc_sigma(ctx, n, b1, b2, pl.sig_slot, &H, dints, b, false));
+  }
+  DDC_TRY(stage_event(ctx, 2));
+  // ---- stages 3-4: X straight into V, Y into the top of U (ascending order)
+  {
+    Arena b = a;
+    DDC_TRY(bd_vectors(ctx, n, b1, b2, pl.sig_slot, blo, bhi, dV, ldv, dU, ldu, pl.sig, b, false));
+  }
+  if (m > n) {
+    zero_rows_kernel<<<dim3(std::min(ceil_div(m - n, 256), 64), n), 256, 0, ctx->stream>>>(n, m, n, dU, ldu);
+    count_launch();
+  }
+  DDC_TRY(stage_event(ctx, 3));
+  // ---- stage 5
+  {
+    Arena b = a;
+    DDC_TRY(apply_left_reflectors(ctx, m, n, pl.W, ldw, pl.tauq, dU, ldu, n, kind, plain, b, false));
+    Arena c = a;
+    DDC_TRY(apply_right_reflectors(ctx, n, std::max(0, n - 2), pl.W, ldw, pl.taup, dV, ldv, n, kind, plain, c, false));
+  }
+  sigma_out_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(n, pl.sig, dS);
+  count_launch();
+  DDC_TRY(stage_event(ctx, 4));
+  DDC_CUDA_TRY(cudaGetLastError());
+  int rc = check_status(ctx, "svd");
+  if (ctx->timing && rc == DDCSVD_OK) {
+    for (int k = 0; k < 4; k++) cudaEventElapsedTime(&ctx->stage_ms[k], ctx->ev[k], ctx->ev[k + 1]);
+    ktimer_collect(ctx);
+  }
+  return rc;
+}
+
+__global__ void transpose_f32_kernel(int rows, int cols, const float* __restrict__ A, int lda, float* AT, int ldat) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int r = r0 + threadIdx.x, c = c0 + k;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? A[r + (size_t)c * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int c = c0 + threadIdx.x, r = r0 + k;
+    if (r < rows && c < cols) AT[c + (size_t)r * ldat] = tile[threadIdx.x][k];
+  }
+}
+
+static int svd_device(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
+                      int ldu, float* dV, int ldv, int mode, float* dAT_scratch) {
+  mode = resolve_mode(mode);
+  if (mode < DDCSVD_MODE_PLAIN_FP32 || mode > DDCSVD_MODE_BLOCKED_BF16X3) return DDCSVD_ERR_ARG;
+  if ((mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3) && !tc_available(ctx)) {
+    set_last_error("tensor-core mode requested but tcgen05 kernels are unavailable on this device");
+    return DDCSVD_ERR_UNSUPPORTED;
+  }
+  if (m >= n) return svd_core(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, true);
+  // m < n: SVD of A^T (n x m); U_A = V_{A^T}, V_A = U_{A^T}
+  transpose_f32_kernel<<<dim3(ceil_div(m, 32), ceil_div(n, 32)), dim3(32, 8), 0, ctx->stream>>>(m, n, dA, lda,
+                                                                                               dAT_scratch, n);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return svd_core(ctx, n, m, dAT_scratch, n, dS, dV, ldv, dU, ldu, mode, true);
+}
+
+}  // namespace ddcsvd
+
+using namespace ddcsvd;
+
+// ---------------------------------------------------------------- handles
+static std::mutex g_default_mu;
+static ddcsvd_context* g_default[64] = {nullptr};
+
+static int create_ctx(ddcsvd_context** out, int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_last_error("no CUDA device");
+    return DDCSVD_ERR_NODEVICE;
+  }
+  if (device < 0) DDC_CUDA_TRY(cudaGetDevice(&device));
+  if (device >= ndev) return DDCSVD_ERR_ARG;
+  DDC_CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  DDC_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) {
+    set_last_error("device %d is sm_%d%d; this library is built for sm_103a", device, prop.major, prop.minor);
+    return DDCSVD_ERR_NODEVICE;
+  }
+  ddcsvd_context* c = new ddcsvd_context();
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->own_stream = true;
+  DDC_CUDA_TRY(cudaMalloc(&c->d_status, sizeof(DevStatus)));
+  DDC_CUDA_TRY(cudaMallocHost(&c->h_status, sizeof(DevStatus)));
+  for (int k = 0; k < 5; k++) DDC_CUDA_TRY(cudaEventCreate(&c->ev[k]));
+  *out = c;
+  return DDCSVD_OK;
+}
+
+static int default_ctx(ddcsvd_context** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("no CUDA device");
+    return DDCSVD_ERR_NODEVICE;
+  }
+  std::lock_guard<std::mutex> g(g_default_mu);
+  if (dev < 0 || dev >= 64) return DDCSVD_ERR_ARG;
+  if (!g_default[dev]) DDC_TRY(create_ctx(&g_default[dev], dev));
+  *out = g_default[dev];
+  return DDCSVD_OK;
+}
+
+extern "C" {
+
+const char* ddcsvd_status_string(int s) {
+  switch (s) {
+    case DDCSVD_OK: return "ok";
+    case DDCSVD_ERR_ARG: return "invalid argument";
+    case DDCSVD_ERR_CUDA: return "CUDA error";
+    case DDCSVD_ERR_ALLOC: return "allocation failed";
+    case DDCSVD_ERR_NOCONV: return "iteration did not converge";
+    case DDCSVD_ERR_TIMEOUT: return "device wait timed out";
+    case DDCSVD_ERR_NODEVICE: return "no usable device";
+    case DDCSVD_ERR_NONFINITE: return "input holds NaN or Inf";
+    case DDCSVD_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* ddcsvd_last_error(void) { return t_last_error.c_str(); }
+
+long long ddcsvd_kernel_launch_count(void) { return __atomic_load_n(&g_launch_count, __ATOMIC_RELAXED); }
+
+int ddcsvd_create(ddcsvd_handle_t* handle, int device) {
+  if (!handle) return DDCSVD_ERR_ARG;
+  return create_ctx(handle, device);
+}
+
+int ddcsvd_destroy(ddcsvd_handle_t h) {
+  if (!h) return DDCSVD_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  if (h->ws) cudaFree(h->ws);
+  if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->d_status) cudaFree(h->d_status);
+  if (h->h_status) cudaFreeHost(h->h_status);
+  for (int k = 0; k < 5; k++) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return DDCSVD_OK;
+}
+
+int ddcsvd_set_stream(ddcsvd_handle_t h, void* stream) {
+  if (!h) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  if (h->own_stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+    h->own_stream = false;
+  }
+  // NULL selects the legacy default stream (what torch calls stream 0)
+  h->stream = (cudaStream_t)stream;
+  return DDCSVD_OK;
+}
+
+int ddcsvd_release_workspace(ddcsvd_handle_t h) {
+  if (!h) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  cudaStreamSynchronize(h->stream);
+  if (h->ws) cudaFree(h->ws);
+  h->ws = nullptr;
+  h->ws_bytes = 0;
+  return DDCSVD_OK;
+}
+
+int ddcsvd_set_stage_timing(ddcsvd_handle_t h, int enable) {
+  if (!h) return DDCSVD_ERR_ARG;
+  h->timing = enable != 0;
+  return DDCSVD_OK;
+}
+
+int ddcsvd_get_kernel_times(ddcsvd_handle_t h, float* ms, int* launches, int nclass) {
+  if (!h || !ms || nclass < 0) return DDCSVD_ERR_ARG;
+  for (int c = 0; c < nclass && c < 8; c++) {
+    ms[c] = h->kern_ms[c];
+    if (launches) launches[c] = h->kern_n[c];
+  }
+  return DDCSVD_OK;
+}
+
+int ddcsvd_get_stage_times(ddcsvd_handle_t h, float* ms4) {
+  if (!h || !ms4) return DDCSVD_ERR_ARG;
+  for (int k = 0; k < 4; k++) ms4[k] = h->stage_ms[k];
+  return DDCSVD_OK;
+}
+
+int ddcsvd_svd_f32_device(ddcsvd_handle_t h, int m, int n, const float* dA, int lda, float* dSigma,
+                          float* dU, int ldu, float* dV, int ldv, int mode) {
+  if (!h || m <= 0 || n <= 0 || !dA || !dSigma || !dU || !dV) return DDCSVD_ERR_ARG;
+  if (lda < m || ldu < m || ldv < n) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  float* at = nullptr;
+  if (m < n) {
+    // A^T scratch lives in its own allocation so the pipeline workspace stays intact
+    DDC_CUDA_TRY(cudaMallocAsync((void**)&at, sizeof(float) * (size_t)m * n, h->stream));
+  }
+  int rc = svd_device(h, m, n, dA, lda, dSigma, dU, ldu, dV, ldv, mode, at);
+  if (at) cudaFreeAsync(at, h->stream);
+  return rc;
+}
+
+static int bidiag_device(ddcsvd_context* h, int m, int n, float* dA, int lda, float* dD, float* dE,
+                         float* dTauq, float* dTaup, int mode) {
+  mode = resolve_mode(mode);
+  if ((mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3) && !tc_available(h))
+    return DDCSVD_ERR_UNSUPPORTED;
+  const GemmKind kind = kind_of(mode);
+  BidiagWork bw;
+  size_t scb = gemm_scratch_bytes(kind, m, n, 2 * kPanel);
+  char* sc = nullptr;
+  for (int pass = 0; pass < 2; pass++) {
+    Arena a;
+    a.plan = pass == 0;
+    a.base = (char*)h->ws;
+    plan_bidiag(a, m, n, lda, bidiag_coop_ctas(h, m, n), kind, &bw);
+    sc = a.take<char>(scb);
+    if (pass == 0) DDC_TRY(ensure_workspace(h, a.off + 4096));
+  }
+  DDC_TRY(reset_status(h));
+  Arena s;
+  s.base = sc;
+  s.plan = false;
+  s.cap = scb;
+  if (mode == DDCSVD_MODE_PLAIN_FP32) DDC_TRY(bidiag_plain(h, m, n, dA, lda, dD, dE, dTauq, dTaup, bw));
+  else DDC_TRY(bidiag_blocked(h, m, n, dA, lda, dD, dE, dTauq, dTaup, bw, kind, &s));
+  return check_status(h, "bidiag");
+}
+
+int ddcsvd_bidiag_f32_device(ddcsvd_handle_t h, int m, int n, float* dA, int lda, float* dD, float* dE,
+                             float* dTauq, float* dTaup, int mode) {
+  if (!h || m <= 0 || n <= 0 || m < n || lda < m || (lda % 4) != 0) return DDCSVD_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(dA) & 15) != 0) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  return bidiag_device(h, m, n, dA, lda, dD, dE, dTauq, dTaup, mode);
+}
+
+// Standalone stages 2-4 on a device FP64 bidiagonal: read it back, split it
+// (FP64 tolerance), build the forest, run D&C (and the vectors if asked).
+static int bd_standalone(ddcsvd_context* h, int N, const double* dB1, const double* dB2, bool square,
+                         const double* dSigmaIn, double* dSigmaOut, float* dX, float* dY) {
+  const BdBlob L = BdBlob::layout(N);
+  // workspace: blob + sigma (slot order) + max(D&C, vectors)
+  size_t need;
+  {
+    Arena a;
+    a.take<char>(L.bytes);
+    a.take<double>(N + 4);
+    Arena b = a, c = a;
+    DDC_TRY(dc_sigma(h, N, nullptr, nullptr, nullptr, nullptr, nullptr, b, true));
+    if (dX) DDC_TRY(bd_vectors(h, N, nullptr, nullptr, nullptr, nullptr, nullptr, dX, N, dY, N, nullptr, c, true));
+    need = std::max(b.off, c.off);
+  }
+  DDC_TRY(ensure_workspace(h, need + 4096));
+  Arena a;
+  a.plan = false;
+  a.base = (char*)h->ws;
+  char* blob = a.take<char>(L.bytes);
+  double* sig_slot = a.take<double>(N + 4);
+  DDC_TRY(ensure_pinned(h, L.bytes));
+  char* hb = (char*)h->pinned;
+  DDC_CUDA_TRY(cudaMemcpyAsync(hb + L.off_b1, dB1, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaMemcpyAsync(hb + L.off_b2, dB2, sizeof(double) * (square ? std::max(N - 1, 0) : N),
+                               cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  double* b64 = (double*)(hb + L.off_b2);
+  const double last = square ? 0.0 : b64[N - 1];
+  if (square) b64[N - 1] = 0.0;
+  DcHost H;
+  {
+    // split keeps the coupling to the extra column of an N x (N+1) bidiagonal
+    const BdBlob& LL = L;
+    double* a64 = (double*)(hb + LL.off_b1);
+    std::vector<int> starts;
+    split_bidiagonal(N, a64, b64, DBL_EPSILON, starts, (int*)(hb + LL.off_lo), (int*)(hb + LL.off_hi));
+    b64[N - 1] = last;
+    dc_build_host(N, starts, H);
+    memcpy(hb + LL.off_ints, H.ints.data(), sizeof(int) * H.ints.size());
+    DDC_CUDA_TRY(cudaMemcpyAsync(blob, hb, LL.off_ints + sizeof(int) * H.ints.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+  }
+  const double* b1 = (const double*)(blob + L.off_b1);
+  const double* b2 = (const double*)(blob + L.off_b2);
+  const int* blo = (const int*)(blob + L.off_lo);
+  const int* bhi = (const int*)(blob + L.off_hi);
+  const int* dints = (const int*)(blob + L.off_ints);
+  DDC_TRY(reset_status(h));
+  // node 0 is the first block's root; it spans all rows iff nothing split
+  const int root_rows = H.ints[H.nnodes];
+  const bool single = dSigmaIn != nullptr && root_rows == N;
+  if (dX && single) {
+    // one unreduced block: the caller's ascending sigma is already in slot order
+    DDC_CUDA_TRY(cudaMemcpyAsync(sig_slot, dSigmaIn, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    Arena b = a;
+    DDC_TRY(dc_sigma(h, N, b1, b2, sig_slot, &H, dints, b, false));
+  }
+  if (dX) {
+    Arena c = a;
+    DDC_TRY(bd_vectors(h, N, b1, b2, sig_slot, blo, bhi, dX, N, dY, N, dSigmaOut, c, false));
+  } else {
+    DDC_TRY(sort_values(h, N, sig_slot, dSigmaOut, a));
+  }
+  return check_status(h, dX ? "bdvec" : "bdsdc");
+}
+
+int ddcsvd_bdsdc_sigma_device(ddcsvd_handle_t h, int N, const double* dB1, const double* dB2, double* dSigma) {
+  if (!h || N <= 0 || !dB1 || !dB2 || !dSigma) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  return bd_standalone(h, N, dB1, dB2, false, nullptr, dSigma, nullptr, nullptr);
+}
+
+int ddcsvd_bdvec_device(ddcsvd_handle_t h, int N, const double* dA, const double* dB, const double* dSigma,
+                        float* dX, float* dY) {
+  if (!h || N <= 0 || !dA || !dB || !dSigma || !dX || !dY) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  double* scratch_sorted = nullptr;
+  DDC_CUDA_TRY(cudaMallocAsync((void**)&scratch_sorted, sizeof(double) * N, h->stream));
+  int rc = bd_standalone(h, N, dA, dB, true, dSigma, scratch_sorted, dX, dY);
+  cudaFreeAsync(scratch_sorted, h->stream);
+  return rc;
+}
+
+// ---------------------------------------------------------------- host-buffer API
+static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda, float* S, float* U, int ldu,
+                        float* V, int ldv, int mode) {
+  const int k = std::min(m, n);
+  float *dA = nullptr, *dS = nullptr, *dU = nullptr, *dV = nullptr;
+  const size_t na = (size_t)m * n, nu = (size_t)m * k, nv = (size_t)n * k;
+  DDC_CUDA_TRY(cudaMallocAsync((void**)&dA, sizeof(float) * (na + k + nu + nv + 64), h->stream));
+  dS = dA + na;
+  dU = dS + k;
+  dV = dU + nu;
+  int rc = DDCSVD_OK;
+  do {
+    if (lda == m) {
+      if (cudaMemcpyAsync(dA, A, sizeof(float) * na, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    } else {
+      if (cudaMemcpy2DAsync(dA, sizeof(float) * m, A, sizeof(float) * lda, sizeof(float) * m, n,
+                            cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    }
+    float* at = nullptr;
+    if (m < n && cudaMallocAsync((void**)&at, sizeof(float) * na, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+    rc = svd_device(h, m, n, dA, m, dS, dU, m, dV, n, mode, at);
+    if (at) cudaFreeAsync(at, h->stream);
+    if (rc != DDCSVD_OK) break;
+    if (cudaMemcpyAsync(S, dS, sizeof(float) * k, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    if (cudaMemcpy2DAsync(U, sizeof(float) * ldu, dU, sizeof(float) * m, sizeof(float) * m, k,
+                          cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    if (cudaMemcpy2DAsync(V, sizeof(float) * ldv, dV, sizeof(float) * n, sizeof(float) * n, k,
+                          cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+  } while (0);
+  cudaFreeAsync(dA, h->stream);
+  cudaStreamSynchronize(h->stream);
+  if (rc == DDCSVD_ERR_CUDA && t_last_error.empty()) set_last_error("CUDA copy failed");
+  return rc;
+}
+
+int ddcsvd_svd_f32(int m, int n, const float* A, int lda, float* sigma, float* U, int ldu, float* V, int ldv,
+                   int mode) {
+  if (m <= 0 || n <= 0 || !A || !sigma || !U || !V || lda < m || ldu < m || ldv < n) return DDCSVD_ERR_ARG;
+  ddcsvd_context* h;
+  DDC_TRY(default_ctx(&h));
+  std::lock_guard<std::mutex> g(h->mu);
+  return svd_host_f32(h, m, n, A, lda, sigma, U, ldu, V, ldv, mode);
+}
+
+int svd_gpu_ex(int m, int n, double* A, double* sigma, double* U, double* V, int mode) {
+  if (m <= 0 || n <= 0 || !A || !sigma || !U || !V) return DDCSVD_ERR_ARG;
+  ddcsvd_context* h;
+  DDC_TRY(default_ctx(&h));
+  std::lock_guard<std::mutex> g(h->mu);
+  const int k = std::min(m, n);
+  const size_t na = (size_t)m * n, nu = (size_t)m * k, nv = (size_t)n * k;
+  DDC_TRY(ensure_pinned(h, sizeof(float) * (na + k + nu + nv + 64)));
+  float* pa = (float*)h->pinned;
+  float* ps = pa + na;
+  float* pu = ps + k;
+  float* pv = pu + nu;
+  for (size_t i = 0; i < na; i++) pa[i] = (float)A[i];
+  int rc = svd_host_f32(h, m, n, pa, m, ps, pu, m, pv, n, mode);
+  if (rc != DDCSVD_OK) return rc;
+  for (int i = 0; i < k; i++) sigma[i] = ps[i];
+  for (size_t i = 0; i < nu; i++) U[i] = pu[i];
+  for (size_t i = 0; i < nv; i++) V[i] = pv[i];
+  return DDCSVD_OK;
+}
+
+void svd_gpu(int m, int n, double* A, double* sigma, double* U, double* V) {
+  int rc = svd_gpu_ex(m, n, A, sigma, U, V, DDCSVD_MODE_AUTO);
+  if (rc != DDCSVD_OK) {
+    fprintf(stderr, "svd_gpu: %s (%s)\n", ddcsvd_status_string(rc), ddcsvd_last_error());
+    if (sigma && m > 0 && n > 0)
+      for (int i = 0; i < std::min(m, n); i++) sigma[i] = __builtin_nan("");
+  }
+}
+
+void bidiag_par(int m, int n, double* A, double* alpha, double* beta) {
+  int rc = DDCSVD_OK;
+  ddcsvd_context* h = nullptr;
+  if (m <= 0 || n <= 0 || !A || !alpha || !beta || m < n) rc = DDCSVD_ERR_ARG;
+  if (rc == DDCSVD_OK) rc = default_ctx(&h);
+  if (rc == DDCSVD_OK) {
+    std::lock_guard<std::mutex> g(h->mu);
+    const int ldw = (int)round_up(m, 32);
+    const size_t na = (size_t)m * n;
+    float* dW = nullptr;
+    double* dOut = nullptr;
+    do {
+      if (cudaMallocAsync((void**)&dW, sizeof(float) * ((size_t)ldw * n + 4 * (size_t)n + 64), h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+      if (cudaMallocAsync((void**)&dOut, sizeof(double) * na, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+      float* dd = dW + (size_t)ldw * n;
+      float* de = dd + n;
+      float* tq = de + n;
+      float* tp = tq + n;
+      rc = ensure_pinned(h, sizeof(float) * na + sizeof(double) * na + 64);
+      if (rc) break;
+      float* pa = (float*)h->pinned;
+      for (size_t i = 0; i < na; i++) pa[i] = (float)A[i];
+      if (cudaMemsetAsync(dW, 0, sizeof(float) * (size_t)ldw * n, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      if (cudaMemcpy2DAsync(dW, sizeof(float) * ldw, pa, sizeof(float) * m, sizeof(float) * m, n,
+                            cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      rc = bidiag_device(h, m, n, dW, ldw, dd, de, tq, tp, DDCSVD_MODE_AUTO);
+      if (rc) break;
+      rc = export_reflectors(h, m, n, dW, ldw, dd, de, tq, tp, dOut);
+      if (rc) break;
+      double* po = (double*)((char*)h->pinned + round_up(sizeof(float) * na, 256));
+      float* pd = (float*)h->pinned;
+      if (cudaMemcpyAsync(po, dOut, sizeof(double) * na, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      if (cudaMemcpyAsync(pd, dd, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      if (cudaStreamSynchronize(h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      memcpy(A, po, sizeof(double) * na);
+      for (int i = 0; i < n; i++) alpha[i] = pd[i];
+      for (int i = 0; i < n - 1; i++) beta[i] = pd[n + i];
+    } while (0);
+    if (dW) cudaFreeAsync(dW, h->stream);
+    if (dOut) cudaFreeAsync(dOut, h->stream);
+    cudaStreamSynchronize(h->stream);
+  }
+  if (rc != DDCSVD_OK) {
+    fprintf(stderr, "bidiag_par: %s (%s)\n", ddcsvd_status_string(rc), ddcsvd_last_error());
+    for (int i = 0; m > 0 && n > 0 && i < std::min(m, n); i++) alpha[i] = __builtin_nan("");
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,703 @@
+// bidiag.cu -- stage 1: Householder Golub-Kahan bidiagonalisation (FP32).
+//
+// Replaces bidiag_par (bidiag_par.c:34-450) and its ten OpenCL kernels
+// (normsq_matcol/matrow, sum, update_scale_matcol/matrow, left/right_dotprods,
+// left/right_update_mat, sanders).  Same reflector convention as the reference
+// (bidiag.c:76-94): alpha_i = -sign(x_1) ||x||, sign(0) = +1, and a one-element
+// reflector flips the sign (H = -1).  Reflectors are kept in LAPACK form in
+// the working matrix (unit leading entry stored explicitly, scalar tau
+// separate); export_reflectors() rewrites them in the reference's normalised
+// form (H = I - 2 v v^T, ||v|| = 1).
+//
+// Two algorithms, both one persistent cooperative kernel per launch with a
+// bounded grid barrier:
+//
+//  * bidiag_panel_kernel (BLOCKED modes): LAPACK-labrd-style panel of kPanel
+//    columns.  Per column only the current column and row are updated; the
+//    trailing block is read twice (y = A^T u, x = A v) and updated once per
+//    panel by a rank-2*kPanel GEMM (tensor cores in the TF32X3/BF16X3 modes).
+//    Work split: rows are owned by CTAs for column-shaped work (column update,
+//    u scaling, x = A v, X), columns for row-shaped work (y = A^T u, Y, row
+//    update, v scaling).  Because the GEMVs are fed with the *unscaled*
+//    column/row (kept in xcol / xrow) and the reflector scale is applied
+//    algebraically, each column costs exactly two grid barriers.
+//
+//  * bidiag_plain_kernel (PLAIN_FP32): the reference's unblocked algorithm --
+//    rank-1 update of the trailing block after every reflector
+//    (left_update_mat.cl / right_update_mat.cl), fused with the dot products,
+//    also two grid barriers per column.
+//
+// Loads of data that other CTAs write during the kernel go through L2 only
+// (ld.global.cg) so that no SM reads a stale L1 line.
+#include "internal.hpp"
+
+namespace ddcsvd {
+
+constexpr int kPS = 2 * kPanel + 4;  // floats per partial-sum record
+
+struct PanelParams {
+  int m, n, k0, nb, ldw, ldn, P;
+  int rc, cc;  // rows / columns per CTA
+  float* W;
+  float *X, *Y, *VT;
+  float *d, *e, *tauq, *taup;
+  float *xcol, *xrow;
+  float *colpart, *rowpart;  // [P][kPS]
+  double *colnrm, *rownrm;   // [P]
+  GridBarrier* bar;
+  DevStatus* st;
+};
+
+__device__ __forceinline__ float sgn_ref(float x) { return x < 0.f ? -1.f : 1.f; }
+
+// Householder parameters for x = (x0, tail) with ||tail||^2 = t2 (FP64).
+__device__ __forceinline__ void householder(float x0, double t2, float* alpha, float* tau,
+                                            float* scale) {
+  double nrm = sqrt((double)x0 * (double)x0 + t2);
+  if (nrm == 0.0) {
+    *alpha = 0.f;
+    *tau = 0.f;
+    *scale = 0.f;
+    return;
+  }
+  double s = x0 < 0.f ? -1.0 : 1.0;
+  double a = -s * nrm;
+  *alpha = (float)a;
+  *tau = (float)((nrm + fabs((double)x0)) / nrm);
+  *scale = (float)(1.0 / ((double)x0 - a));
+}
+
+// sum_{r in [r0, r1)} col[r] * xs[r]; col in global (16B-aligned base), xs in
+// shared memory indexed absolutely.  Warp-cooperative, result in all lanes.
+__device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, const float* xs, int r0,
+                                              int r1, int lane) {
+  float acc = 0.f;
+  if (r1 <= r0) return 0.f;
+  int a0 = min(r1, (r0 + 3) & ~3);
+  int a1 = max(a0, r1 & ~3);
+  if (lane < a0 - r0) acc += __ldcg(col + r0 + lane) * xs[r0 + lane];
+  if (lane < r1 - a1) acc += __ldcg(col + a1 + lane) * xs[a1 + lane];
+  const float4* c4 = reinterpret_cast<const float4*>(col + a0);
+  const float4* x4 = reinterpret_cast<const float4*>(xs + a0);
+  const int nq = (a1 - a0) >> 2;
+  int q = lane;
+  for (; q + 96 < nq; q += 128) {
+    float4 w0 = __ldcg(c4 + q), w1 = __ldcg(c4 + q + 32), w2 = __ldcg(c4 + q + 64),
+           w3 = __ldcg(c4 + q + 96);
+    float4 v0 = x4[q], v1 = x4[q + 32], v2 = x4[q + 64], v3 = x4[q + 96];
+    acc += w0.x * v0.x + w0.y * v0.y + w0.z * v0.z + w0.w * v0.w;
+    acc += w1.x * v1.x + w1.y * v1.y + w1.z * v1.z + w1.w * v1.w;
+    acc += w2.x * v2.x + w2.y * v2.y + w2.z * v2.z + w2.w * v2.w;
+    acc += w3.x * v3.x + w3.y * v3.y + w3.z * v3.z + w3.w * v3.w;
+  }
+  for (; q < nq; q += 32) {
+    float4 w0 = __ldcg(c4 + q);
+    float4 v0 = x4[q];
+    acc += w0.x * v0.x + w0.y * v0.y + w0.z * v0.z + w0.w * v0.w;
+  }
+  return warp_sum(acc);
+}
+
+// Row-block GEMV: out[r - ra] = sum_{c in [c0, n)} W[r, c] * xs[c] for the
+// CTA's float4-aligned row block [ra, ra + 4*R4).  red: blockDim float4s.
+__device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int ldw, int ra,
+                                                int R4, int c0, int n, const float* xs,
+                                                float4* red, float* out) {
+  const int t = threadIdx.x;
+  const int G = blockDim.x / R4;
+  const int q = t % R4, g = t / R4;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (g < G) {
+    const float* base = W + ra + 4 * q;
+    int c = c0 + g;
+    for (; c + 3 * G < n; c += 4 * G) {
+      float4 w0 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)c * ldw));
+      float4 w1 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + G) * ldw));
+      float4 w2 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + 2 * G) * ldw));
+      float4 w3 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + 3 * G) * ldw));
+      float x0 = xs[c], x1 = xs[c + G], x2 = xs[c + 2 * G], x3 = xs[c + 3 * G];
+      acc.x += w0.x * x0 + w1.x * x1 + w2.x * x2 + w3.x * x3;
+      acc.y += w0.y * x0 + w1.y * x1 + w2.y * x2 + w3.y * x3;
+      acc.z += w0.z * x0 + w1.z * x1 + w2.z * x2 + w3.z * x3;
+      acc.w += w0.w * x0 + w1.w * x1 + w2.w * x2 + w3.w * x3;
+    }
+    for (; c < n; c += G) {
+      float4 w0 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)c * ldw));
+      float x0 = xs[c];
+      acc.x += w0.x * x0;
+      acc.y += w0.y * x0;
+      acc.z += w0.z * x0;
+      acc.w += w0.w * x0;
+    }
+  }
+  red[t] = acc;
+  __syncthreads();
+  if (t < 4 * R4) {
+    const int qq = t >> 2, comp = t & 3;
+    float s = 0.f;
+    for (int gg = 0; gg < G; gg++) {
+      float4 v = red[gg * R4 + qq];
+      s += comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
+    }
+    out[t] = s;
+  }
+  __syncthreads();
+}
+
+// Shared-memory layout of the panel kernel (floats unless noted).
+struct PanelSmem {
+  float* big;     // max(m, n) + 4: xcol / xrow by absolute index
+  float4* red;    // blockDim
+  float* own;     // rc: own rows' x (S1) / GEMV output (S6)
+  float* owncol;  // cc: own columns' updated row values
+  float* ypart;   // cc * 8: column dot partials
+  float *Yi, *VTi, *Wi, *Xi, *p1, *p2, *q1, *q2, *tot;
+  double* dred;   // 32
+  float* scal;    // 8
+};
+
+__device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc) {
+  PanelSmem s;
+  float* p = smem;
+  s.big = p;
+  p += round_up(bigsz + 4, 4);
+  s.red = reinterpret_cast<float4*>(p);
+  p += 4 * blockDim.x;
+  s.own = p;
+  p += round_up(rc + 4, 4);
+  s.owncol = p;
+  p += round_up(cc + 4, 4);
+  s.ypart = p;
+  p += round_up(cc * 8 + 4, 4);
+  s.Yi = p; p += kPanel + 4;
+  s.VTi = p; p += kPanel + 4;
+  s.Wi = p; p += kPanel + 4;
+  s.Xi = p; p += kPanel + 4;
+  s.p1 = p; p += kPanel + 4;
+  s.p2 = p; p += kPanel + 4;
+  s.q1 = p; p += kPanel + 4;
+  s.q2 = p; p += kPanel + 4;
+  s.tot = p; p += kPS + 4;
+  p = reinterpret_cast<float*>(round_up(reinterpret_cast<uintptr_t>(p), 16));
+  s.dred = reinterpret_cast<double*>(p);
+  p += 64;
+  s.scal = p;
+  return s;
+}
+
+size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads) {
+  size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) +
+             round_up(cc + 4, 4) + round_up(cc * 8 + 4, 4) + 8 * (kPanel + 4) + kPS + 4 + 4 + 64 + 8;
+  return f * sizeof(float) + 64;
+}
+
+__global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelParams p) {
+  extern __shared__ __align__(16) float smem[];
+  const int m = p.m, n = p.n, k0 = p.k0, ldw = p.ldw, ldn = p.ldn;
+  const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc);
+  float* W = p.W;
+  float *X = p.X, *Y = p.Y, *VT = p.VT;
+  // static partitions for this panel
+  const int rbase = k0 & ~3;
+  const int ra = rbase + b * p.rc, rb = min(m, ra + p.rc);
+  const int ca = k0 + 1 + b * p.cc, cb = min(n, ca + p.cc);
+  float prev_taup = 0.f;  // tau of the previous step's right reflector
+
+  for (int j = 0; j < p.nb; j++) {
+    const int i = k0 + j;
+    // ---------------- S1: update column i on own rows, partial sums
+    if (t < j) {
+      S.Yi[t] = __ldcg(Y + i + (size_t)t * ldn);
+      // VT[i, t]: row t of the panel's right reflectors at column i; the entry
+      // of the previous step (t = j-1) is its unit leading element.
+      S.VTi[t] = (t == j - 1) ? (prev_taup != 0.f ? 1.f : 0.f) : __ldcg(VT + i + (size_t)t * ldn);
+    }
+    __syncthreads();
+    const int r_s = max(ra, i);
+    const int nrow = max(0, rb - r_s);
+    for (int rr = t; rr < nrow; rr += blockDim.x) {
+      const int r = r_s + rr;
+      float x = __ldcg(W + r + (size_t)i * ldw);
+      for (int l = 0; l < j; l++)
+        x -= __ldcg(W + r + (size_t)(k0 + l) * ldw) * S.Yi[l] +
+             __ldcg(X + r + (size_t)l * ldw) * S.VTi[l];
+      S.own[rr] = x;
+      p.xcol[r] = x;
+    }
+    __syncthreads();
+    {
+      // partial sums over own rows r > i: [0] ||x||^2 (FP64), [1..j] W^T x, [1+j..2j] X^T x
+      const int r1 = max(r_s, i + 1);
+      for (int q = wid; q < 2 * j + 1; q += nw) {
+        if (q == 0) {
+          double acc = 0.0;
+          for (int r = r1 + lane; r < rb; r += 32) {
+            double x = S.own[r - r_s];
+            acc += x * x;
+          }
+          acc = warp_sum(acc);
+          if (lane == 0) p.colnrm[b] = acc;
+        } else {
+          const float* src = (q <= j) ? (W + (size_t)(k0 + q - 1) * ldw) : (X + (size_t)(q - 1 - j) * ldw);
+          float acc = 0.f;
+          for (int r = r1 + lane; r < rb; r += 32) acc += __ldcg(src + r) * S.own[r - r_s];
+          acc = warp_sum(acc);
+          if (lane == 0) p.colpart[(size_t)b * kPS + q] = acc;
+        }
+      }
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 1)) return;
+
+    // ---------------- S2: column reflector
+    if (t < 2 * j + 1) {
+      if (t == 0) {
+        double acc = 0.0;
+        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.colnrm + bb);
+        S.dred[0] = acc;
+      } else {
+        float acc = 0.f;
+        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.colpart + (size_t)bb * kPS + t);
+        S.tot[t] = acc;
+      }
+    }
+    if (t < j) {
+      S.Wi[t] = __ldcg(W + i + (size_t)(k0 + t) * ldw);
+      S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
+    }
+    __syncthreads();
+    if (t == 0) {
+      float x0 = __ldcg(p.xcol + i), alpha, tau, scale;
+      householder(x0, S.dred[0], &alpha, &tau, &scale);
+      S.scal[0] = alpha;
+      S.scal[1] = tau;
+      S.scal[2] = scale;
+      if (b == 0) {
+        p.d[i] = alpha;
+        p.tauq[i] = tau;
+      }
+    }
+    __syncthreads();
+    const float tq = S.scal[1], sq = S.scal[2];
+    if (t < j) {
+      S.p1[t] = S.Wi[t] + sq * S.tot[1 + t];
+      S.p2[t] = S.Xi[t] + sq * S.tot[1 + j + t];
+    }
+    for (int rr = t; rr < nrow; rr += blockDim.x) {
+      const int r = r_s + rr;
+      W[r + (size_t)i * ldw] = (r == i) ? 1.f : S.own[rr] * sq;
+    }
+    if (i == n - 1) break;  // last column: no right reflector
+    // ---------------- S3: y = A^T u on own columns, Y column j, row-i update
+    {
+      // stage the unscaled column into shared memory
+      for (int r = i + 1 + t; r < m; r += blockDim.x) S.big[r] = __ldcg(p.xcol + r);
+      __syncthreads();
+      const int c_s = max(ca, i + 1);
+      const int ncol = max(0, cb - c_s);
+      if (ncol > 0) {
+        int segs = min(8, max(1, nw / ncol));
+        const int len = m - (i + 1);
+        const int seglen = (int)round_up(ceil_div(max(len, 1), segs), 4);
+        for (int item = wid; item < ncol * segs; item += nw) {
+          const int cl = item / segs, sg = item % segs;
+          const int r0 = i + 1 + sg * seglen, r1 = min(m, r0 + seglen);
+          float v = warp_dot_col(W + (size_t)(c_s + cl) * ldw, S.big, r0, r1, lane);
+          if (lane == 0) S.ypart[cl * 8 + sg] = v;
+        }
+        __syncthreads();
+        for (int cl = t; cl < ncol; cl += blockDim.x) {
+          const int c = c_s + cl;
+          float ydot = 0.f;
+          for (int sg = 0; sg < segs; sg++) ydot += S.ypart[cl * 8 + sg];
+          const float wic = __ldcg(W + i + (size_t)c * ldw);
+          float yv = wic + sq * ydot;
+          for (int l = 0; l < j; l++)
+            yv -= __ldcg(Y + c + (size_t)l * ldn) * S.p1[l] + __ldcg(VT + c + (size_t)l * ldn) * S.p2[l];
+          const float ycj = tq * yv;
+          Y[c + (size_t)j * ldn] = ycj;
+          float w = wic - ycj;
+          for (int l = 0; l < j; l++)
+            w -= __ldcg(Y + c + (size_t)l * ldn) * S.Wi[l] + __ldcg(VT + c + (size_t)l * ldn) * S.Xi[l];
+          S.owncol[cl] = w;
+          p.xrow[c] = w;
+        }
+      } else {
+        __syncthreads();
+      }
+      __syncthreads();
+      // partials over own columns c > i+1: [0] ||w||^2, [1..j+1] Y^T w, [j+2..2j+1] VT^T w
+      const int c1 = max(c_s, i + 2);
+      for (int q = wid; q < 2 * j + 2; q += nw) {
+        if (q == 0) {
+          double acc = 0.0;
+          for (int c = c1 + lane; c < cb; c += 32) {
+            double w = S.owncol[c - c_s];
+            acc += w * w;
+          }
+          acc = warp_sum(acc);
+          if (lane == 0) p.rownrm[b] = acc;
+        } else {
+          const float* src = (q <= j + 1) ? (Y + (size_t)(q - 1) * ldn) : (VT + (size_t)(q - j - 2) * ldn);
+          float acc = 0.f;
+          for (int c = c1 + lane; c < cb; c += 32) acc += __ldcg(src + c) * S.owncol[c - c_s];
+          acc = warp_sum(acc);
+          if (lane == 0) p.rowpart[(size_t)b * kPS + q] = acc;
+        }
+      }
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 2)) return;
+
+    // ---------------- S5: row reflector
+    if (t < 2 * j + 2) {
+      if (t == 0) {
+        double acc = 0.0;
+        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.rownrm + bb);
+        S.dred[0] = acc;
+      } else {
+        float acc = 0.f;
+        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.rowpart + (size_t)bb * kPS + t);
+        S.tot[t] = acc;
+      }
+    }
+    __syncthreads();
+    if (t == 0) {
+      float x0 = __ldcg(p.xrow + i + 1), beta, tau, scale;
+      if (i < n - 2) {
+        householder(x0, S.dred[0], &beta, &tau, &scale);
+      } else {  // one element left: no reflection (bidiag.c:125-129)
+        beta = x0;
+        tau = 0.f;
+        scale = 0.f;
+      }
+      S.scal[3] = beta;
+      S.scal[4] = tau;
+      S.scal[5] = scale;
+      if (b == 0) {
+        p.e[i] = beta;
+        p.taup[i] = tau;
+      }
+    }
+    __syncthreads();
+    const float tp = S.scal[4], sp = S.scal[5];
+    prev_taup = tp;
+    if (t <= j) S.q1[t] = __ldcg(Y + i + 1 + (size_t)t * ldn) + sp * S.tot[1 + t];
+    if (t < j) S.q2[t] = __ldcg(VT + i + 1 + (size_t)t * ldn) + sp * S.tot[j + 2 + t];
+    {
+      const int c_s = max(ca, i + 1);
+      for (int c = c_s + t; c < cb; c += blockDim.x) {
+        float v;
+        if (c == i + 1) v = (tp != 0.f) ? 1.f : 0.f;
+        else v = S.owncol[c - c_s] * sp;
+        W[i + (size_t)c * ldw] = v;
+        VT[c + (size_t)j * ldn] = v;
+      }
+    }
+    // stage the unscaled row for x = A v
+    for (int c = i + 2 + t; c < n; c += blockDim.x) S.big[c] = __ldcg(p.xrow + c);
+    __syncthreads();
+    // ---------------- S6: x = A v on own rows, X column j
+    {
+      const int r_lo = max(ra, i + 1);
+      if (rb > r_lo) {
+        const int R4 = (rb - ra + 3) >> 2;
+        if (tp != 0.f) {
+          block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
+        } else {
+          __syncthreads();
+          __syncthreads();
+        }
+        for (int r = r_lo + t; r < rb; r += blockDim.x) {
+          float xv = 0.f;
+          if (tp != 0.f) {
+            float tv = __ldcg(W + r + (size_t)(i + 1) * ldw) + sp * S.own[r - ra];
+            tv -= __ldcg(W + r + (size_t)i * ldw) * S.q1[j];
+            for (int l = 0; l < j; l++)
+              tv -= __ldcg(W + r + (size_t)(k0 + l) * ldw) * S.q1[l] +
+                    __ldcg(X + r + (size_t)l * ldw) * S.q2[l];
+            xv = tp * tv;
+          }
+          X[r + (size_t)j * ldw] = xv;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------
+// Plain (unblocked) kernel: the whole bidiagonalisation in one launch.
+// ------------------------------------------------------------------------
+struct PlainParams {
+  int m, n, ldw, P, rc, cc;
+  float* W;
+  float *d, *e, *tauq, *taup;
+  float *xcol, *xrow;
+  double *colnrm, *rownrm;
+  GridBarrier* bar;
+  DevStatus* st;
+};
+
+__global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_plain_kernel(PlainParams p) {
+  extern __shared__ __align__(16) float smem[];
+  const int m = p.m, n = p.n, ldw = p.ldw;
+  const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  float* big = smem;
+  float4* red = reinterpret_cast<float4*>(big + round_up(max(m, n) + 4, 4));
+  float* own = reinterpret_cast<float*>(red + blockDim.x);
+  float* owncol = own + round_up(p.rc + 4, 4);
+  double* dred = reinterpret_cast<double*>(
+      round_up(reinterpret_cast<uintptr_t>(owncol + round_up(p.cc + 4, 4)), 16));
+  float* scal = reinterpret_cast<float*>(dred + 32);
+  float* W = p.W;
+  // fixed partitions for the whole factorisation
+  const int ra = b * p.rc, rb = min(m, ra + p.rc);
+  const int ca = 1 + b * p.cc, cb = min(n, ca + p.cc);
+  // column 0 partials (the fused tail of S6 provides them for later columns)
+  {
+    const int r_s = max(ra, 0);
+    double acc = 0.0;
+    for (int r = r_s + t; r < rb; r += blockDim.x) {
+      float x = __ldcg(W + r);
+      p.xcol[r] = x;
+      if (r > 0) acc += (double)x * x;
+    }
+    acc = block_sum(acc, dred);
+    if (t == 0) p.colnrm[b] = acc;
+  }
+  if (!grid_sync(p.bar, p.P, p.st, 11)) return;
+  for (int i = 0; i < n; i++) {
+    // ---------------- column reflector
+    if (t == 0) {
+      double acc = 0.0;
+      for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.colnrm + bb);
+      float alpha, tau, scale;
+      householder(__ldcg(p.xcol + i), acc, &alpha, &tau, &scale);
+      scal[0] = alpha;
+      scal[1] = tau;
+      scal[2] = scale;
+      if (b == 0) {
+        p.d[i] = alpha;
+        p.tauq[i] = tau;
+      }
+    }
+    __syncthreads();
+    const float tq = scal[1], sq = scal[2];
+    for (int r = max(ra, i) + t; r < rb; r += blockDim.x)
+      W[r + (size_t)i * ldw] = (r == i) ? 1.f : __ldcg(p.xcol + r) * sq;
+    if (i == n - 1) break;
+    // ---------------- left update of own columns (left_dotprods + left_update_mat)
+    for (int r = i + 1 + t; r < m; r += blockDim.x) big[r] = __ldcg(p.xcol + r) * sq;
+    if (t == 0) big[i] = 1.f;
+    __syncthreads();
+    {
+      const int c_s = max(ca, i + 1);
+      for (int c = c_s + wid; c < cb; c += nw) {
+        float* col = W + (size_t)c * ldw;
+        float wv = warp_dot_col(col, big, i, m, lane);
+        const float f = tq * wv;
+        for (int r = i + lane; r < m; r += 32) col[r] = __ldcg(col + r) - f * big[r];
+        __syncwarp();
+        if (lane == 0) {
+          float v = __ldcg(col + i);
+          owncol[c - c_s] = v;
+          p.xrow[c] = v;
+        }
+      }
+      __syncthreads();
+      double acc = 0.0;
+      for (int c = max(c_s, i + 2) + t; c < cb; c += blockDim.x) {
+        double v = owncol[c - c_s];
+        acc += v * v;
+      }
+      acc = block_sum(acc, dred);
+      if (t == 0) p.rownrm[b] = acc;
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 12)) return;
+    // ---------------- row reflector
+    if (t == 0) {
+      double acc = 0.0;
+      for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.rownrm + bb);
+      float x0 = __ldcg(p.xrow + i + 1), beta, tau, scale;
+      if (i < n - 2) householder(x0, acc, &beta, &tau, &scale);
+      else { beta = x0; tau = 0.f; scale = 0.f; }
+      scal[3] = beta;
+      scal[4] = tau;
+      scal[5] = scale;
+      if (b == 0) {
+        p.e[i] = beta;
+        p.taup[i] = tau;
+      }
+    }
+    __syncthreads();
+    const float tp = scal[4], sp = scal[5];
+    for (int c = max(ca, i + 1) + t; c < cb; c += blockDim.x)
+      W[i + (size_t)c * ldw] = (c == i + 1) ? (tp != 0.f ? 1.f : 0.f) : __ldcg(p.xrow + c) * sp;
+    for (int c = i + 2 + t; c < n; c += blockDim.x) big[c] = __ldcg(p.xrow + c) * sp;
+    if (t == 0) big[i + 1] = 1.f;
+    __syncthreads();
+    // ---------------- right update of own rows (right_dotprods + right_update_mat)
+    const int r_lo = max(ra, i + 1);
+    double nacc = 0.0;
+    if (rb > r_lo) {
+      const int R4 = (rb - ra + 3) >> 2;
+      if (tp != 0.f) {
+        block_rows_gemv(W, ldw, ra, R4, i + 1, n, big, red, own);
+        // own[r - ra] = sum_{c > i} W[r,c] v_c ; W[r, c] -= tp * own * v_c
+        const int cols = n - (i + 1);
+        for (int idx = t; idx < cols * (rb - r_lo); idx += blockDim.x) {
+          const int cl = idx / (rb - r_lo), rr = idx % (rb - r_lo);
+          const int r = r_lo + rr, c = i + 1 + cl;
+          float* a = W + r + (size_t)c * ldw;
+          *a = __ldcg(a) - tp * own[r - ra] * big[c];
+        }
+        __syncthreads();
+      } else {
+        __syncthreads();
+        __syncthreads();
+      }
+      // fused: next column's partial norm on own rows
+      for (int r = r_lo + t; r < rb; r += blockDim.x) {
+        float x = __ldcg(W + r + (size_t)(i + 1) * ldw);
+        p.xcol[r] = x;
+        if (r > i + 1) nacc += (double)x * x;
+      }
+    }
+    nacc = block_sum(nacc, dred);
+    if (t == 0) p.colnrm[b] = nacc;
+    if (!grid_sync(p.bar, p.P, p.st, 13)) return;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Reflector export to the reference's storage (bidiag_par.c:63-68).
+// ------------------------------------------------------------------------
+__global__ void export_reflectors_kernel(int m, int n, const float* __restrict__ W, int ldw,
+                                         const float* d, const float* e, const float* tauq,
+                                         const float* taup, double* out) {
+  const int c = blockIdx.x;
+  for (int r = threadIdx.x; r < m; r += blockDim.x) {
+    double v = 0.0;
+    const float w = W[r + (size_t)c * ldw];
+    if (r >= c) {  // left reflector c
+      const float a = d[c], tq = tauq[c];
+      double f = (a < 0.f ? 1.0 : -1.0) * sqrt(0.5 * (double)tq);
+      v = f * (double)w;
+      if (tq == 0.f) v = (r == c) ? 0.0 : 0.0;
+    } else if (r == c - 1) {  // leading entry of right reflector r (or the no-reflect zero)
+      const float tp = taup[r];
+      v = (tp == 0.f) ? 0.0 : (e[r] < 0.f ? 1.0 : -1.0) * sqrt(0.5 * (double)tp) * (double)w;
+    } else {  // r < c - 1: right reflector r
+      const float tp = taup[r];
+      v = (tp == 0.f) ? 0.0 : (e[r] < 0.f ? 1.0 : -1.0) * sqrt(0.5 * (double)tp) * (double)w;
+    }
+    out[r + (size_t)c * m] = v;
+  }
+}
+
+// ------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------
+int bidiag_coop_ctas(ddcsvd_context* ctx, int m, int n) {
+  (void)m;
+  (void)n;
+  return ctx->num_sms;
+}
+
+void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWork* w) {
+  w->ldn = (int)round_up(n, 32);
+  w->P = P;
+  w->X = a.take<float>((size_t)ldw * kPanel);
+  w->Y = a.take<float>((size_t)w->ldn * kPanel);
+  w->VT = a.take<float>((size_t)w->ldn * kPanel);
+  w->xcol = a.take<float>(ldw + 4);
+  w->xrow = a.take<float>(w->ldn + 4);
+  w->colpart = a.take<float>((size_t)P * kPS + 2 * P);
+  w->rowpart = a.take<float>((size_t)P * kPS + 2 * P);
+  w->bar = a.take<GridBarrier>(4);
+  w->gemm_scratch = a.take<char>(gemm_scratch_bytes(kind, m, n, 2 * kPanel));
+}
+
+static int launch_coop(const void* fn, int P, int threads, size_t smem, void* args,
+                       cudaStream_t s) {
+  DDC_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  void* argv[] = {args};
+  DDC_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads), argv, smem, s));
+  count_launch();
+  return DDCSVD_OK;
+}
+
+int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,
+                   float* tauq, float* taup, BidiagWork& w, GemmKind kind, Arena* scratch) {
+  if (m < n || n <= 0) return DDCSVD_ERR_ARG;
+  const int P = w.P;
+  for (int k0 = 0; k0 < n; k0 += kPanel) {
+    const int nb = std::min(kPanel, n - k0);
+    PanelParams pp;
+    pp.m = m; pp.n = n; pp.k0 = k0; pp.nb = nb; pp.ldw = ldw; pp.ldn = w.ldn; pp.P = P;
+    pp.rc = (int)round_up(ceil_div(m - (k0 & ~3), P), 4);
+    pp.cc = std::max(1, ceil_div(n - k0 - 1, P));
+    pp.W = W; pp.X = w.X; pp.Y = w.Y; pp.VT = w.VT;
+    pp.d = d; pp.e = e; pp.tauq = tauq; pp.taup = taup;
+    pp.xcol = w.xcol; pp.xrow = w.xrow;
+    pp.colpart = w.colpart; pp.rowpart = w.rowpart;
+    pp.colnrm = reinterpret_cast<double*>(w.colpart + (size_t)P * kPS);
+    pp.rownrm = reinterpret_cast<double*>(w.rowpart + (size_t)P * kPS);
+    // colnrm / rownrm live after the float records: make them 8-byte aligned
+    pp.colnrm = reinterpret_cast<double*>(round_up(reinterpret_cast<uintptr_t>(pp.colnrm), 8));
+    pp.rownrm = reinterpret_cast<double*>(round_up(reinterpret_cast<uintptr_t>(pp.rownrm), 8));
+    pp.bar = w.bar;
+    pp.st = ctx->d_status;
+    DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
+    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads);
+    ktimer_begin(ctx, KC_BIDIAG);
+    DDC_TRY(launch_coop((const void*)bidiag_panel_kernel, P, kBidiagThreads, smem, &pp, ctx->stream));
+    ktimer_end(ctx);
+    const int kn = k0 + nb;
+    if (kn < n) {
+      // W[kn:m, kn:n] -= U_p Y^T + X VT^T   (rank-2*nb update)
+      const int M = m - kn, N = n - kn;
+      Mat A1{W + kn + (size_t)k0 * ldw, 1, ldw};
+      Mat B1{w.Y + kn, w.ldn, 1};  // B1(k, c) = Y[kn + c, k]
+      Mat A2{w.X + kn, 1, ldw};
+      Mat B2{w.VT + kn, w.ldn, 1};
+      ktimer_begin(ctx, KC_TRAIL_GEMM);
+      DDC_TRY(gemm(ctx, kind, M, N, nb, A1, B1, nb, A2, B2, -1.f, 1.f, W + kn + (size_t)kn * ldw,
+                   ldw, scratch));
+      ktimer_end(ctx);
+    }
+  }
+  return DDCSVD_OK;
+}
+
+int bidiag_plain(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,
+                 float* tauq, float* taup, BidiagWork& w) {
+  if (m < n || n <= 0) return DDCSVD_ERR_ARG;
+  PlainParams pp;
+  pp.m = m; pp.n = n; pp.ldw = ldw; pp.P = w.P;
+  pp.rc = (int)round_up(ceil_div(m, w.P), 4);
+  pp.cc = std::max(1, ceil_div(n - 1, w.P));
+  pp.W = W; pp.d = d; pp.e = e; pp.tauq = tauq; pp.taup = taup;
+  pp.xcol = w.xcol; pp.xrow = w.xrow;
+  pp.colnrm = reinterpret_cast<double*>(round_up(reinterpret_cast<uintptr_t>(w.colpart), 8));
+  pp.rownrm = reinterpret_cast<double*>(round_up(reinterpret_cast<uintptr_t>(w.rowpart), 8));
+  pp.bar = w.bar;
+  pp.st = ctx->d_status;
+  DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
+  size_t smem = (round_up(std::max(m, n) + 4, 4) + 4 * kBidiagThreads + round_up(pp.rc + 4, 4) +
+                 round_up(pp.cc + 4, 4) + 4 + 64 + 16) * sizeof(float) + 64;
+  ktimer_begin(ctx, KC_BIDIAG);
+  int rc = launch_coop((const void*)bidiag_plain_kernel, w.P, kBidiagThreads, smem, &pp, ctx->stream);
+  ktimer_end(ctx);
+  return rc;
+}
+
+int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw, const float* d,
+                      const float* e, const float* tauq, const float* taup, double* A_out) {
+  export_reflectors_kernel<<<n, 256, 0, ctx->stream>>>(m, n, W, ldw, d, e, tauq, taup, A_out);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+}  // namespace ddcsvd

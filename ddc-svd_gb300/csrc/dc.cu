@@ -1,0 +1,638 @@
+// dc.cu -- stage 2: double divide-and-conquer singular values (FP64).
+//
+// Replaces GetSingularValues_Parallel / DivideAndConquer_Parallel
+// (Calculations-Parallel.c:706-874).  The recursion tree is the reference's:
+// an N x (N+1) upper bidiagonal node splits at K = N/2 into a K x (K+1) and an
+// (N-K-1) x (N-K) child (:731-750); leaves have N <= 2 (:722-726).  A merge
+// forms z from the children's last/first right-vector rows and the rotation
+// (r0, c0, s0) of their null vectors (:769-782), solves the secular equation
+// for the new singular values (:48-348) and, unless it is the root,
+// recomputes z-hat (Gu-Eisenstat) and the first/last rows of the merged right
+// vectors for its parent (:351-588), then normalises them with phi/psi
+// (:807-845).
+//
+// GB300 layout: one cooperative persistent kernel walks the tree bottom-up,
+// one depth at a time, with five bounded grid barriers per depth:
+//   P1  leaves (thread each) and merge set-up (CTA per node): parallel merge
+//       of the children's sorted values, deflation, compaction;
+//   P2  secular roots, one warp per root, lanes split the O(N) sums;
+//   P3  z-hat, one warp per component, lanes split the O(N) product;
+//   P4  merged first/last rows, one warp per root;
+//   P5  merge of roots and deflated values into ascending order, row
+//       normalisation (CTA per node).
+// Nodes of one depth own disjoint slot ranges, so every per-node array is
+// indexed by slot and lives in one N-element buffer; outputs ping-pong
+// between two buffers by depth parity.
+//
+// Deliberate differences from the reference (shared with the FP64 oracle):
+// roots are iterated to full FP64 accuracy with a two-pole rational model
+// (middle way) inside a bisection bracket, differences d_j^2 - sigma_i^2 are
+// formed from the nearer pole without cancellation, z-hat uses products
+// instead of logs, sign(z-hat_j) = sign(z_j), tiny z_j and equal d_j deflate,
+// and every iteration is capped.
+#include <algorithm>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace ddcsvd {
+
+constexpr int kDcThreads = 512;
+constexpr int kSecMaxIt = 80;
+
+struct DcParams {
+  int N, nnodes, maxdepth, P;
+  const int* nd_r0;
+  const int* nd_nn;
+  const int* nd_slot;
+  const int* nd_K;
+  const int* nd_c1;
+  const int* nd_c2;
+  const int* depth_start;  // [maxdepth + 2]
+  const int* depth_merge;  // merge-node ids sorted by depth then slot
+  const int* dm_start;     // [maxdepth + 2] ranges into depth_merge
+  const double* b1;
+  const double* b2;
+  double* sig[2];
+  double* F[2];
+  double* L[2];
+  double *ds, *zs, *hfs, *hls;
+  double *dq, *zq, *fq, *lq;
+  double *dd, *fd, *ld;  // deflated entries (ascending d)
+  double *tau, *zh, *rS, *rF, *rL;
+  int* org;
+  int* defl;
+  int* nq;
+  double *zz, *phi, *psi;
+  double* out;
+  GridBarrier* bar;
+  DevStatus* st;
+};
+
+// ---------------------------------------------------------------- leaves
+__device__ void dc_leaf(int nn, const double* b1, const double* b2, double* sig, double* fr,
+                        double* lr, double* phi, double* psi) {
+  if (nn == 1) {
+    double s = hypot(b1[0], b2[0]);
+    sig[0] = s;
+    if (s > 0.0) {
+      fr[0] = b1[0] / s; lr[0] = b2[0] / s; *phi = b2[0] / s; *psi = -b1[0] / s;
+    } else {
+      fr[0] = 1.0; lr[0] = 0.0; *phi = 0.0; *psi = 1.0;
+    }
+    return;
+  }
+  const double x1 = b1[0], x2 = b2[0], x3 = b1[1], x4 = b2[1];
+  const double a = x1 * x1 + x2 * x2, e = x3 * x3 + x4 * x4, c = x2 * x3;
+  const double det = x1 * x1 * x3 * x3 + x1 * x1 * x4 * x4 + x2 * x2 * x4 * x4;
+  const double rad = hypot(0.5 * (a - e), c);
+  const double lmax = 0.5 * (a + e) + rad;
+  const double lmin = (lmax > 0.0) ? det / lmax : 0.0;
+  const double lam[2] = {lmin, lmax};
+  for (int k = 0; k < 2; k++) {
+    sig[k] = sqrt(lam[k]);
+    double u1a = c, u2a = lam[k] - a, u1b = lam[k] - e, u2b = c;
+    double na = hypot(u1a, u2a), nb = hypot(u1b, u2b), u1, u2;
+    if (na >= nb && na > 0.0) { u1 = u1a / na; u2 = u2a / na; }
+    else if (nb > 0.0) { u1 = u1b / nb; u2 = u2b / nb; }
+    else { u1 = (k == 0) ? 0.0 : 1.0; u2 = (k == 0) ? 1.0 : 0.0; }
+    double v1 = x1 * u1, v2 = x2 * u1 + x3 * u2, v3 = x4 * u2;
+    double nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    if (nv > 0.0) { fr[k] = v1 / nv; lr[k] = v3 / nv; }
+    else { fr[k] = (k == 0) ? 1.0 : 0.0; lr[k] = 0.0; }
+  }
+  double n1 = x2 * x4, n2 = -x1 * x4, n3 = x1 * x3;
+  double nn3 = sqrt(n1 * n1 + n2 * n2 + n3 * n3);
+  if (nn3 > 0.0) { *phi = n1 / nn3; *psi = n3 / nn3; }
+  else { *phi = 0.0; *psi = 1.0; }
+}
+
+// ---------------------------------------------------------------- block helpers
+// Exclusive scan of per-thread counts; returns this thread's offset, total in *tot.
+__device__ int block_exscan(int v, int* sh, int* tot) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (t == 0) {
+    int acc = 0;
+    for (int w = 0; w < nw; w++) { int s = sh[w]; sh[w] = acc; acc += s; }
+    sh[nw] = acc;
+  }
+  __syncthreads();
+  int r = sh[wid] + x - v;
+  *tot = sh[nw];
+  __syncthreads();
+  return r;
+}
+
+__device__ double block_max(double v, double* sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < nw; w++) r = fmax(r, sh[w]);
+  __syncthreads();
+  return r;
+}
+
+__device__ double block_sumd(double v, double* sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < nw; w++) r += sh[w];
+  __syncthreads();
+  return r;
+}
+
+// number of a[0..n) < v (strict) or <= v
+__device__ __forceinline__ int count_lt(const double* a, int n, double v) {
+  int lo = 0, hi = n;
+  while (lo < hi) { int mid = (lo + hi) >> 1; if (a[mid] < v) lo = mid + 1; else hi = mid; }
+  return lo;
+}
+__device__ __forceinline__ int count_le(const double* a, int n, double v) {
+  int lo = 0, hi = n;
+  while (lo < hi) { int mid = (lo + hi) >> 1; if (a[mid] <= v) lo = mid + 1; else hi = mid; }
+  return lo;
+}
+
+// ---------------------------------------------------------------- P1 merge set-up
+__device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, double* shd) {
+  const int t = threadIdx.x;
+  const int nn = p.nd_nn[node], slot = p.nd_slot[node], K = p.nd_K[node], r0 = p.nd_r0[node];
+  const int c1 = p.nd_c1[node], c2 = p.nd_c2[node];
+  const int n1 = K, n2 = nn - K - 1;
+  const int cp = par ^ 1;
+  const double* s1 = p.sig[cp] + slot + 1;
+  const double* f1 = p.F[cp] + slot + 1;
+  const double* l1 = p.L[cp] + slot + 1;
+  const double* s2 = p.sig[cp] + slot + K + 1;
+  const double* f2 = p.F[cp] + slot + K + 1;
+  const double* l2 = p.L[cp] + slot + K + 1;
+  const double bk1 = p.b1[r0 + K], bk2 = p.b2[r0 + K];
+  const double phi1 = p.phi[c1], psi1 = p.psi[c1], phi2 = p.phi[c2], psi2 = p.psi[c2];
+  const double r = hypot(bk1 * psi1, bk2 * phi2);  // Calculations-Parallel.c:769-771
+  const double c0 = (r > 0.0) ? bk1 * psi1 / r : 1.0;
+  const double s0 = (r > 0.0) ? bk2 * phi2 / r : 0.0;
+  double* ds = p.ds + slot;
+  double* zs = p.zs + slot;
+  double* hfs = p.hfs + slot;
+  double* hls = p.hls + slot;
+  // parallel merge of [0] ++ child1 ++ child2 by value (ties: entry 0, then child1)
+  double dmax = 0.0, zmax = 0.0;
+  if (t == 0) {
+    ds[0] = 0.0; zs[0] = r; hfs[0] = c0 * phi1; hls[0] = s0 * psi2;
+    zmax = fabs(r);
+  }
+  for (int k = t; k < n1; k += blockDim.x) {
+    const double v = s1[k];
+    const int pos = 1 + k + count_lt(s2, n2, v);
+    const double z = bk1 * l1[k];
+    ds[pos] = v; zs[pos] = z; hfs[pos] = f1[k]; hls[pos] = 0.0;
+    dmax = fmax(dmax, fabs(v)); zmax = fmax(zmax, fabs(z));
+  }
+  for (int k = t; k < n2; k += blockDim.x) {
+    const double v = s2[k];
+    const int pos = 1 + k + count_le(s1, n1, v);
+    const double z = bk2 * f2[k];
+    ds[pos] = v; zs[pos] = z; hfs[pos] = 0.0; hls[pos] = l2[k];
+    dmax = fmax(dmax, fabs(v)); zmax = fmax(zmax, fabs(z));
+  }
+  dmax = block_max(dmax, shd);
+  zmax = block_max(zmax, shd);
+  const double tol = 8.0 * DBL_EPSILON * fmax(dmax, zmax);
+  __syncthreads();
+  // deflation 1: negligible z
+  const int per = ceil_div(nn, blockDim.x);
+  const int lo = min(nn, t * per), hi = min(nn, lo + per);
+  int cnt = 0;
+  for (int k = lo; k < hi; k++) {
+    int dfl = fabs(zs[k]) <= tol;
+    p.defl[slot + k] = dfl;
+    cnt += !dfl;
+  }
+  int tot;
+  int off = block_exscan(cnt, shi, &tot);
+  // positions of non-deflated entries -> compacted arrays (tentative)
+  for (int k = lo; k < hi; k++)
+    if (!p.defl[slot + k]) { p.dq[slot + off] = ds[k]; off++; }
+  __syncthreads();
+  // deflation 2 needed?  (adjacent non-deflated values within tol)
+  __shared__ int need2;
+  if (t == 0) need2 = 0;
+  __syncthreads();
+  for (int k = 1 + t; k < tot; k += blockDim.x)
+    if (p.dq[slot + k] - p.dq[slot + k - 1] <= tol) need2 = 1;
+  __syncthreads();
+  if (need2 && t == 0) {
+    int prev = -1;
+    for (int k = 0; k < nn; k++) {
+      if (p.defl[slot + k]) continue;
+      if (prev >= 0 && ds[k] - ds[prev] <= tol) {
+        double rr = hypot(zs[prev], zs[k]);
+        double c = zs[k] / rr, s = zs[prev] / rr;
+        zs[k] = rr; zs[prev] = 0.0; p.defl[slot + prev] = 1;
+        double fa = hfs[prev], fb = hfs[k], la = hls[prev], lb = hls[k];
+        hfs[prev] = c * fa - s * fb; hfs[k] = s * fa + c * fb;
+        hls[prev] = c * la - s * lb; hls[k] = s * la + c * lb;
+      }
+      prev = k;
+    }
+  }
+  __syncthreads();
+  // final compaction: non-deflated -> dq/zq/fq/lq, deflated -> dd/fd/ld
+  cnt = 0;
+  for (int k = lo; k < hi; k++) cnt += !p.defl[slot + k];
+  off = block_exscan(cnt, shi, &tot);
+  int doff = lo - off;  // deflated entries before this thread's range
+  double zzl = 0.0;
+  for (int k = lo; k < hi; k++) {
+    if (!p.defl[slot + k]) {
+      p.dq[slot + off] = ds[k]; p.zq[slot + off] = zs[k];
+      p.fq[slot + off] = hfs[k]; p.lq[slot + off] = hls[k];
+      zzl += zs[k] * zs[k];
+      off++;
+    } else {
+      p.dd[slot + doff] = ds[k]; p.fd[slot + doff] = hfs[k]; p.ld[slot + doff] = hls[k];
+      doff++;
+    }
+  }
+  double zz = block_sumd(zzl, shd);
+  if (t == 0) {
+    p.nq[node] = tot;
+    p.zz[node] = zz;
+    p.phi[node] = -s0 * phi1;  // Calculations-Parallel.c:807-808 (normalised in P5)
+    p.psi[node] = c0 * psi2;
+  }
+}
+
+// ---------------------------------------------------------------- secular roots (warp)
+__device__ __forceinline__ void sec_eval(int q, const double* d, const double* z, double dorg,
+                                         double tau, int split, int lane, double& f, double& psi,
+                                         double& dpsi, double& phi, double& dphi) {
+  double ps = 0.0, dps = 0.0, ph = 0.0, dph = 0.0;
+  for (int j = lane; j < q; j += 32) {
+    const double dj = d[j];
+    const double del = (dj - dorg) * (dj + dorg) - tau;
+    const double tt = z[j] / del;
+    if (j <= split) { ps += z[j] * tt; dps += tt * tt; }
+    else { ph += z[j] * tt; dph += tt * tt; }
+  }
+  psi = warp_sum(ps); dpsi = warp_sum(dps); phi = warp_sum(ph); dphi = warp_sum(dph);
+  f = 1.0 + psi + phi;
+}
+
+// Root i of the node's secular equation; returns origin (local index) and tau.
+__device__ bool sec_root(int q, const double* d, const double* z, double zz, int i, int lane,
+                         int* origin, double* tau_out) {
+  double f, psi, dpsi, phi, dphi;
+  bool conv = false;
+  if (i < q - 1) {
+    const double dd = (d[i + 1] - d[i]) * (d[i + 1] + d[i]);
+    sec_eval(q, d, z, d[i], 0.5 * dd, i, lane, f, psi, dpsi, phi, dphi);
+    const int o = (f >= 0.0) ? i : i + 1;
+    const double dorg = d[o];
+    double lo, hi, tau;
+    if (o == i) { lo = 0.0; hi = 0.5 * dd; tau = 0.5 * dd; }
+    else { lo = -0.5 * dd; hi = 0.0; tau = -0.5 * dd; }
+    const double da0 = (d[i] - dorg) * (d[i] + dorg);
+    const double db0 = (d[i + 1] - dorg) * (d[i + 1] + dorg);
+    for (int it = 0; it < kSecMaxIt; it++) {
+      sec_eval(q, d, z, dorg, tau, i, lane, f, psi, dpsi, phi, dphi);
+      const double err = 8.0 * (1.0 + fabs(psi) + fabs(phi)) + fabs(tau) * (dpsi + dphi);
+      if (fabs(f) <= DBL_EPSILON * err) { conv = true; break; }
+      if (f < 0.0) lo = tau; else hi = tau;
+      if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) { conv = true; break; }
+      const double da = da0 - tau, db = db0 - tau;
+      const double s1 = da * da * dpsi, s2 = db * db * dphi;
+      const double c = f - s1 / da - s2 / db;
+      const double aq = c, bq = c * (da + db) + s1 + s2, cq = da * db * f;
+      const double disc = sqrt(fabs(bq * bq - 4.0 * aq * cq));
+      double eta;
+      if (aq == 0.0) eta = cq / bq;
+      else if (bq <= 0.0) eta = (bq - disc) / (2.0 * aq);
+      else eta = 2.0 * cq / (bq + disc);
+      double tn = tau + eta;
+      if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+      tau = tn;
+    }
+    *origin = o;
+    *tau_out = tau;
+    return conv;
+  }
+  const int o = q - 1;
+  const double dorg = d[o];
+  double lo = 0.0, hi = zz, tau = 0.5 * zz;
+  for (int it = 0; it < kSecMaxIt; it++) {
+    sec_eval(q, d, z, dorg, tau, q - 1, lane, f, psi, dpsi, phi, dphi);
+    const double err = 8.0 * (1.0 + fabs(psi)) + fabs(tau) * dpsi;
+    if (fabs(f) <= DBL_EPSILON * err) { conv = true; break; }
+    if (f < 0.0) lo = tau; else hi = tau;
+    if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) { conv = true; break; }
+    const double da = -tau;
+    const double s1 = da * da * dpsi;
+    const double c = f - s1 / da;
+    double tn = (c != 0.0) ? tau + da + s1 / c : 0.5 * (lo + hi);
+    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+    tau = tn;
+  }
+  *origin = o;
+  *tau_out = tau;
+  return conv;
+}
+
+// merge node at depth d containing slot position pos (or -1)
+__device__ __forceinline__ int find_node(const DcParams& p, int d, int pos) {
+  int lo = p.dm_start[d], hi = p.dm_start[d + 1];
+  // largest merge node with slot <= pos
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (p.nd_slot[p.depth_merge[mid]] <= pos) lo = mid + 1; else hi = mid;
+  }
+  if (lo == p.dm_start[d]) return -1;
+  int node = p.depth_merge[lo - 1];
+  int slot = p.nd_slot[node];
+  return (pos < slot + p.nd_nn[node]) ? node : -1;
+}
+
+// ---------------------------------------------------------------- P5 final merge
+__device__ void dc_finish_node(const DcParams& p, int node, int par, bool rows, double* shd) {
+  const int t = threadIdx.x;
+  const int nn = p.nd_nn[node], slot = p.nd_slot[node];
+  const int q = p.nq[node], nd = nn - q;
+  const double* rs = p.rS + slot;
+  const double* dd = p.dd + slot;
+  double* sig = p.sig[par] + slot;
+  double* F = p.F[par] + slot;
+  double* L = p.L[par] + slot;
+  for (int k = t; k < q; k += blockDim.x) {
+    const int pos = k + count_lt(dd, nd, rs[k]);
+    sig[pos] = rs[k];
+    if (rows) { F[pos] = p.rF[slot + k]; L[pos] = p.rL[slot + k]; }
+  }
+  for (int k = t; k < nd; k += blockDim.x) {
+    const int pos = k + count_le(rs, q, dd[k]);
+    sig[pos] = dd[k];
+    if (rows) { F[pos] = p.fd[slot + k]; L[pos] = p.ld[slot + k]; }
+  }
+  if (!rows) return;
+  __syncthreads();
+  double sf = 0.0, sl = 0.0;
+  for (int k = t; k < nn; k += blockDim.x) { sf += F[k] * F[k]; sl += L[k] * L[k]; }
+  sf = block_sumd(sf, shd);
+  sl = block_sumd(sl, shd);
+  const double ph = p.phi[node], ps = p.psi[node];
+  const double nf = sqrt(sf + ph * ph), nl = sqrt(sl + ps * ps);
+  for (int k = t; k < nn; k += blockDim.x) {
+    if (nf > 0.0) F[k] /= nf;
+    if (nl > 0.0) L[k] /= nl;
+  }
+  __syncthreads();
+  if (t == 0) {
+    if (nf > 0.0) p.phi[node] = ph / nf;
+    if (nl > 0.0) p.psi[node] = ps / nl;
+  }
+}
+
+__global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
+  __shared__ int shi[40];
+  __shared__ double shd[40];
+  const int t = threadIdx.x, lane = t & 31;
+  const int gw = (blockIdx.x * blockDim.x + t) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int gt = blockIdx.x * blockDim.x + t, nthreads = gridDim.x * blockDim.x;
+  for (int d = p.maxdepth; d >= 0; d--) {
+    const int par = d & 1;
+    const bool rows = d > 0;
+    // ---- P1a leaves of this depth (thread each)
+    for (int k = p.depth_start[d] + gt; k < p.depth_start[d + 1]; k += nthreads) {
+      if (p.nd_K[k] >= 0) continue;
+      const int nn = p.nd_nn[k], slot = p.nd_slot[k], r0 = p.nd_r0[k];
+      double phi, psi;
+      dc_leaf(nn, p.b1 + r0, p.b2 + r0, p.sig[par] + slot, p.F[par] + slot, p.L[par] + slot, &phi, &psi);
+      p.phi[k] = phi;
+      p.psi[k] = psi;
+    }
+    // ---- P1b merge set-up (CTA per node)
+    for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
+      dc_setup_node(p, p.depth_merge[mi], par, shi, shd);
+    if (p.dm_start[d + 1] == p.dm_start[d]) {  // only leaves at this depth
+      if (d > 0 && !grid_sync(p.bar, p.P, p.st, 600 + d)) return;
+      continue;
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 100 + d)) return;
+    // ---- P2 secular roots (warp per root)
+    for (int pos = gw; pos < p.N; pos += nwarps) {
+      const int node = find_node(p, d, pos);
+      if (node < 0) continue;
+      const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
+      if (i >= q) continue;
+      int o;
+      double tau;
+      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.zz[node], i, lane, &o, &tau);
+      if (lane == 0) {
+        p.org[pos] = o;
+        p.tau[pos] = tau;
+        const double dorg = p.dq[slot + o];
+        p.rS[pos] = sqrt(dorg * dorg + tau);
+        if (!ok) set_error(p.st, DDCSVD_ERR_NOCONV, pos);
+      }
+    }
+    if (rows) {
+      if (!grid_sync(p.bar, p.P, p.st, 200 + d)) return;
+      // ---- P3 z-hat (warp per component)
+      for (int pos = gw; pos < p.N; pos += nwarps) {
+        const int node = find_node(p, d, pos);
+        if (node < 0) continue;
+        const int slot = p.nd_slot[node], j = pos - slot, q = p.nq[node];
+        if (j >= q) continue;
+        const double* dq = p.dq + slot;
+        const double* tau = p.tau + slot;
+        const int* org = p.org + slot;
+        const double dj = dq[j];
+        double prod = 1.0;
+        for (int k = lane; k < q - 1; k += 32) {
+          const int ok = org[k];
+          const double num = tau[k] - (dj - dq[ok]) * (dj + dq[ok]);
+          const int kk = (k < j) ? k : k + 1;
+          const double den = (dq[kk] - dj) * (dq[kk] + dj);
+          prod *= num / den;
+        }
+        prod = warp_prod(prod);
+        if (lane == 0) {
+          const int ol = org[q - 1];
+          prod *= tau[q - 1] - (dj - dq[ol]) * (dj + dq[ol]);
+          const double a = sqrt(fabs(prod));
+          p.zh[pos] = (p.zq[pos] >= 0.0) ? a : -a;
+        }
+      }
+      if (!grid_sync(p.bar, p.P, p.st, 300 + d)) return;
+      // ---- P4 rows of the merged right vectors (warp per root)
+      for (int pos = gw; pos < p.N; pos += nwarps) {
+        const int node = find_node(p, d, pos);
+        if (node < 0) continue;
+        const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
+        if (i >= q) continue;
+        const double* dq = p.dq + slot;
+        const double dorg = dq[p.org[pos]], ti = p.tau[pos];
+        double nv = 0.0, sf = 0.0, sl = 0.0;
+        for (int j = lane; j < q; j += 32) {
+          const double dj = dq[j];
+          const double del = (dj - dorg) * (dj + dorg) - ti;
+          const double v = p.zh[slot + j] / del;
+          nv += v * v;
+          sf += v * p.fq[slot + j];
+          sl += v * p.lq[slot + j];
+        }
+        nv = warp_sum(nv); sf = warp_sum(sf); sl = warp_sum(sl);
+        if (lane == 0) {
+          nv = sqrt(nv);
+          p.rF[pos] = sf / nv;
+          p.rL[pos] = sl / nv;
+        }
+      }
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 400 + d)) return;
+    // ---- P5 final merge + normalisation (CTA per node)
+    for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
+      dc_finish_node(p, p.depth_merge[mi], par, rows, shd);
+    if (d > 0 && !grid_sync(p.bar, p.P, p.st, 500 + d)) return;
+  }
+}
+
+__global__ void dc_copy_out(int N, const double* s, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) out[i] = s[i];
+}
+
+// ---------------------------------------------------------------- host: forest
+// One tree per unreduced block [lo, hi) of the (split) bidiagonal; a block's
+// singular values occupy slots [lo, hi).
+static int build_tree(DcHost& T, int r0, int nn, int slot, int depth) {
+  int id = (int)T.r0.size();
+  T.r0.push_back(r0); T.nn.push_back(nn); T.slot.push_back(slot);
+  T.K.push_back(-1); T.c1.push_back(-1); T.c2.push_back(-1); T.depth.push_back(depth);
+  T.maxdepth = std::max(T.maxdepth, depth);
+  if (nn > 2) {
+    int K = nn / 2;
+    T.K[id] = K;
+    int a = build_tree(T, r0, K, slot + 1, depth + 1);
+    int b = build_tree(T, r0 + K + 1, nn - K - 1, slot + K + 1, depth + 1);
+    T.c1[id] = a;
+    T.c2[id] = b;
+  }
+  return id;
+}
+
+void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
+  DcHost T0;
+  for (size_t b = 0; b + 1 < starts.size(); b++) {
+    const int lo = starts[b], hi = starts[b + 1];
+    if (hi > lo) build_tree(T0, lo, hi - lo, lo, 0);
+  }
+  const int nnodes = (int)T0.r0.size();
+  std::vector<int> order(nnodes);
+  for (int i = 0; i < nnodes; i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int x, int y) {
+    return T0.depth[x] != T0.depth[y] ? T0.depth[x] < T0.depth[y] : T0.slot[x] < T0.slot[y];
+  });
+  std::vector<int> newid(nnodes);
+  for (int i = 0; i < nnodes; i++) newid[order[i]] = i;
+  const int md = T0.maxdepth;
+  std::vector<int> r0(nnodes), nn(nnodes), slot(nnodes), K(nnodes), c1(nnodes), c2(nnodes), dep(nnodes);
+  for (int i = 0; i < nnodes; i++) {
+    int o = order[i];
+    r0[i] = T0.r0[o]; nn[i] = T0.nn[o]; slot[i] = T0.slot[o]; K[i] = T0.K[o]; dep[i] = T0.depth[o];
+    c1[i] = T0.c1[o] >= 0 ? newid[T0.c1[o]] : -1;
+    c2[i] = T0.c2[o] >= 0 ? newid[T0.c2[o]] : -1;
+  }
+  std::vector<int> ds(md + 2, nnodes), dms(md + 2, 0), dmerge;
+  for (int d = md; d >= 0; d--) {
+    int first = nnodes;
+    for (int i = nnodes - 1; i >= 0; i--) if (dep[i] >= d) first = i;
+    ds[d] = first;
+  }
+  for (int d = 0; d <= md; d++) {
+    dms[d] = (int)dmerge.size();
+    for (int i = ds[d]; i < ds[d + 1]; i++) if (K[i] >= 0) dmerge.push_back(i);
+  }
+  dms[md + 1] = (int)dmerge.size();
+  H.nnodes = nnodes;
+  H.maxdepth = md;
+  H.ndm = (int)dmerge.size();
+  H.ints.clear();
+  auto app = [&](const std::vector<int>& v) { H.ints.insert(H.ints.end(), v.begin(), v.end()); };
+  app(r0); app(nn); app(slot); app(K); app(c1); app(c2); app(ds); app(dms); app(dmerge);
+}
+
+size_t dc_max_ints(int N) { return 9 * (size_t)(2 * N + 8) + 2 * 64 + 16; }
+
+int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, double* sigma,
+             const DcHost* H, const int* dints, Arena& a, bool plan_only) {
+  if (N <= 0) return DDCSVD_ERR_ARG;
+  const int maxnodes = 2 * N + 8;
+  int* scratch_ints = a.take<int>((size_t)N * 2 + maxnodes);
+  double* dbl = a.take<double>((size_t)N * 25 + 3 * (size_t)maxnodes + 8);
+  GridBarrier* bar = a.take<GridBarrier>(4);
+  if (plan_only) return DDCSVD_OK;
+  const int nnodes = H->nnodes, md = H->maxdepth;
+  DcParams p;
+  p.N = N; p.nnodes = nnodes; p.maxdepth = md;
+  size_t o = 0;
+  p.nd_r0 = dints + o; o += nnodes;
+  p.nd_nn = dints + o; o += nnodes;
+  p.nd_slot = dints + o; o += nnodes;
+  p.nd_K = dints + o; o += nnodes;
+  p.nd_c1 = dints + o; o += nnodes;
+  p.nd_c2 = dints + o; o += nnodes;
+  p.depth_start = dints + o; o += md + 2;
+  p.dm_start = dints + o; o += md + 2;
+  p.depth_merge = dints + o; o += H->ndm;
+  p.org = scratch_ints;
+  p.defl = scratch_ints + N;
+  p.nq = scratch_ints + 2 * (size_t)N;
+  p.b1 = b1; p.b2 = b2;
+  double* q = dbl;
+  for (int k = 0; k < 2; k++) { p.sig[k] = q; q += N; p.F[k] = q; q += N; p.L[k] = q; q += N; }
+  p.ds = q; q += N; p.zs = q; q += N; p.hfs = q; q += N; p.hls = q; q += N;
+  p.dq = q; q += N; p.zq = q; q += N; p.fq = q; q += N; p.lq = q; q += N;
+  p.dd = q; q += N; p.fd = q; q += N; p.ld = q; q += N;
+  p.tau = q; q += N; p.zh = q; q += N; p.rS = q; q += N; p.rF = q; q += N; p.rL = q; q += N;
+  p.zz = q; q += maxnodes; p.phi = q; q += maxnodes; p.psi = q; q += maxnodes;
+  p.out = sigma;
+  p.bar = bar;
+  p.st = ctx->d_status;
+  int occ = 0;
+  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dc_kernel, kDcThreads, 0));
+  if (occ < 1) {
+    set_last_error("dc_kernel cannot be resident");
+    return DDCSVD_ERR_CUDA;
+  }
+  const int P = std::min(ctx->num_sms, std::max(1, ceil_div(N, 16)));
+  p.P = P;
+  DDC_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), ctx->stream));
+  void* argv[] = {&p};
+  ktimer_begin(ctx, KC_DC);
+  DDC_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)dc_kernel, dim3(P), dim3(kDcThreads), argv, 0,
+                                           ctx->stream));
+  ktimer_end(ctx);
+  count_launch();
+  dc_copy_out<<<std::min(ceil_div(N, 256), 1024), 256, 0, ctx->stream>>>(N, p.sig[0], sigma);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+}  // namespace ddcsvd

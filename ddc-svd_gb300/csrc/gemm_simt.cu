@@ -1,0 +1,170 @@
+// gemm_simt.cu -- FP32 CUDA-core GEMM with strided operands and
+// deterministic split-K, plus the gemm() dispatcher that picks the back end.
+//
+// Used for the trailing updates and the WY back-transformation in
+// DDCSVD_MODE_BLOCKED_FP32, and for the small T-factor products in every
+// mode.  The tensor-core back ends (gemm_tc.cu) take over the large products
+// in the TF32X3 / BF16X3 modes.
+#include "internal.hpp"
+
+namespace ddcsvd {
+
+constexpr int BM = 128, BN = 128, BK = 16, GT = 256;
+
+struct GemmTerm {
+  const float* A;
+  long long ars, acs;
+  const float* B;
+  long long brs, bcs;
+  int K;
+};
+
+// Cs[kz] (M x N, ld M) = sum over the K-range of split kz (no alpha/beta)
+// when `partial` is set; otherwise C = beta*C + alpha*acc.
+template <bool A_RCONTIG, bool B_CCONTIG>
+__device__ __forceinline__ void load_tiles(const GemmTerm& T, int m0, int n0, int k0, int kend,
+                                           int M, int N, float (*As)[BM + 4], float (*Bs)[BN + 4]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < (BM * BK) / GT; s++) {
+    const int idx = t + GT * s;
+    int r, k;
+    if (A_RCONTIG) { k = idx / BM; r = idx % BM; }
+    else { r = idx / BK; k = idx % BK; }
+    const int gr = m0 + r, gk = k0 + k;
+    As[k][r] = (gr < M && gk < kend) ? T.A[gr * T.ars + gk * T.acs] : 0.f;
+  }
+#pragma unroll
+  for (int s = 0; s < (BN * BK) / GT; s++) {
+    const int idx = t + GT * s;
+    int c, k;
+    if (B_CCONTIG) { k = idx / BN; c = idx % BN; }
+    else { c = idx / BK; k = idx % BK; }
+    const int gc = n0 + c, gk = k0 + k;
+    Bs[k][c] = (gc < N && gk < kend) ? T.B[gk * T.brs + gc * T.bcs] : 0.f;
+  }
+}
+
+__device__ __forceinline__ void run_term(const GemmTerm& T, int m0, int n0, int kb, int ke, int M,
+                                         int N, float (*As)[BM + 4], float (*Bs)[BN + 4],
+                                         float acc[8][8]) {
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const bool arc = (T.ars == 1), bcc = (T.bcs == 1);
+  for (int k0 = kb; k0 < ke; k0 += BK) {
+    __syncthreads();
+    if (arc && bcc) load_tiles<true, true>(T, m0, n0, k0, ke, M, N, As, Bs);
+    else if (arc) load_tiles<true, false>(T, m0, n0, k0, ke, M, N, As, Bs);
+    else if (bcc) load_tiles<false, true>(T, m0, n0, k0, ke, M, N, As, Bs);
+    else load_tiles<false, false>(T, m0, n0, k0, ke, M, N, As, Bs);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < BK; k++) {
+      float a[8], b[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) a[i] = As[k][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 8; j++) b[j] = Bs[k][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(GT) gemm_simt_kernel(int M, int N, GemmTerm T1, GemmTerm T2,
+                                                       float alpha, float beta, float* C, int ldc,
+                                                       float* partial, int ksplit) {
+  __shared__ __align__(16) float As[BK][BM + 4];
+  __shared__ __align__(16) float Bs[BK][BN + 4];
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, kz = blockIdx.z;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+  // split-K over the concatenated K range of both terms
+  const int Ktot = T1.K + T2.K;
+  const int chunk = (int)round_up(ceil_div(Ktot, ksplit), BK);
+  const int kb = kz * chunk, ke = min(Ktot, kb + chunk);
+  if (kb < T1.K) run_term(T1, m0, n0, kb, min(ke, T1.K), M, N, As, Bs, acc);
+  if (ke > T1.K && T2.K > 0)
+    run_term(T2, m0, n0, max(kb, T1.K) - T1.K, ke - T1.K, M, N, As, Bs, acc);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int r = m0 + ty + 16 * i;
+    if (r >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int c = n0 + tx + 16 * j;
+      if (c >= N) continue;
+      if (partial) {
+        partial[(size_t)kz * M * N + r + (size_t)c * M] = acc[i][j];
+      } else {
+        float* cp = C + r + (size_t)c * ldc;
+        *cp = (beta == 0.f ? 0.f : beta * *cp) + alpha * acc[i][j];
+      }
+    }
+  }
+}
+
+__global__ void splitk_reduce_kernel(int M, int N, int ksplit, const float* partial, float alpha,
+                                     float beta, float* C, int ldc) {
+  const size_t tot = (size_t)M * N;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < ksplit; z++) s += partial[(size_t)z * tot + idx];
+    const int r = (int)(idx % M), c = (int)(idx / M);
+    float* cp = C + r + (size_t)c * ldc;
+    *cp = (beta == 0.f ? 0.f : beta * *cp) + alpha * s;
+  }
+}
+
+int gemm_tc(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2,
+            Mat A2, Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch);
+size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K);
+
+size_t gemm_scratch_bytes(GemmKind kind, int M, int N, int K) {
+  size_t simt = (size_t)16 * M * N * sizeof(float) + 4096;
+  if (kind == GEMM_SIMT) return simt;
+  return std::max(simt, gemm_tc_scratch_bytes(kind, M, N, K));
+}
+
+int gemm_simt(ddcsvd_context* ctx, int M, int N, int K1, Mat A1, Mat B1, int K2, Mat A2, Mat B2,
+              float alpha, float beta, float* C, int ldc, Arena* scratch) {
+  if (M <= 0 || N <= 0) return DDCSVD_OK;
+  GemmTerm T1{A1.p, A1.rs, A1.cs, B1.p, B1.rs, B1.cs, K1};
+  GemmTerm T2{A2.p, A2.rs, A2.cs, B2.p, B2.rs, B2.cs, A2.p ? K2 : 0};
+  const int tiles = ceil_div(M, BM) * ceil_div(N, BN);
+  const int Ktot = T1.K + T2.K;
+  int ksplit = 1;
+  if (scratch && !scratch->plan && tiles < ctx->num_sms && Ktot >= 4 * BK * 8) {
+    ksplit = std::min(16, std::max(1, (2 * ctx->num_sms) / tiles));
+    ksplit = std::min(ksplit, std::max(1, Ktot / (8 * BK)));
+    while (ksplit > 1 && (size_t)ksplit * M * N * sizeof(float) > scratch->cap) ksplit--;
+  }
+  float* partial = (ksplit > 1) ? reinterpret_cast<float*>(scratch->base) : nullptr;
+  dim3 grid(ceil_div(M, BM), ceil_div(N, BN), ksplit);
+  gemm_simt_kernel<<<grid, GT, 0, ctx->stream>>>(M, N, T1, T2, alpha, beta, C, ldc, partial, ksplit);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  if (ksplit > 1) {
+    const int blocks = std::min(4 * ctx->num_sms, ceil_div(M * N, 256));
+    splitk_reduce_kernel<<<blocks, 256, 0, ctx->stream>>>(M, N, ksplit, partial, alpha, beta, C, ldc);
+    count_launch();
+    DDC_CUDA_TRY(cudaGetLastError());
+  }
+  return DDCSVD_OK;
+}
+
+int gemm(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2, Mat A2,
+         Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch) {
+  // a tensor-core kind never degrades to the CUDA-core kernel: gemm_tc fails
+  // loudly when the tcgen05 path is unavailable
+  if (kind != GEMM_SIMT) return gemm_tc(ctx, kind, M, N, K1, A1, B1, K2, A2, B2, alpha, beta, C, ldc, scratch);
+  return gemm_simt(ctx, M, N, K1, A1, B1, K2, A2, B2, alpha, beta, C, ldc, scratch);
+}
+
+}  // namespace ddcsvd

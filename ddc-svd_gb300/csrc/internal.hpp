@@ -1,0 +1,143 @@
+// internal.hpp -- declarations shared by the translation units of libddcsvd.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+struct ddcsvd_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // device workspace (grown on demand, reused across calls)
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  // pinned host staging for the host-buffer entry points
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  // status word (device) and its pinned mirror
+  ddcsvd::DevStatus* d_status = nullptr;
+  ddcsvd::DevStatus* h_status = nullptr;
+  // optional stage timing
+  bool timing = false;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float stage_ms[4] = {0, 0, 0, 0};
+  // optional per-kernel-class timing (event pairs around launches)
+  std::vector<cudaEvent_t> kev;       // pool, pairs
+  std::vector<int> kcat;              // category of each recorded pair
+  int kused = 0;
+  float kern_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int kern_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::mutex mu;
+};
+
+namespace ddcsvd {
+
+// Bump allocator over the context workspace.  `plan` mode only counts.
+struct Arena {
+  char* base = nullptr;
+  size_t off = 0;
+  bool plan = true;
+  size_t cap = 0;  // capacity when used as a fixed scratch region (0 = unchecked)
+  template <typename T>
+  T* take(size_t count) {
+    off = (size_t)round_up((long long)off, 256);
+    T* p = plan ? nullptr : reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+// Kernel classes for ddcsvd_get_kernel_times.
+enum KernelClass { KC_BIDIAG = 0, KC_TRAIL_GEMM = 1, KC_DC = 2, KC_VECTORS = 3, KC_BACKXFORM = 4 };
+void ktimer_begin(ddcsvd_context* ctx, int cls);  // no-ops unless timing is on
+void ktimer_end(ddcsvd_context* ctx);
+void ktimer_collect(ddcsvd_context* ctx);        // after a stream sync
+
+int ensure_workspace(ddcsvd_context* ctx, size_t bytes);
+int ensure_pinned(ddcsvd_context* ctx, size_t bytes);
+int check_status(ddcsvd_context* ctx, const char* stage);  // syncs the stream
+int reset_status(ddcsvd_context* ctx);
+
+// ---------------------------------------------------------------- GEMM back ends
+enum GemmKind { GEMM_SIMT = 0, GEMM_TF32X3 = 1, GEMM_BF16X3 = 2 };
+
+// Operand descriptor: element (r, c) of the logical matrix lives at
+// p[r * rs + c * cs]; exactly one of rs / cs is 1.
+struct Mat {
+  const float* p;
+  long long rs, cs;
+};
+
+// C(M x N, col-major, ldc) = beta * C + alpha * (A1 B1 + A2 B2), A_t: M x K_t, B_t: K_t x N.
+// A2/B2 may be null (K2 = 0).
+int gemm(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2, Mat A2,
+         Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch);
+size_t gemm_scratch_bytes(GemmKind kind, int M, int N, int K);
+bool tc_available(ddcsvd_context* ctx);
+
+// ---------------------------------------------------------------- stage 1
+struct BidiagWork {
+  float *X, *Y, *VT;  // panel matrices (ldx = ldw, ldy = ldvt = ldn)
+  int ldn;
+  float *xcol, *xrow;
+  float *colpart, *rowpart;
+  GridBarrier* bar;
+  int P;  // CTAs of the cooperative launch
+  char* gemm_scratch;
+};
+constexpr int kPanel = 32;       // bidiagonalisation panel width
+constexpr int kBidiagThreads = 512;
+void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWork* w);
+int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,
+                   float* tauq, float* taup, BidiagWork& w, GemmKind kind, Arena* scratch);
+int bidiag_plain(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,
+                 float* tauq, float* taup, BidiagWork& w);
+int bidiag_coop_ctas(ddcsvd_context* ctx, int m, int n);
+// LAPACK-form reflectors -> the reference's normalised form, FP64 output (ld = m).
+int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw, const float* d,
+                      const float* e, const float* tauq, const float* taup, double* A_out);
+
+// ---------------------------------------------------------------- stage 2
+// Host description of the D&C forest (one tree per unreduced block).
+struct DcHost {
+  std::vector<int> r0, nn, slot, K, c1, c2, depth;  // construction scratch
+  int maxdepth = 0;
+  int nnodes = 0, ndm = 0;
+  std::vector<int> ints;  // packed node table uploaded to the device
+};
+void dc_build_host(int N, const std::vector<int>& block_starts, DcHost& H);
+size_t dc_max_ints(int N);
+int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, double* sigma,
+             const DcHost* H, const int* dints, Arena& a, bool plan_only);
+
+// Splits the N x N bidiagonal (host copies a[N], b[N]) at |b_i| <= 4 eps max|B|:
+// zeroes those b_i (and b[N-1]), fills block_starts (ascending, ends with N)
+// and, per row, the bounds of its block.
+int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, Arena& a);
+void split_bidiagonal(int N, double* a, double* b, double eps, std::vector<int>& block_starts,
+                      int* blk_lo, int* blk_hi);
+
+// ---------------------------------------------------------------- stages 3-4
+// sigma (slot order: ascending within each block) -> X, Y columns in global
+// ascending order; sigma_sorted receives the sorted values.
+int bd_vectors(ddcsvd_context* ctx, int N, const double* a, const double* b, const double* sigma,
+               const int* blk_lo, const int* blk_hi, float* X, int ldx, float* Y, int ldy,
+               double* sigma_sorted, Arena& arena, bool plan_only);
+
+// ---------------------------------------------------------------- stage 5
+constexpr int kWY = 64;  // reflectors per WY block in the back-transformation
+// C (rows x ncols, ldc) := Q C with Q = H_0 ... H_{nref-1} (left reflectors in W columns).
+int apply_left_reflectors(ddcsvd_context* ctx, int m, int nref, const float* W, int ldw,
+                          const float* tauq, float* C, int ldc, int ncols, GemmKind kind,
+                          bool plain, Arena& a, bool plan_only);
+// C (n x ncols) := P C with P = G_0 ... G_{nref-1} (right reflectors in W rows).
+int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W, int ldw,
+                           const float* taup, float* C, int ldc, int ncols, GemmKind kind,
+                           bool plain, Arena& a, bool plan_only);
+
+}  // namespace ddcsvd

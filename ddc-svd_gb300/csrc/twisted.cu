@@ -1,0 +1,241 @@
+// twisted.cu -- stages 3-4: singular vectors of the bidiagonal (FP64 core).
+//
+// Replaces CalcRightSingularVectors (parallel-twisted.c:554-637) and
+// RighttoLeftSingularVectors (:530-551).  For each sigma_k the reference
+// factors B^T B - sigma_k^2 I forward (P D1 P^T) and backward (Q D2 Q^T)
+// (:320-362), picks the twist r = argmin |gamma| (:458-488), solves for the
+// vector from x_r = 1 outwards (:494-521) and normalises it (:88-123).  It
+// forms B^T B explicitly, which squares the condition number and fails on
+// graded spectra.  Here the same two factorisations come from the
+// differential stationary / progressive qd transforms of B^T B = L D L^T
+// (d_i = a_i^2, l_i = b_i / a_i) taken from the bidiagonal itself, which keep
+// relative accuracy for small sigma; twist, solve and normalisation follow
+// the reference.  Left vectors: y = B x normalised (the reference divides by
+// sigma, :548, which fails for sigma = 0).
+//
+// GB300 mapping: each thread owns one sigma_k; a CTA of two warps handles 32
+// vectors, warp 0 running the top-down (stationary) transform while warp 1
+// runs the bottom-up (progressive) transform of the same 32 shifts, so the
+// two sequential FP64 recurrences overlap.  Per-step arrays are stored
+// interleaved by vector (element i of vector k at [i * N + k]) so every
+// access of a warp is one contiguous 256-byte segment.
+#include <vector>
+
+#include "internal.hpp"
+
+namespace ddcsvd {
+
+__global__ void tw_setup_kernel(int N, const double* __restrict__ a, const double* __restrict__ b,
+                                double* dd, double* ll, double* dl, double* dll) {
+  // floor for zero diagonal entries (rank-deficient B): keeps l_i finite
+  __shared__ double smax;
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int i = 0; i < N; i++) m = fmax(m, fabs(a[i]));
+    for (int i = 0; i + 1 < N; i++) m = fmax(m, fabs(b[i]));
+    smax = (m > 0.0 ? m : 1.0) * DBL_EPSILON * DBL_EPSILON;
+  }
+  __syncthreads();
+  const double fl = smax;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double ai = a[i];
+    if (fabs(ai) < fl) ai = (ai < 0.0) ? -fl : fl;
+    const double di = ai * ai;
+    const double li = (i + 1 < N) ? b[i] / ai : 0.0;
+    dd[i] = di;
+    ll[i] = li;
+    dl[i] = di * li;
+    dll[i] = di * li * li;
+  }
+}
+
+struct TwParams {
+  int N;
+  const double *dd, *ll, *dl, *dll;
+  const double* sigma;
+  const int *blo, *bhi;       // block of each slot
+  double *Lp, *Um, *S, *Pp;  // N x N, interleaved [i * N + k]
+  double* Z;                  // N x N interleaved (zero outside the block)
+  double *xinv, *yinv;        // per vector
+  int* rank;                  // output column of each vector
+  const double *a, *b;
+};
+
+__global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
+  const int N = p.N;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const bool act = k < N;
+  const int lo = act ? p.blo[k] : 0, hi = act ? p.bhi[k] : 0;
+  const double lam = act ? p.sigma[k] * p.sigma[k] : 0.0;
+  const double tiny = DBL_MIN / DBL_EPSILON;
+  if (w == 0) {
+    // stationary qd on the block: L D L^T - lam = L+ D+ L+^T, s_lo = -lam
+    double s = -lam;
+    for (int i = lo; i < hi - 1; i++) {
+      double dp = p.dd[i] + s;
+      if (fabs(dp) < tiny) dp = -tiny;
+      const double L = p.dl[i] / dp;
+      p.Lp[(size_t)i * N + k] = L;
+      p.S[(size_t)i * N + k] = s;
+      s = L * p.ll[i] * s - lam;
+    }
+    if (hi > lo) p.S[(size_t)(hi - 1) * N + k] = s;
+  } else if (hi > lo) {
+    // progressive qd on the block: L D L^T - lam = U- D- U-^T, p_{hi-1} = d_{hi-1} - lam
+    double pv = p.dd[hi - 1] - lam;
+    p.Pp[(size_t)(hi - 1) * N + k] = pv;
+    for (int i = hi - 2; i >= lo; i--) {
+      double dm = p.dll[i] + pv;
+      if (fabs(dm) < tiny) dm = -tiny;
+      const double tt = p.dd[i] / dm;
+      p.Um[(size_t)i * N + k] = p.ll[i] * tt;
+      pv = pv * tt - lam;
+      p.Pp[(size_t)i * N + k] = pv;
+    }
+  }
+  __syncthreads();
+  if (w != 0 || !act) return;
+  // twist index r = argmin |gamma_i|, gamma_i = s_i + p_i + lam (ties: larger i)
+  int r = hi - 1;
+  double gbest = fabs(p.S[(size_t)(hi - 1) * N + k] + p.Pp[(size_t)(hi - 1) * N + k] + lam);
+  for (int i = hi - 2; i >= lo; i--) {
+    const double g = fabs(p.S[(size_t)i * N + k] + p.Pp[(size_t)i * N + k] + lam);
+    if (g < gbest) { gbest = g; r = i; }
+  }
+  // solve N_r z = gamma_r e_r with z_r = 1, outwards from r
+  double nrm = 1.0;
+  p.Z[(size_t)r * N + k] = 1.0;
+  double z = 1.0;
+  for (int i = r - 1; i >= lo; i--) {
+    z = -p.Lp[(size_t)i * N + k] * z;
+    p.Z[(size_t)i * N + k] = z;
+    nrm += z * z;
+  }
+  z = 1.0;
+  for (int i = r + 1; i < hi; i++) {
+    z = -p.Um[(size_t)(i - 1) * N + k] * z;
+    p.Z[(size_t)i * N + k] = z;
+    nrm += z * z;
+  }
+  // ||B z||^2 for the left vector (b is zero at the block end)
+  double by = 0.0;
+  double zi = p.Z[(size_t)lo * N + k];
+  for (int i = lo; i < hi; i++) {
+    const double zn = (i + 1 < hi) ? p.Z[(size_t)(i + 1) * N + k] : 0.0;
+    const double y = p.a[i] * zi + ((i + 1 < hi) ? p.b[i] * zn : 0.0);
+    by += y * y;
+    zi = zn;
+  }
+  p.xinv[k] = 1.0 / sqrt(nrm);
+  p.yinv[k] = (by > 0.0) ? 1.0 / sqrt(by) : 0.0;
+}
+
+// rank[k] = position of sigma_k in ascending order (stable); sorted values out.
+__global__ void tw_rank_kernel(int N, const double* __restrict__ sigma, int* rank, double* sorted) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    const double v = sigma[k];
+    int r = 0;
+    for (int j = 0; j < N; j++) {
+      const double u = sigma[j];
+      r += (u < v) || (u == v && j < k);
+    }
+    rank[k] = r;
+    if (sorted) sorted[r] = v;
+  }
+}
+
+// X[i + rank_k*ldx] = z_k[i] / ||z_k||, Y[i + rank_k*ldy] = (B z_k)[i] / ||B z_k||.
+__global__ void tw_finalize_kernel(TwParams p, float* X, int ldx, float* Y, int ldy) {
+  __shared__ double tile[33][33];
+  const int N = p.N;
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int rr = ty; rr < 33; rr += 8) {
+    const int i = i0 + rr, k = k0 + tx;
+    tile[rr][tx] = (i < N && k < N) ? p.Z[(size_t)i * N + k] : 0.0;
+  }
+  __syncthreads();
+  for (int kk = ty; kk < 32; kk += 8) {
+    const int k = k0 + kk, i = i0 + tx;
+    if (k >= N || i >= N) continue;
+    const int col = p.rank[k];
+    const double xi = tile[tx][kk], xn = tile[tx + 1][kk];
+    X[i + (size_t)col * ldx] = (float)(xi * p.xinv[k]);
+    const double y = p.a[i] * xi + ((i + 1 < N) ? p.b[i] * xn : 0.0);
+    Y[i + (size_t)col * ldy] = (float)(y * p.yinv[k]);
+  }
+}
+
+int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, Arena& a) {
+  int* rank = a.take<int>(N + 8);
+  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, in, rank, out);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+void split_bidiagonal(int N, double* a, double* b, double eps, std::vector<int>& starts, int* blk_lo,
+                      int* blk_hi) {
+  double bmax = 0.0;
+  for (int i = 0; i < N; i++) bmax = std::max(bmax, fabs(a[i]));
+  for (int i = 0; i + 1 < N; i++) bmax = std::max(bmax, fabs(b[i]));
+  const double tol = 4.0 * eps * bmax;
+  starts.clear();
+  starts.push_back(0);
+  for (int i = 0; i + 1 < N; i++) {
+    if (fabs(b[i]) <= tol) {
+      b[i] = 0.0;
+      starts.push_back(i + 1);
+    }
+  }
+  if (N >= 1) b[N - 1] = 0.0;
+  starts.push_back(N);
+  for (size_t s = 0; s + 1 < starts.size(); s++)
+    for (int i = starts[s]; i < starts[s + 1]; i++) {
+      blk_lo[i] = starts[s];
+      blk_hi[i] = starts[s + 1];
+    }
+}
+
+int bd_vectors(ddcsvd_context* ctx, int N, const double* a, const double* b, const double* sigma,
+               const int* blk_lo, const int* blk_hi, float* X, int ldx, float* Y, int ldy,
+               double* sigma_sorted, Arena& arena, bool plan_only) {
+  if (N <= 0) return DDCSVD_ERR_ARG;
+  double* small = arena.take<double>(6 * (size_t)N + 8);
+  int* rank = arena.take<int>(N + 8);
+  double* big = arena.take<double>(5 * (size_t)N * N);
+  if (plan_only) return DDCSVD_OK;
+  TwParams p;
+  p.N = N;
+  double* dd = small;
+  double* ll = small + N;
+  double* dl = small + 2 * (size_t)N;
+  double* dll = small + 3 * (size_t)N;
+  p.dd = dd; p.ll = ll; p.dl = dl; p.dll = dll;
+  p.xinv = small + 4 * (size_t)N;
+  p.yinv = small + 5 * (size_t)N;
+  p.sigma = sigma;
+  p.blo = blk_lo;
+  p.bhi = blk_hi;
+  p.rank = rank;
+  p.a = a;
+  p.b = b;
+  const size_t NN = (size_t)N * N;
+  p.Lp = big; p.Um = big + NN; p.S = big + 2 * NN; p.Pp = big + 3 * NN; p.Z = big + 4 * NN;
+  DDC_CUDA_TRY(cudaMemsetAsync(p.Z, 0, sizeof(double) * NN, ctx->stream));
+  ktimer_begin(ctx, KC_VECTORS);
+  tw_setup_kernel<<<1, 256, 0, ctx->stream>>>(N, a, b, dd, ll, dl, dll);
+  count_launch();
+  twisted_kernel<<<ceil_div(N, 32), 64, 0, ctx->stream>>>(p);
+  count_launch();
+  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, rank, sigma_sorted);
+  count_launch();
+  tw_finalize_kernel<<<dim3(ceil_div(N, 32), ceil_div(N, 32)), dim3(32, 8), 0, ctx->stream>>>(p, X, ldx, Y, ldy);
+  count_launch();
+  ktimer_end(ctx);
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+}  // namespace ddcsvd

@@ -1,0 +1,289 @@
+"""ddcsvd -- Python face of libddcsvd.so (GB300 / sm_103a dense SVD).
+
+The functions mirror the reference's C interface (svd_gpu, bidiag_par) with
+numpy host arrays, plus device entry points on torch CUDA tensors.  All
+numerical work happens in the CUDA library; this module only marshals
+pointers.  Matrices are column-major inside the library: a torch tensor A of
+shape (m, n) is passed as the column-major buffer of A (its transpose is
+made contiguous), and outputs come back as (m, k) / (n, k) views.
+Singular values are ascending, as the reference returns them
+(Calculations-Parallel.c:56).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import MODES, DdcsvdError, check, load
+
+__all__ = ["svd_gpu", "bidiag_par", "svd", "Handle", "svd_device", "bidiag_device",
+           "bdsdc_sigma_device", "bdvec_device", "svd_batched_device", "svd_backward_device",
+           "launch_count", "DdcsvdError", "MODES"]
+
+
+def _mode(mode) -> int:
+    return MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+def _addr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ---------------------------------------------------------------- host drop-ins
+def svd_gpu(A: np.ndarray, mode="auto"):
+    """svd_gpu (svd_gpu.c:53) on a float64 host matrix; returns (sigma, U, V).
+
+    Goes through svd_gpu_ex so that failures raise instead of filling NaN."""
+    lib = load()
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    m, n = A.shape
+    k = min(m, n)
+    s = np.zeros(k)
+    U = np.zeros((m, k), order="F")
+    V = np.zeros((n, k), order="F")
+    check(lib.svd_gpu_ex(m, n, _addr(A), _addr(s), _addr(U), _addr(V), _mode(mode)), "svd_gpu")
+    return s, U, V
+
+
+def svd_gpu_void(A: np.ndarray):
+    """The exact void drop-in svd_gpu(m, n, A, sigma, U, V) (A is clobbered)."""
+    lib = load()
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    m, n = A.shape
+    k = min(m, n)
+    s = np.zeros(k)
+    U = np.zeros((m, k), order="F")
+    V = np.zeros((n, k), order="F")
+    lib.svd_gpu(m, n, _addr(A), _addr(s), _addr(U), _addr(V))
+    return s, U, V
+
+
+def bidiag_par(A: np.ndarray):
+    """bidiag_par (bidiag_par.c:34) on a float64 host matrix (m >= n).
+
+    Returns (A_reflectors, alpha, beta) in the reference's storage."""
+    lib = load()
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    m, n = A.shape
+    al = np.zeros(n)
+    be = np.zeros(max(n - 1, 1))
+    lib.bidiag_par(m, n, _addr(A), _addr(al), _addr(be))
+    if np.isnan(al).any():
+        raise DdcsvdError(2, "bidiag_par")
+    return A, al, be[: n - 1]
+
+
+def svd(A: np.ndarray, mode="auto"):
+    """FP32 host SVD (A not modified); returns (sigma asc, U (m,k), V (n,k)) as float32."""
+    lib = load()
+    A = np.asarray(A, dtype=np.float32, order="F")
+    m, n = A.shape
+    k = min(m, n)
+    s = np.zeros(k, dtype=np.float32)
+    U = np.zeros((m, k), dtype=np.float32, order="F")
+    V = np.zeros((n, k), dtype=np.float32, order="F")
+    check(lib.ddcsvd_svd_f32(m, n, _addr(A), m, _addr(s), _addr(U), m, _addr(V), n, _mode(mode)),
+          "ddcsvd_svd_f32")
+    return s, U, V
+
+
+def launch_count() -> int:
+    return int(load().ddcsvd_kernel_launch_count())
+
+
+# ---------------------------------------------------------------- device API (torch)
+class Handle:
+    """Owns a library handle bound to the current device and torch's current stream."""
+
+    def __init__(self, device: int | None = None, stream=None):
+        import torch
+        lib = load()
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = device
+        h = ctypes.c_void_p()
+        check(lib.ddcsvd_create(ctypes.addressof(h), device), "ddcsvd_create")
+        self._h = h
+        s = stream if stream is not None else torch.cuda.current_stream(device)
+        check(lib.ddcsvd_set_stream(self._h, ctypes.c_void_p(s.cuda_stream)), "ddcsvd_set_stream")
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def stage_timing(self, enable: bool = True) -> None:
+        check(load().ddcsvd_set_stage_timing(self._h, int(enable)), "set_stage_timing")
+
+    def stage_times(self) -> list[float]:
+        buf = (ctypes.c_float * 4)()
+        check(load().ddcsvd_get_stage_times(self._h, ctypes.addressof(buf)), "get_stage_times")
+        return [float(x) for x in buf]
+
+    def kernel_times(self, nclass: int = 5):
+        """(ms, launches) per kernel class of the last SVD (timing must be on)."""
+        ms = (ctypes.c_float * nclass)()
+        nl = (ctypes.c_int * nclass)()
+        check(load().ddcsvd_get_kernel_times(self._h, ctypes.addressof(ms), ctypes.addressof(nl), nclass),
+              "get_kernel_times")
+        return [float(x) for x in ms], [int(x) for x in nl]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().ddcsvd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_handles: dict = {}
+
+
+def _handle(h: Handle | None) -> Handle:
+    if h is not None:
+        return h
+    import torch
+    dev = torch.cuda.current_device()
+    key = (dev, torch.cuda.current_stream(dev).cuda_stream)
+    if key not in _default_handles:
+        _default_handles[key] = Handle(dev)
+    return _default_handles[key]
+
+
+def colmajor(A):
+    """Column-major storage of a (m, n) torch tensor: returns (buffer (n, m) contiguous, ld)."""
+    Ac = A.t().contiguous()
+    return Ac, A.shape[0]
+
+
+def svd_device(A, mode="auto", handle: Handle | None = None, out=None):
+    """SVD of a float32 CUDA tensor (m, n).  Returns (sigma (k,), U (m, k), V (n, k)).
+
+    `out` = (s, Ut, Vt) with Ut of shape (k, m) and Vt of shape (k, n)
+    (the column-major buffers) lets a caller reuse output memory."""
+    import torch
+    h = _handle(handle)
+    m, n = A.shape
+    k = min(m, n)
+    Ac, lda = colmajor(A)
+    if out is None:
+        s = torch.empty(k, dtype=torch.float32, device=A.device)
+        Ut = torch.empty((k, m), dtype=torch.float32, device=A.device)
+        Vt = torch.empty((k, n), dtype=torch.float32, device=A.device)
+    else:
+        s, Ut, Vt = out
+    check(load().ddcsvd_svd_f32_device(h.ptr, m, n, Ac.data_ptr(), lda, s.data_ptr(), Ut.data_ptr(), m,
+                                       Vt.data_ptr(), n, _mode(mode)), "ddcsvd_svd_f32_device")
+    return s, Ut.t(), Vt.t()
+
+
+def svd_device_colmajor(h: Handle, m: int, n: int, Ac, s, Ut, Vt, mode="auto"):
+    """Lowest-level device call on prepared column-major buffers (no copies)."""
+    check(load().ddcsvd_svd_f32_device(h.ptr, m, n, Ac.data_ptr(), m, s.data_ptr(), Ut.data_ptr(), m,
+                                       Vt.data_ptr(), n, _mode(mode)), "ddcsvd_svd_f32_device")
+
+
+def bidiag_device(A, mode="auto", handle: Handle | None = None):
+    """Stage 1 on a float32 CUDA tensor (m >= n).  Returns (W_colmajor (n, ldw), d, e, tauq, taup)."""
+    import torch
+    h = _handle(handle)
+    m, n = A.shape
+    ldw = (m + 31) // 32 * 32
+    W = torch.zeros((n, ldw), dtype=torch.float32, device=A.device)
+    W[:, :m] = A.t()
+    d = torch.zeros(n, dtype=torch.float32, device=A.device)
+    e = torch.zeros(max(n, 1), dtype=torch.float32, device=A.device)
+    tq = torch.zeros(n, dtype=torch.float32, device=A.device)
+    tp = torch.zeros(max(n, 1), dtype=torch.float32, device=A.device)
+    check(load().ddcsvd_bidiag_f32_device(h.ptr, m, n, W.data_ptr(), ldw, d.data_ptr(), e.data_ptr(),
+                                          tq.data_ptr(), tp.data_ptr(), _mode(mode)), "bidiag")
+    return W, d, e[: max(n - 1, 0)], tq, tp[: max(n - 1, 0)]
+
+
+def bdsdc_sigma_device(b1, b2, handle: Handle | None = None):
+    """Stage 2: ascending sigma of the N x (N+1) bidiagonal (float64 CUDA tensors, b2 length N)."""
+    import torch
+    h = _handle(handle)
+    N = b1.shape[0]
+    s = torch.empty(N, dtype=torch.float64, device=b1.device)
+    check(load().ddcsvd_bdsdc_sigma_device(h.ptr, N, b1.contiguous().data_ptr(), b2.contiguous().data_ptr(),
+                                           s.data_ptr()), "bdsdc_sigma")
+    return s
+
+
+def bdvec_device(a, b, sigma, handle: Handle | None = None):
+    """Stages 3-4: (X, Y) right/left vectors of the N x N bidiagonal, as (N, N) with column k = vector k."""
+    import torch
+    h = _handle(handle)
+    N = a.shape[0]
+    Xt = torch.empty((N, N), dtype=torch.float32, device=a.device)
+    Yt = torch.empty((N, N), dtype=torch.float32, device=a.device)
+    bb = torch.zeros(max(N, 1), dtype=torch.float64, device=a.device)
+    bb[: N - 1] = b[: N - 1]
+    check(load().ddcsvd_bdvec_device(h.ptr, N, a.contiguous().data_ptr(), bb.data_ptr(),
+                                     sigma.contiguous().data_ptr(), Xt.data_ptr(), Yt.data_ptr()), "bdvec")
+    return Xt.t(), Yt.t()
+
+
+def svd_batched_device(mats, handle: Handle | None = None):
+    """Batched SVD of a list of float32 CUDA tensors of uneven shapes (one launch sequence).
+
+    Returns a list of (sigma, U, V) like svd_device."""
+    import torch
+    h = _handle(handle)
+    B = len(mats)
+    ms = np.array([a.shape[0] for a in mats], dtype=np.int32)
+    ns = np.array([a.shape[1] for a in mats], dtype=np.int32)
+    ks = np.minimum(ms, ns)
+    offA = np.zeros(B, dtype=np.int64)
+    offS = np.zeros(B, dtype=np.int64)
+    offU = np.zeros(B, dtype=np.int64)
+    offV = np.zeros(B, dtype=np.int64)
+    offA[1:] = np.cumsum(ms.astype(np.int64) * ns)[:-1]
+    offS[1:] = np.cumsum(ks.astype(np.int64))[:-1]
+    offU[1:] = np.cumsum(ms.astype(np.int64) * ks)[:-1]
+    offV[1:] = np.cumsum(ns.astype(np.int64) * ks)[:-1]
+    dev = mats[0].device
+    A = torch.cat([a.t().contiguous().reshape(-1) for a in mats])
+    S = torch.empty(int(ks.sum()), dtype=torch.float32, device=dev)
+    U = torch.empty(int((ms.astype(np.int64) * ks).sum()), dtype=torch.float32, device=dev)
+    V = torch.empty(int((ns.astype(np.int64) * ks).sum()), dtype=torch.float32, device=dev)
+    check(load().ddcsvd_svd_batched_f32_device(h.ptr, B, _addr(ms), _addr(ns), A.data_ptr(), _addr(offA),
+                                               S.data_ptr(), _addr(offS), U.data_ptr(), _addr(offU),
+                                               V.data_ptr(), _addr(offV)), "svd_batched")
+    out = []
+    for b in range(B):
+        m, n, k = int(ms[b]), int(ns[b]), int(ks[b])
+        s = S[offS[b]: offS[b] + k]
+        Ub = U[offU[b]: offU[b] + m * k].view(k, m).t()
+        Vb = V[offV[b]: offV[b] + n * k].view(k, n).t()
+        out.append((s, Ub, Vb))
+    return out
+
+
+def svd_backward_device(U, S, V, gU, gS, gV, handle: Handle | None = None):
+    """Adjoint of the thin SVD for a batch: U (B, m, k), S (B, k), V (B, n, k) -> gA (B, m, n)."""
+    import torch
+    h = _handle(handle)
+    Bt, m, k = U.shape
+    n = V.shape[1]
+    dt = U.dtype
+    fn = load().ddcsvd_svd_backward_f64_device if dt == torch.float64 else load().ddcsvd_svd_backward_f32_device
+
+    def cm(x):  # (B, r, c) -> column-major per matrix
+        return None if x is None else x.transpose(1, 2).contiguous()
+
+    Uc, Vc = cm(U), cm(V)
+    gUc, gVc = cm(gU), cm(gV)
+    Sc = S.contiguous()
+    gSc = None if gS is None else gS.contiguous()
+    gA = torch.empty((Bt, n, m), dtype=dt, device=U.device)
+    ptr = lambda x: 0 if x is None else x.data_ptr()  # noqa: E731
+    check(fn(h.ptr, Bt, m, n, ptr(Uc), ptr(Sc), ptr(Vc), ptr(gUc), ptr(gSc), ptr(gVc), gA.data_ptr()),
+          "svd_backward")
+    return gA.transpose(1, 2)

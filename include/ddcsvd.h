@@ -1,0 +1,174 @@
+/*
+ * ddcsvd.h -- C ABI of libddcsvd.so, a GB300 (sm_103a) implementation of the
+ * ddc-svd dense SVD pipeline.
+ *
+ * Drop-in entry points keep the reference's signatures and argument layout:
+ *   svd_gpu     replaces svd_gpu.h:5   (svd_gpu.c:53-131)
+ *   bidiag_par  replaces bidiag_par.h:30 (bidiag_par.c:34-450)
+ * Everything else extends that interface (status codes, FP32 buffers, device
+ * pointers, batching, the adjoint).  All matrices are column-major.  The
+ * singular values come out ascending, as the reference returns them
+ * (Calculations-Parallel.c:56); column i of U / V belongs to sigma[i].
+ *
+ * Errors: every int-returning function returns DDCSVD_OK (0) or one of the
+ * DDCSVD_ERR_* codes; ddcsvd_last_error() gives a one-line description of the
+ * last failure on the calling thread.  The void drop-ins cannot return a
+ * status; on failure they fill sigma with NaN and print one line to stderr
+ * (the reference aborts the process instead, svd_gpu.c:85).
+ */
+#ifndef DDCSVD_H
+#define DDCSVD_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define DDCSVD_OK 0
+#define DDCSVD_ERR_ARG 1       /* invalid size, stride or pointer            */
+#define DDCSVD_ERR_CUDA 2      /* a CUDA runtime call failed                  */
+#define DDCSVD_ERR_ALLOC 3     /* device or pinned host allocation failed     */
+#define DDCSVD_ERR_NOCONV 4    /* an iteration hit its cap without converging */
+#define DDCSVD_ERR_TIMEOUT 5   /* a device-side wait gave up (bounded spin)   */
+#define DDCSVD_ERR_NODEVICE 6  /* no usable sm_103 device                     */
+#define DDCSVD_ERR_NONFINITE 7 /* input holds NaN or Inf                      */
+#define DDCSVD_ERR_UNSUPPORTED 8
+
+/* ---------------------------------------------------------------- modes
+ * Which bidiagonalisation / back-transformation the pipeline uses.
+ *   PLAIN_FP32   unblocked Householder steps (rank-1 updates), reflectors
+ *                applied one at a time -- the reference's algorithm shape on
+ *                FP32 CUDA cores.
+ *   BLOCKED_FP32 panel (WY / Bischof) bidiagonalisation with rank-2b trailing
+ *                updates and WY back-transformation, FP32 CUDA-core GEMMs.
+ *   BLOCKED_TF32X3 the same with the GEMMs on tcgen05 tensor cores in split
+ *                TF32 (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM).
+ *   BLOCKED_BF16X3 the same in split BF16.
+ *   AUTO         BLOCKED_TF32X3.                                           */
+#define DDCSVD_MODE_AUTO 0
+#define DDCSVD_MODE_PLAIN_FP32 1
+#define DDCSVD_MODE_BLOCKED_FP32 2
+#define DDCSVD_MODE_BLOCKED_TF32X3 3
+#define DDCSVD_MODE_BLOCKED_BF16X3 4
+
+typedef struct ddcsvd_context *ddcsvd_handle_t;
+
+/* ---------------------------------------------------------------- drop-ins */
+
+/* Replaces svd_gpu.h:5 / svd_gpu.c:53.  Host buffers, FP64 in and out.
+ * The reference leaves A overwritten with its Householder reflectors
+ * (bidiag_par.c:63-68); this implementation leaves A unchanged (callers of
+ * the reference cannot rely on A after the call, and bidiag_par below still
+ * returns the reflectors).  sigma: min(m,n) values, ascending.
+ * U: m x min(m,n) (column i at U + i*m); V: n x min(m,n) (column i at V + i*n).
+ * Computes in the default mode (DDCSVD_MODE env var, else AUTO): FP32
+ * bidiagonalisation and back-transformation, FP64 singular values and
+ * bidiagonal vectors. */
+void svd_gpu(int m, int n, double *A, double *sigma, double *U, double *V);
+
+/* Replaces bidiag_par.h:30 / bidiag_par.c:34 (m >= n).  Host buffers.
+ * alpha: min(m,n) diagonal entries, beta: n-1 superdiagonal entries.  A is
+ * overwritten with the reflectors as bidiag_par leaves it: the i-th left
+ * reflector v in the partial column from A[i,i], the i-th right reflector in
+ * the partial row from A[i,i+1], each with H = I - 2 v v^T and ||v|| = 1. */
+void bidiag_par(int m, int n, double *A, double *alpha, double *beta);
+
+/* ---------------------------------------------------------------- status-returning host API */
+
+/* svd_gpu with a status and an explicit mode (DDCSVD_MODE_*). */
+int svd_gpu_ex(int m, int n, double *A, double *sigma, double *U, double *V, int mode);
+
+/* FP32 host buffers, A is not modified.  lda >= m, ldu >= m, ldv >= n. */
+int ddcsvd_svd_f32(int m, int n, const float *A, int lda, float *sigma, float *U, int ldu,
+                   float *V, int ldv, int mode);
+
+/* ---------------------------------------------------------------- handles and device API */
+
+/* A handle owns a CUDA stream, a device workspace and pinned staging memory
+ * on one device.  Calls on one handle are serialised; use one handle per
+ * host thread for concurrency.  device < 0 selects the current device. */
+int ddcsvd_create(ddcsvd_handle_t *handle, int device);
+int ddcsvd_destroy(ddcsvd_handle_t handle);
+/* Work of this handle goes to `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * A new handle starts on a private non-blocking stream. */
+int ddcsvd_set_stream(ddcsvd_handle_t handle, void *stream);
+/* Frees the cached device workspace (it regrows on the next call). */
+int ddcsvd_release_workspace(ddcsvd_handle_t handle);
+
+/* Full SVD, device pointers (FP32).  The call is asynchronous on the
+ * handle's stream except that it reads back one status word at the end. */
+int ddcsvd_svd_f32_device(ddcsvd_handle_t handle, int m, int n, const float *dA, int lda,
+                          float *dSigma, float *dU, int ldu, float *dV, int ldv, int mode);
+
+/* Stage 1 alone: FP32 bidiagonalisation of dA (m >= n) in place.  dA keeps
+ * the reflectors in LAPACK form (unit leading entry implicit, scale in
+ * dTauq / dTaup); dD (n) and dE (n-1) receive the bidiagonal. */
+int ddcsvd_bidiag_f32_device(ddcsvd_handle_t handle, int m, int n, float *dA, int lda,
+                             float *dD, float *dE, float *dTauq, float *dTaup, int mode);
+
+/* Stage 2 alone (Calculations-Parallel.c:852 GetSingularValues_Parallel):
+ * ascending singular values of the N x (N+1) upper bidiagonal with diagonal
+ * dB1 (N) and superdiagonal dB2 (N; dB2[N-1] = 0 gives the square case). */
+int ddcsvd_bdsdc_sigma_device(ddcsvd_handle_t handle, int N, const double *dB1, const double *dB2,
+                              double *dSigma);
+
+/* Stages 3-4 alone (parallel-twisted.c:554 CalcRightSingularVectors and :530
+ * RighttoLeftSingularVectors): right (dX) and left (dY) singular vectors of
+ * the N x N upper bidiagonal (dA diagonal N, dB superdiagonal N-1) for the
+ * given ascending dSigma.  dX, dY: N x N column-major FP32, ld = N. */
+int ddcsvd_bdvec_device(ddcsvd_handle_t handle, int N, const double *dA, const double *dB,
+                        const double *dSigma, float *dX, float *dY);
+
+/* ---------------------------------------------------------------- batched */
+
+/* Many independent SVDs of uneven sizes in one launch sequence (device
+ * pointers).  Matrix b is dA + offA[b] (m[b] x n[b], column-major, ld m[b]);
+ * its results go to dSigma + offS[b] (min(m,n)), dU + offU[b]
+ * (m x min(m,n), ld m) and dV + offV[b] (n x min(m,n), ld n).  Offsets are
+ * element offsets in host arrays. */
+int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t handle, int batch, const int *m, const int *n,
+                                  const float *dA, const long long *offA, float *dSigma,
+                                  const long long *offS, float *dU, const long long *offU,
+                                  float *dV, const long long *offV);
+
+/* ---------------------------------------------------------------- adjoint */
+
+/* Reverse-mode derivative of the thin SVD A = U diag(s) V^T (m >= n, k = n)
+ * for a batch of equally sized matrices (device pointers, FP64 or FP32 by
+ * the _f64/_f32 suffix; strides between matrices are m*k, k, n*k, m*n).
+ * Given dL/ds (gs), dL/dU (gU), dL/dV (gV) -- any may be NULL for zero --
+ * writes dL/dA (gA, m x n):
+ *   gA = U [diag(gs) + (F o (U^T gU - gU^T U)) S + S (F o (V^T gV - gV^T V))] V^T
+ *        + (I - U U^T) gU S^-1 V^T,   F_ij = 1/(s_j^2 - s_i^2) (i != j), 0 on the diagonal. */
+int ddcsvd_svd_backward_f64_device(ddcsvd_handle_t handle, int batch, int m, int n,
+                                   const double *dU, const double *dS, const double *dV,
+                                   const double *gU, const double *gS, const double *gV,
+                                   double *gA);
+int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t handle, int batch, int m, int n,
+                                   const float *dU, const float *dS, const float *dV,
+                                   const float *gU, const float *gS, const float *gV, float *gA);
+
+/* ---------------------------------------------------------------- diagnostics */
+
+const char *ddcsvd_status_string(int status);
+/* Last error description on the calling thread ("" if none). */
+const char *ddcsvd_last_error(void);
+/* Number of kernels this library launched since load (for launch accounting). */
+long long ddcsvd_kernel_launch_count(void);
+/* Device time (ms) of the stages of the last ddcsvd_svd_f32_device call on the
+ * handle when timing is enabled: [bidiag, sigma, vectors, back-transform]. */
+int ddcsvd_set_stage_timing(ddcsvd_handle_t handle, int enable);
+int ddcsvd_get_stage_times(ddcsvd_handle_t handle, float *ms4);
+/* With timing enabled: summed device time (ms) and launch count per kernel
+ * class of the last SVD on the handle: [0] bidiagonalisation kernels,
+ * [1] trailing-update GEMMs, [2] D&C kernel, [3] vector kernels,
+ * [4] back-transformation.  nclass <= 8. */
+int ddcsvd_get_kernel_times(ddcsvd_handle_t handle, float *ms, int *launches, int nclass);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DDCSVD_H */

@@ -1,0 +1,274 @@
+"""GPU parity tests: the CUDA library (through its C ABI) against the FP64
+oracle, LAPACK, and the reference's own outputs (tests/golden).
+
+Tolerances (FP32 pipeline, FP64 singular-value and bidiagonal-vector stages):
+  sig_abs = max|s - s*| / s_max*      <= 1e-5
+  resid   = ||A - U S V^T||_F/||A||_F <= 1e-5
+  orth    = ||Q^T Q - I||_F / sqrt(k) <= 1e-5
+The FP64 references are computed on the FP32-rounded input.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_names, graded
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+BASE_MODES = ["plain", "blocked"]
+
+
+def tc_modes(lib):
+    return [m for m in ("tf32x3", "bf16x3") if _mode_available(lib, m)]
+
+
+_avail = {}
+
+
+def _mode_available(lib, mode):
+    if mode not in _avail:
+        import torch
+        try:
+            lib.svd_device(torch.ones((4, 4), device="cuda"), mode=mode)
+            _avail[mode] = True
+        except lib.DdcsvdError as e:
+            assert e.status == 8, e  # only "unsupported" may mark a mode unavailable
+            _avail[mode] = False
+    return _avail[mode]
+
+
+def run(lib, torch, A, mode):
+    s, U, V = lib.svd_device(torch.from_numpy(np.asarray(A, dtype=np.float32)).cuda(), mode=mode)
+    torch.cuda.synchronize()
+    return s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy()
+
+
+def check_metrics(orc, A, s, U, V, tol=TOL, sig_true=None):
+    A64 = np.asarray(A, dtype=np.float32).astype(np.float64)
+    if sig_true is None:
+        sig_true = np.linalg.svd(A64, compute_uv=False)
+    met = orc.metrics(A64, s, U, V, sig_true)
+    assert np.all(np.diff(s) >= 0), "singular values must come out ascending"
+    assert met["sig_abs"] <= tol and met["resid"] <= tol, met
+    assert met["orth_u"] <= tol and met["orth_v"] <= tol, met
+    return met
+
+
+# ------------------------------------------------------------------ end to end
+SHAPES = [(1, 1), (2, 2), (3, 3), (2, 1), (1, 3), (5, 3), (3, 5), (17, 17), (33, 20), (64, 64), (100, 37),
+          (20, 33), (128, 96), (257, 129), (512, 256)]
+
+
+@pytest.mark.parametrize("mode", BASE_MODES)
+@pytest.mark.parametrize("m,n", SHAPES)
+def test_svd_uniform(lib, cuda, orc, mode, m, n):
+    rng = np.random.default_rng(m * 7919 + n)
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    s, U, V = run(lib, cuda, A, mode)
+    check_metrics(orc, A, s, U, V)
+
+
+@pytest.mark.parametrize("m,n", [(64, 64), (257, 129), (512, 256), (300, 1000)])
+def test_svd_tensor_core_modes(lib, cuda, orc, m, n):
+    modes = tc_modes(lib)
+    if not modes:
+        pytest.skip("tensor-core modes not built")
+    rng = np.random.default_rng(m + n)
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    for mode in modes:
+        s, U, V = run(lib, cuda, A, mode)
+        check_metrics(orc, A, s, U, V)
+
+
+@pytest.mark.parametrize("mode", BASE_MODES)
+@pytest.mark.parametrize("kind", ["identity", "zero", "diag_repeated", "rank_deficient", "graded", "block"])
+def test_svd_structured(lib, cuda, orc, mode, kind):
+    n = 96
+    rng = np.random.default_rng(5)
+    if kind == "identity":
+        A = np.eye(n)
+    elif kind == "zero":
+        A = np.zeros((n, n))
+    elif kind == "diag_repeated":
+        A = np.diag(np.repeat([3.0, 2.0, 1.0], n // 3))
+    elif kind == "rank_deficient":
+        A = rng.standard_normal((n, 7)) @ rng.standard_normal((7, n))
+    elif kind == "graded":
+        A, _ = graded(n)
+    else:
+        A = np.zeros((n, n))
+        A[:40, :40] = rng.standard_normal((40, 40))
+        A[40:, 40:] = rng.standard_normal((n - 40, n - 40))
+    s, U, V = run(lib, cuda, A, mode)
+    A64 = A.astype(np.float32).astype(np.float64)
+    st = np.linalg.svd(A64, compute_uv=False)
+    assert np.max(np.abs(np.sort(s) - np.sort(st))) <= TOL * max(st.max(), 1e-30)
+    if kind != "zero":
+        check_metrics(orc, A, s, U, V)
+
+
+@pytest.mark.parametrize("mode", BASE_MODES)
+def test_svd_graded_1024(lib, cuda, orc, mode):
+    A, s_true = graded(1024, seed=1)
+    s, U, V = run(lib, cuda, A, mode)
+    check_metrics(orc, A, s, U, V)
+
+
+def test_svd_matches_oracle_vectors(lib, cuda, orc):
+    """Per-vector agreement with the FP64 oracle (up to sign) where sigma is well separated."""
+    rng = np.random.default_rng(21)
+    A = rng.uniform(-1, 1, (200, 120)).astype(np.float32)
+    s, U, V = run(lib, cuda, A, "blocked")
+    so, Uo, Vo = orc.svd(A.astype(np.float64))
+    assert np.max(np.abs(s - so)) <= 1e-5 * so.max()
+    gaps = np.diff(so)
+    gap = np.minimum(np.r_[np.inf, gaps], np.r_[gaps, np.inf]) / so.max()
+    for k in np.nonzero(gap > 1e-3)[0]:
+        assert abs(abs(U[:, k] @ Uo[:, k]) - 1) < 1e-4
+        assert abs(abs(V[:, k] @ Vo[:, k]) - 1) < 1e-4
+
+
+def test_deterministic(lib, cuda):
+    rng = np.random.default_rng(3)
+    A = rng.uniform(-1, 1, (300, 200)).astype(np.float32)
+    r1 = run(lib, cuda, A, "blocked")
+    r2 = run(lib, cuda, A, "blocked")
+    for a, b in zip(r1, r2):
+        assert np.array_equal(a, b)
+
+
+def test_nonfinite_input_fails_loudly(lib, cuda):
+    A = np.ones((16, 8), dtype=np.float32)
+    A[3, 2] = np.nan
+    with pytest.raises(lib.DdcsvdError) as ei:
+        run(lib, cuda, A, "blocked")
+    assert ei.value.status == 7
+    s, U, V = run(lib, cuda, np.eye(8, dtype=np.float32), "blocked")  # handle still usable
+    assert np.allclose(s, 1.0)
+
+
+# ------------------------------------------------------------------ stage parity
+@pytest.mark.parametrize("mode", BASE_MODES)
+@pytest.mark.parametrize("m,n", [(8, 8), (33, 20), (100, 100), (260, 130), (513, 300)])
+def test_bidiag_stage_vs_oracle(lib, cuda, orc, mode, m, n):
+    rng = np.random.default_rng(m * 31 + n)
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    W, d, e, tq, tp = lib.bidiag_device(cuda.from_numpy(A).cuda(), mode=mode)
+    _, al, be = orc.bidiag(A.astype(np.float64))
+    d = d.double().cpu().numpy()
+    e = e.double().cpu().numpy()
+    scale = np.linalg.norm(A, 2)
+    # same reflector sign convention as the reference: entries agree, not only |entries|
+    assert np.max(np.abs(d - al)) <= 2e-5 * scale
+    assert np.max(np.abs(e - be)) <= 2e-5 * scale
+
+
+@pytest.mark.parametrize("name", [g for g in golden_names("bidiag_") if
+                                  (lambda s: int(s.split("_")[1].split("x")[0]) >= int(s.split("x")[1]))(g)])
+def test_bidiag_par_dropin_vs_reference(lib, cuda, name):
+    g = golden(name)
+    A_r, al, be = lib.bidiag_par(g["A"])
+    scale = np.abs(g["A"]).max() * max(g["A"].shape)
+    assert np.max(np.abs(al - g["alpha"])) <= 1e-5 * scale
+    assert np.max(np.abs(be - g["beta"])) <= 1e-5 * scale
+    ok = np.isfinite(g["A_refl"])
+    assert np.max(np.abs(A_r[ok] - g["A_refl"][ok])) <= 1e-4
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 7, 64, 300, 1000])
+@pytest.mark.parametrize("rect", [False, True])
+def test_dc_stage_vs_oracle(lib, cuda, orc, N, rect):
+    rng = np.random.default_rng(N + 100 * rect)
+    b1 = rng.uniform(0.2, 2.0, N)
+    b2 = rng.uniform(0.2, 2.0, N)
+    if not rect:
+        b2[-1] = 0.0
+    s = lib.bdsdc_sigma_device(cuda.from_numpy(b1).cuda(), cuda.from_numpy(b2).cuda()).cpu().numpy()
+    so = orc.dc_sigma(b1, b2)
+    assert np.max(np.abs(s - so)) <= 1e-13 * so.max()
+    assert np.max(np.abs(s - so) / so) <= 1e-11
+
+
+@pytest.mark.parametrize("kind", ["graded", "split", "repeated", "tiny_z"])
+def test_dc_stage_hard_cases(lib, cuda, orc, kind):
+    N = 257
+    rng = np.random.default_rng(9)
+    b1 = rng.uniform(0.5, 1.5, N)
+    b2 = rng.uniform(0.5, 1.5, N)
+    b2[-1] = 0.0
+    if kind == "graded":
+        b1 *= 10.0 ** (-6 * np.arange(N) / N)
+        b2 *= 10.0 ** (-6 * np.arange(N) / N)
+    elif kind == "split":
+        b2[[10, 11, 100, 200]] = 0.0
+    elif kind == "repeated":
+        b1[:] = 1.0
+        b2[::2] = 0.0
+    else:
+        b2[50:60] = 1e-18
+    s = lib.bdsdc_sigma_device(cuda.from_numpy(b1).cuda(), cuda.from_numpy(b2).cuda()).cpu().numpy()
+    so, _, _ = orc.bdsvd(b1, b2)
+    B = np.diag(b1) + np.diag(b2[:-1], 1)
+    st = np.sort(np.linalg.svd(B, compute_uv=False))
+    assert np.max(np.abs(s - st)) <= 1e-12 * st.max()
+    assert np.max(np.abs(s - so)) <= 1e-12 * st.max()
+
+
+@pytest.mark.parametrize("N", [1, 2, 5, 64, 500])
+@pytest.mark.parametrize("kind", ["uniform", "graded", "split"])
+def test_vector_stage_vs_oracle(lib, cuda, orc, N, kind):
+    rng = np.random.default_rng(N * 3 + len(kind))
+    a = rng.uniform(0.5, 1.5, N)
+    b = rng.uniform(0.5, 1.5, max(N - 1, 0))
+    if kind == "graded":
+        a *= 10.0 ** (-6 * np.arange(N) / max(N, 1))
+        b *= 10.0 ** (-6 * np.arange(1, N) / max(N, 1))
+    elif kind == "split" and N > 4:
+        b[N // 2] = 0.0
+    so, Xo, b_split = orc.bdsvd(a, b)
+    T = cuda
+    s_gpu = lib.bdsdc_sigma_device(T.from_numpy(a).cuda(), T.from_numpy(np.r_[b, 0.0]).cuda())
+    X, Y = lib.bdvec_device(T.from_numpy(a).cuda(), T.from_numpy(np.r_[b, 0.0]).cuda(), s_gpu)
+    X = X.double().cpu().numpy()
+    Y = Y.double().cpu().numpy()
+    k = N
+    assert np.linalg.norm(X.T @ X - np.eye(k)) / np.sqrt(k) <= 1e-6
+    assert np.linalg.norm(Y.T @ Y - np.eye(k)) / np.sqrt(k) <= 1e-6
+    B = np.diag(a) + (np.diag(b_split, 1) if N > 1 else 0)
+    R = B @ X - Y * so
+    assert np.linalg.norm(R) <= 1e-6 * np.linalg.norm(B) * np.sqrt(k)
+    for j in range(N):  # per vector, against the oracle (FP32 output)
+        assert abs(abs(X[:, j] @ Xo[:, j]) - 1) <= 1e-6
+
+
+# ------------------------------------------------------------------ drop-ins vs the reference
+@pytest.mark.parametrize("name", golden_names("svd_"))
+def test_svd_gpu_dropin_vs_reference(lib, cuda, orc, name):
+    g = golden(name)
+    s, U, V = lib.svd_gpu(g["A"])
+    smax = g["sigma_lapack"].max()
+    assert np.all(np.diff(s) >= 0)
+    assert np.max(np.abs(s - g["sigma_lapack"])) <= 1e-5 * smax  # vs LAPACK (FP64)
+    if np.all(np.isfinite(g["sigma"])):
+        assert np.max(np.abs(s - g["sigma"])) <= 1e-4 * smax     # vs the reference, to its accuracy
+    check_metrics(orc, g["A"], s, U, V, sig_true=g["sigma_lapack"])
+    gaps = np.diff(s)
+    gap = np.minimum(np.r_[np.inf, gaps], np.r_[gaps, np.inf]) / smax
+    Ur = g["U"].astype(np.float64)
+    for k in range(len(s)):
+        if gap[k] > 1e-2 and np.all(np.isfinite(Ur[:, k])):
+            assert abs(abs(U[:, k] @ Ur[:, k]) / np.linalg.norm(Ur[:, k]) - 1) < 1e-3
+
+
+def test_void_dropin_signature(lib, cuda):
+    rng = np.random.default_rng(1)
+    A = rng.uniform(1, 4, (40, 40))
+    s, U, V = lib.svd_gpu_void(A)
+    assert np.allclose(np.sort(s), np.sort(np.linalg.svd(A, compute_uv=False)), rtol=0, atol=1e-5 * 40 * 2.5)
+
+
+def test_host_f32_api(lib, cuda, orc):
+    rng = np.random.default_rng(2)
+    A = rng.uniform(-1, 1, (150, 90)).astype(np.float32)
+    s, U, V = lib.svd(A)
+    check_metrics(orc, A, s.astype(np.float64), U.astype(np.float64), V.astype(np.float64))
