@@ -218,8 +218,42 @@ static int stage_event(ddcsvd_context* ctx, int k) {
 // Full SVD of the m x n (m >= n) device matrix dA.  Workspace: region A
 // (matrix, bidiagonal, sigma) persists through the call; region B is scratch
 // reused by each stage in turn.
+static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
+                         int ldu, float* dV, int ldv, int mode, bool check_finite);
+
+__global__ void copy2d_kernel(int rows, int cols, const float* __restrict__ src, int lds, float* dst, int ldd) {
+  const int c = blockIdx.y;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    dst[r + (size_t)c * ldd] = src[r + (size_t)c * lds];
+}
+
+// The tensor-core back-transformation reads U and V through TMA, which needs
+// 16-byte aligned bases and leading dimensions; other layouts go through
+// aligned staging buffers.
 static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                     int ldu, float* dV, int ldv, int mode, bool check_finite) {
+  const bool tcmode = (mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3);
+  auto ok = [](const float* p, int ld) { return ((reinterpret_cast<uintptr_t>(p) & 15) == 0) && (ld % 4 == 0); };
+  if (!tcmode || (ok(dU, ldu) && ok(dV, ldv)))
+    return svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
+  const int lu = (int)round_up(m, 4), lv = (int)round_up(n, 4);
+  float* buf = nullptr;
+  DDC_CUDA_TRY(cudaMallocAsync((void**)&buf, sizeof(float) * ((size_t)lu * n + (size_t)lv * n + 64), ctx->stream));
+  float* Ui = buf;
+  float* Vi = buf + (size_t)lu * n + 32;
+  int rc = svd_core_impl(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite);
+  if (rc == DDCSVD_OK) {
+    copy2d_kernel<<<dim3(ceil_div(m, 256), n), 256, 0, ctx->stream>>>(m, n, Ui, lu, dU, ldu);
+    copy2d_kernel<<<dim3(ceil_div(n, 256), n), 256, 0, ctx->stream>>>(n, n, Vi, lv, dV, ldv);
+    count_launch(2);
+  }
+  cudaFreeAsync(buf, ctx->stream);
+  if (rc == DDCSVD_OK) rc = check_status(ctx, "svd");
+  return rc;
+}
+
+static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
+                         int ldu, float* dV, int ldv, int mode, bool check_finite) {
   const bool plain = (mode == DDCSVD_MODE_PLAIN_FP32);
   const GemmKind kind = kind_of(mode);
   const int P = bidiag_coop_ctas(ctx, m, n);
@@ -510,6 +544,7 @@ int ddcsvd_get_stage_times(ddcsvd_handle_t h, float* ms4) {
 
 int ddcsvd_svd_f32_device(ddcsvd_handle_t h, int m, int n, const float* dA, int lda, float* dSigma,
                           float* dU, int ldu, float* dV, int ldv, int mode) {
+  t_last_error.clear();
   if (!h || m <= 0 || n <= 0 || !dA || !dSigma || !dU || !dV) return DDCSVD_ERR_ARG;
   if (lda < m || ldu < m || ldv < n) return DDCSVD_ERR_ARG;
   std::lock_guard<std::mutex> g(h->mu);
@@ -686,6 +721,7 @@ static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda
 
 int ddcsvd_svd_f32(int m, int n, const float* A, int lda, float* sigma, float* U, int ldu, float* V, int ldv,
                    int mode) {
+  t_last_error.clear();
   if (m <= 0 || n <= 0 || !A || !sigma || !U || !V || lda < m || ldu < m || ldv < n) return DDCSVD_ERR_ARG;
   ddcsvd_context* h;
   DDC_TRY(default_ctx(&h));
@@ -694,6 +730,7 @@ int ddcsvd_svd_f32(int m, int n, const float* A, int lda, float* sigma, float* U
 }
 
 int svd_gpu_ex(int m, int n, double* A, double* sigma, double* U, double* V, int mode) {
+  t_last_error.clear();
   if (m <= 0 || n <= 0 || !A || !sigma || !U || !V) return DDCSVD_ERR_ARG;
   ddcsvd_context* h;
   DDC_TRY(default_ctx(&h));
@@ -724,6 +761,7 @@ void svd_gpu(int m, int n, double* A, double* sigma, double* U, double* V) {
 }
 
 void bidiag_par(int m, int n, double* A, double* alpha, double* beta) {
+  t_last_error.clear();
   int rc = DDCSVD_OK;
   ddcsvd_context* h = nullptr;
   if (m <= 0 || n <= 0 || !A || !alpha || !beta || m < n) rc = DDCSVD_ERR_ARG;

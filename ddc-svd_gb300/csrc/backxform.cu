@@ -22,16 +22,19 @@ namespace ddcsvd {
 //                 row l of the block; block rows = W rows j0 ...
 // side 1 (right): reflector j0+l is row j0+l of W from column j0+l+1, unit
 //                 at row l of the block; block rows = positions j0+1 ...
-__global__ void pack_reflectors_kernel(int side, int rows, int bs, int j0, const float* __restrict__ W,
+// Block rows are shifted down by `sh` (< 4) zero rows so that the first row
+// touched in C starts on a 16-byte boundary (tensor-memory-access rule).
+__global__ void pack_reflectors_kernel(int side, int rows, int bs, int j0, int sh, const float* __restrict__ W,
                                        int ldw, const float* __restrict__ tau, float* P, int ldp) {
   const int l = blockIdx.y;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+  for (int rp = blockIdx.x * blockDim.x + threadIdx.x; rp < rows + sh; rp += gridDim.x * blockDim.x) {
+    const int r = rp - sh;
     float v;
-    if (l >= bs || tau[j0 + l] == 0.f) v = 0.f;  // absent / identity reflector
+    if (r < 0 || l >= bs || tau[j0 + l] == 0.f) v = 0.f;  // alignment pad / absent / identity reflector
     else if (r < l) v = 0.f;
     else if (r == l) v = 1.f;
     else v = side == 0 ? W[(j0 + r) + (size_t)(j0 + l) * ldw] : W[(j0 + l) + (size_t)(j0 + 1 + r) * ldw];
-    P[r + (size_t)l * ldp] = v;
+    P[rp + (size_t)l * ldp] = v;
   }
 }
 
@@ -62,8 +65,10 @@ __global__ void wy_tfactor_kernel(int bs, int j0, const float* __restrict__ tau,
 static int apply_blocked(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W,
                          int ldw, const float* tau, float* C, int ldc, int ncols, GemmKind kind,
                          Arena& a, bool plan_only) {
-  const int ldp = (int)round_up(rows_total + 1, 32);
+  const bool tc = (kind != GEMM_SIMT);
+  const int ldp = (int)round_up(rows_total + 4, 32);
   float* Pk = a.take<float>((size_t)ldp * kWY);
+  float* PkT = a.take<float>(tc ? (size_t)ldp * kWY : 16);
   float* G = a.take<float>(kWY * kWY);
   float* T = a.take<float>(kWY * kWY);
   float* W1 = a.take<float>((size_t)kWY * ncols);
@@ -75,32 +80,42 @@ static int apply_blocked(ddcsvd_context* ctx, int side, int rows_total, int nref
   scratch.base = sc;
   scratch.plan = false;
   scratch.cap = sbytes;
+  Mat none{nullptr, 0, 0};
   const int nblk = ceil_div(nref, kWY);
   for (int bi = nblk - 1; bi >= 0; bi--) {
     const int j0 = bi * kWY;
     const int bs = std::min(kWY, nref - j0);
     const int off = side == 0 ? j0 : j0 + 1;  // first row of C touched
-    const int rows = rows_total - off;
-    if (rows <= 0) continue;
+    if (rows_total - off <= 0) continue;
+    const int off_al = off & ~3, sh = off - off_al;
+    const int rows = rows_total - off_al;  // block rows, including the sh zero rows on top
     dim3 g(std::min(ceil_div(rows, 256), 64), bs);
-    pack_reflectors_kernel<<<g, 256, 0, ctx->stream>>>(side, rows, bs, j0, W, ldw, tau, Pk, ldp);
+    pack_reflectors_kernel<<<g, 256, 0, ctx->stream>>>(side, rows - sh, bs, j0, sh, W, ldw, tau, Pk, ldp);
     count_launch();
     DDC_CUDA_TRY(cudaGetLastError());
     Mat UT{Pk, ldp, 1}, U{Pk, 1, ldp};
-    Mat none{nullptr, 0, 0};
-    // G = U^T U  (bs x bs)
+    // G = U^T U (bs x bs) and the triangular factor T
     DDC_TRY(gemm(ctx, GEMM_SIMT, bs, bs, rows, UT, U, 0, none, none, 1.f, 0.f, G, bs, &scratch));
     wy_tfactor_kernel<<<1, kWY, 0, ctx->stream>>>(bs, j0, tau, G, T);
     count_launch();
-    // W1 = U^T C  (bs x ncols)
-    Mat Cb{C + off, 1, ldc};
-    DDC_TRY(gemm(ctx, kind, bs, ncols, rows, UT, Cb, 0, none, none, 1.f, 0.f, W1, bs, &scratch));
-    // W2 = T W1
-    DDC_TRY(gemm(ctx, GEMM_SIMT, bs, ncols, bs, Mat{T, 1, bs}, Mat{W1, 1, bs}, 0, none, none, 1.f, 0.f,
-                 W2, bs, &scratch));
-    // C -= U W2
-    DDC_TRY(gemm(ctx, kind, rows, ncols, bs, U, Mat{W2, 1, bs}, 0, none, none, -1.f, 1.f, C + off, ldc,
-                 &scratch));
+    float* Cb = C + off_al;
+    if (!tc) {
+      // W1 = U^T C (bs x ncols); W2 = T W1; C -= U W2
+      DDC_TRY(gemm(ctx, kind, bs, ncols, rows, UT, Mat{Cb, 1, ldc}, 0, none, none, 1.f, 0.f, W1, bs, &scratch));
+      DDC_TRY(gemm(ctx, GEMM_SIMT, bs, ncols, bs, Mat{T, 1, bs}, Mat{W1, 1, bs}, 0, none, none, 1.f, 0.f, W2, bs,
+                   &scratch));
+      DDC_TRY(gemm(ctx, kind, rows, ncols, bs, U, Mat{W2, 1, bs}, 0, none, none, -1.f, 1.f, Cb, ldc, &scratch));
+    } else {
+      // W1^T = C^T U (ncols x bs): C is already K-major for this product
+      DDC_TRY(gemm_tc_kmajor(ctx, kind, ncols, bs, rows, C, ldc, off_al, Pk, ldp, 0, W1, ncols, 1.f, 0.f,
+                             &scratch));
+      // W2 = T W1 (bs x ncols, col-major with ld kWY: K-major rows, 16-byte aligned for any bs)
+      DDC_TRY(gemm(ctx, GEMM_SIMT, bs, ncols, bs, Mat{T, 1, bs}, Mat{W1, ncols, 1}, 0, none, none, 1.f, 0.f, W2,
+                   kWY, &scratch));
+      // C -= U W2 with U packed K-major (rows x bs, ld kWY)
+      DDC_TRY(pack_kmajor(ctx, rows, bs, Pk, ldp, 0, nullptr, 0, PkT, kWY));
+      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, PkT, kWY, 0, W2, kWY, 0, Cb, ldc, -1.f, 1.f, &scratch));
+    }
   }
   return DDCSVD_OK;
 }

@@ -69,6 +69,7 @@ __device__ __forceinline__ void householder(float x0, double t2, float* alpha, f
 
 // sum_{r in [r0, r1)} col[r] * xs[r]; col in global (16B-aligned base), xs in
 // shared memory indexed absolutely.  Warp-cooperative, result in all lanes.
+// Eight 16-byte loads per lane are kept in flight.
 __device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, const float* xs, int r0,
                                               int r1, int lane) {
   float acc = 0.f;
@@ -81,14 +82,15 @@ __device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, con
   const float4* x4 = reinterpret_cast<const float4*>(xs + a0);
   const int nq = (a1 - a0) >> 2;
   int q = lane;
-  for (; q + 96 < nq; q += 128) {
-    float4 w0 = __ldcg(c4 + q), w1 = __ldcg(c4 + q + 32), w2 = __ldcg(c4 + q + 64),
-           w3 = __ldcg(c4 + q + 96);
-    float4 v0 = x4[q], v1 = x4[q + 32], v2 = x4[q + 64], v3 = x4[q + 96];
-    acc += w0.x * v0.x + w0.y * v0.y + w0.z * v0.z + w0.w * v0.w;
-    acc += w1.x * v1.x + w1.y * v1.y + w1.z * v1.z + w1.w * v1.w;
-    acc += w2.x * v2.x + w2.y * v2.y + w2.z * v2.z + w2.w * v2.w;
-    acc += w3.x * v3.x + w3.y * v3.y + w3.z * v3.z + w3.w * v3.w;
+  for (; q + 224 < nq; q += 256) {
+    float4 w[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) w[u] = __ldcg(c4 + q + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const float4 v = x4[q + 32 * u];
+      acc += w[u].x * v.x + w[u].y * v.y + w[u].z * v.z + w[u].w * v.w;
+    }
   }
   for (; q < nq; q += 32) {
     float4 w0 = __ldcg(c4 + q);
@@ -100,6 +102,7 @@ __device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, con
 
 // Row-block GEMV: out[r - ra] = sum_{c in [c0, n)} W[r, c] * xs[c] for the
 // CTA's float4-aligned row block [ra, ra + 4*R4).  red: blockDim float4s.
+// Each thread keeps eight 16-byte loads in flight.
 __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int ldw, int ra,
                                                 int R4, int c0, int n, const float* xs,
                                                 float4* red, float* out) {
@@ -110,16 +113,19 @@ __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int
   if (g < G) {
     const float* base = W + ra + 4 * q;
     int c = c0 + g;
-    for (; c + 3 * G < n; c += 4 * G) {
-      float4 w0 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)c * ldw));
-      float4 w1 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + G) * ldw));
-      float4 w2 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + 2 * G) * ldw));
-      float4 w3 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + 3 * G) * ldw));
-      float x0 = xs[c], x1 = xs[c + G], x2 = xs[c + 2 * G], x3 = xs[c + 3 * G];
-      acc.x += w0.x * x0 + w1.x * x1 + w2.x * x2 + w3.x * x3;
-      acc.y += w0.y * x0 + w1.y * x1 + w2.y * x2 + w3.y * x3;
-      acc.z += w0.z * x0 + w1.z * x1 + w2.z * x2 + w3.z * x3;
-      acc.w += w0.w * x0 + w1.w * x1 + w2.w * x2 + w3.w * x3;
+    for (; c + 7 * G < n; c += 8 * G) {
+      float4 w[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        w[u] = __ldcg(reinterpret_cast<const float4*>(base + (size_t)(c + u * G) * ldw));
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const float x = xs[c + u * G];
+        acc.x += w[u].x * x;
+        acc.y += w[u].y * x;
+        acc.z += w[u].z * x;
+        acc.w += w[u].w * x;
+      }
     }
     for (; c < n; c += G) {
       float4 w0 = __ldcg(reinterpret_cast<const float4*>(base + (size_t)c * ldw));
@@ -144,19 +150,84 @@ __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int
   __syncthreads();
 }
 
+// Ordered sum over the P per-CTA partial records of `cnt` floats (+ one FP64
+// norm): every thread of the CTA loads a share of the records into shared
+// memory, then thread q adds column q in CTA order (deterministic).
+__device__ __forceinline__ void reduce_partials(const float* __restrict__ part, const double* __restrict__ nrm,
+                                                int P, int cnt, float* stage, float* tot, double* dtot) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int total = P * cnt;
+  // every thread issues up to 8 independent loads before storing any of them
+  for (int base = t; base < total; base += 8 * nt) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int idx = base + u * nt;
+      v[u] = 0.f;
+      if (idx < total) {
+        const int b = idx / cnt;
+        v[u] = __ldcg(part + (size_t)b * kPS + (idx - b * cnt));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int idx = base + u * nt;
+      if (idx < total) stage[idx] = v[u];
+    }
+  }
+  if (t >= 32 && t < 64) {  // one warp sums the FP64 norms
+    double v[8];
+    const int l = t - 32;
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = (l + 32 * u < P) ? __ldcg(nrm + l + 32 * u) : 0.0;
+    double acc = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) acc += v[u];
+    for (int b = l + 256; b < P; b += 32) acc += __ldcg(nrm + b);
+    acc = warp_sum(acc);
+    if (t == 32) *dtot = acc;
+  }
+  __syncthreads();
+  if (t < cnt) {
+    float acc = 0.f;
+    for (int b = 0; b < P; b++) acc += stage[b * cnt + t];
+    tot[t] = acc;
+  }
+  __syncthreads();
+}
+
+// Copies src[lo, hi) into the absolutely indexed shared buffer dst with
+// 16-byte loads (dst and src share the same alignment; entries below lo in
+// the first vector are copied too and never read).
+__device__ __forceinline__ void stage_vec(float* dst, const float* __restrict__ src, int lo, int hi) {
+  const int a = lo & ~3;
+  const int nv = (hi - a + 3) >> 2;
+  const float4* s4 = reinterpret_cast<const float4*>(src + a);
+  float4* d4 = reinterpret_cast<float4*>(dst + a);
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) d4[q] = __ldcg(s4 + q);
+}
+
 // Shared-memory layout of the panel kernel (floats unless noted).
+constexpr int kLD = kPanel + 1;  // padded row length of the cached panel blocks
 struct PanelSmem {
   float* big;     // max(m, n) + 4: xcol / xrow by absolute index
   float4* red;    // blockDim
   float* own;     // rc: own rows' x (S1) / GEMV output (S6)
   float* owncol;  // cc: own columns' updated row values
   float* ypart;   // cc * 8: column dot partials
+  float* UpS;     // rc x kLD: own rows of the panel's left reflectors
+  float* XS;      // rc x kLD: own rows of X
+  float* YS;      // cc x kLD: own columns of Y
+  float* VTS;     // cc x kLD: own columns of VT
+  float* stage;   // P * (2 kPanel + 2): partial records
+  float* pre;     // max(rc, cc): prefetched original row/column entries
+  float* misc;    // 8: prefetched scalars
   float *Yi, *VTi, *Wi, *Xi, *p1, *p2, *q1, *q2, *tot;
   double* dred;   // 32
   float* scal;    // 8
 };
 
-__device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc) {
+__device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
   PanelSmem s;
   float* p = smem;
   s.big = p;
@@ -169,6 +240,13 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc) {
   p += round_up(cc + 4, 4);
   s.ypart = p;
   p += round_up(cc * 8 + 4, 4);
+  s.UpS = p; p += rc * kLD;
+  s.XS = p; p += rc * kLD;
+  s.YS = p; p += cc * kLD;
+  s.VTS = p; p += cc * kLD;
+  s.stage = p; p += P * (2 * kPanel + 2);
+  s.pre = p; p += round_up(max(rc, cc) + 4, 4);
+  s.misc = p; p += 8;
   s.Yi = p; p += kPanel + 4;
   s.VTi = p; p += kPanel + 4;
   s.Wi = p; p += kPanel + 4;
@@ -185,9 +263,11 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc) {
   return s;
 }
 
-size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads) {
-  size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) +
-             round_up(cc + 4, 4) + round_up(cc * 8 + 4, 4) + 8 * (kPanel + 4) + kPS + 4 + 4 + 64 + 8;
+size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P) {
+  size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
+             round_up(cc * 8 + 4, 4) + 2 * (size_t)rc * kLD + 2 * (size_t)cc * kLD +
+             (size_t)P * (2 * kPanel + 2) + round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
+             64 + 8;
   return f * sizeof(float) + 64;
 }
 
@@ -195,7 +275,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
   extern __shared__ __align__(16) float smem[];
   const int m = p.m, n = p.n, k0 = p.k0, ldw = p.ldw, ldn = p.ldn;
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
-  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc);
+  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc, p.P);
   float* W = p.W;
   float *X = p.X, *Y = p.Y, *VT = p.VT;
   // static partitions for this panel
@@ -207,67 +287,60 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
   for (int j = 0; j < p.nb; j++) {
     const int i = k0 + j;
     // ---------------- S1: update column i on own rows, partial sums
+    const int r_s = max(ra, i);
+    const int nrow = max(0, rb - r_s);
+    // one round trip: row i of Y / VT and the own rows of column i
     if (t < j) {
       S.Yi[t] = __ldcg(Y + i + (size_t)t * ldn);
       // VT[i, t]: row t of the panel's right reflectors at column i; the entry
       // of the previous step (t = j-1) is its unit leading element.
       S.VTi[t] = (t == j - 1) ? (prev_taup != 0.f ? 1.f : 0.f) : __ldcg(VT + i + (size_t)t * ldn);
     }
+    for (int rr = t; rr < nrow; rr += blockDim.x) S.pre[rr] = __ldcg(W + r_s + rr + (size_t)i * ldw);
     __syncthreads();
-    const int r_s = max(ra, i);
-    const int nrow = max(0, rb - r_s);
-    for (int rr = t; rr < nrow; rr += blockDim.x) {
-      const int r = r_s + rr;
-      float x = __ldcg(W + r + (size_t)i * ldw);
-      for (int l = 0; l < j; l++)
-        x -= __ldcg(W + r + (size_t)(k0 + l) * ldw) * S.Yi[l] +
-             __ldcg(X + r + (size_t)l * ldw) * S.VTi[l];
-      S.own[rr] = x;
-      p.xcol[r] = x;
+    for (int rr = wid; rr < nrow; rr += nw) {  // warp per row, lanes over l
+      const int r = r_s + rr, lr = r - ra;
+      float part = 0.f;
+      if (lane < j) part = S.UpS[lr * kLD + lane] * S.Yi[lane] + S.XS[lr * kLD + lane] * S.VTi[lane];
+      part = warp_sum(part);
+      if (lane == 0) {
+        const float x = S.pre[rr] - part;
+        S.own[rr] = x;
+        p.xcol[r] = x;
+      }
     }
     __syncthreads();
     {
-      // partial sums over own rows r > i: [0] ||x||^2 (FP64), [1..j] W^T x, [1+j..2j] X^T x
+      // partial sums over own rows r > i: [0] ||x||^2 (FP64), [1..j] Up^T x, [1+j..2j] X^T x
       const int r1 = max(r_s, i + 1);
-      for (int q = wid; q < 2 * j + 1; q += nw) {
-        if (q == 0) {
-          double acc = 0.0;
-          for (int r = r1 + lane; r < rb; r += 32) {
-            double x = S.own[r - r_s];
-            acc += x * x;
-          }
-          acc = warp_sum(acc);
-          if (lane == 0) p.colnrm[b] = acc;
-        } else {
-          const float* src = (q <= j) ? (W + (size_t)(k0 + q - 1) * ldw) : (X + (size_t)(q - 1 - j) * ldw);
-          float acc = 0.f;
-          for (int r = r1 + lane; r < rb; r += 32) acc += __ldcg(src + r) * S.own[r - r_s];
-          acc = warp_sum(acc);
-          if (lane == 0) p.colpart[(size_t)b * kPS + q] = acc;
+      if (wid == 0) {
+        double acc = 0.0;
+        for (int r = r1 + lane; r < rb; r += 32) {
+          double x = S.own[r - r_s];
+          acc += x * x;
         }
+        acc = warp_sum(acc);
+        if (lane == 0) p.colnrm[b] = acc;
+      }
+      if (t >= 32 && t < 32 + 2 * j) {
+        const int q = t - 32;
+        const float* src = (q < j) ? (S.UpS + q) : (S.XS + (q - j));
+        float acc = 0.f;
+        for (int r = r1; r < rb; r++) acc += src[(r - ra) * kLD] * S.own[r - r_s];
+        p.colpart[(size_t)b * kPS + 1 + q] = acc;
       }
     }
     if (!grid_sync(p.bar, p.P, p.st, 1)) return;
 
     // ---------------- S2: column reflector
-    if (t < 2 * j + 1) {
-      if (t == 0) {
-        double acc = 0.0;
-        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.colnrm + bb);
-        S.dred[0] = acc;
-      } else {
-        float acc = 0.f;
-        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.colpart + (size_t)bb * kPS + t);
-        S.tot[t] = acc;
-      }
-    }
     if (t < j) {
       S.Wi[t] = __ldcg(W + i + (size_t)(k0 + t) * ldw);
       S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
     }
-    __syncthreads();
+    if (t == 64) S.misc[0] = __ldcg(p.xcol + i);
+    reduce_partials(p.colpart, p.colnrm, p.P, 2 * j + 1, S.stage, S.tot, S.dred);
     if (t == 0) {
-      float x0 = __ldcg(p.xcol + i), alpha, tau, scale;
+      float x0 = S.misc[0], alpha, tau, scale;
       householder(x0, S.dred[0], &alpha, &tau, &scale);
       S.scal[0] = alpha;
       S.scal[1] = tau;
@@ -285,16 +358,19 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     }
     for (int rr = t; rr < nrow; rr += blockDim.x) {
       const int r = r_s + rr;
-      W[r + (size_t)i * ldw] = (r == i) ? 1.f : S.own[rr] * sq;
+      const float u = (r == i) ? 1.f : S.own[rr] * sq;
+      W[r + (size_t)i * ldw] = u;
+      S.UpS[(r - ra) * kLD + j] = u;
     }
     if (i == n - 1) break;  // last column: no right reflector
     // ---------------- S3: y = A^T u on own columns, Y column j, row-i update
     {
-      // stage the unscaled column into shared memory
-      for (int r = i + 1 + t; r < m; r += blockDim.x) S.big[r] = __ldcg(p.xcol + r);
-      __syncthreads();
+      // stage the unscaled column and prefetch the original row i of own columns
       const int c_s = max(ca, i + 1);
       const int ncol = max(0, cb - c_s);
+      stage_vec(S.big, p.xcol, i + 1, m);
+      for (int cl = t; cl < ncol; cl += blockDim.x) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
+      __syncthreads();
       if (ncol > 0) {
         int segs = min(8, max(1, nw / ncol));
         const int len = m - (i + 1);
@@ -306,63 +382,58 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
           if (lane == 0) S.ypart[cl * 8 + sg] = v;
         }
         __syncthreads();
-        for (int cl = t; cl < ncol; cl += blockDim.x) {
-          const int c = c_s + cl;
+        for (int cl = wid; cl < ncol; cl += nw) {  // warp per column, lanes over l
+          const int c = c_s + cl, lc = c - ca;
           float ydot = 0.f;
           for (int sg = 0; sg < segs; sg++) ydot += S.ypart[cl * 8 + sg];
-          const float wic = __ldcg(W + i + (size_t)c * ldw);
-          float yv = wic + sq * ydot;
-          for (int l = 0; l < j; l++)
-            yv -= __ldcg(Y + c + (size_t)l * ldn) * S.p1[l] + __ldcg(VT + c + (size_t)l * ldn) * S.p2[l];
-          const float ycj = tq * yv;
-          Y[c + (size_t)j * ldn] = ycj;
-          float w = wic - ycj;
-          for (int l = 0; l < j; l++)
-            w -= __ldcg(Y + c + (size_t)l * ldn) * S.Wi[l] + __ldcg(VT + c + (size_t)l * ldn) * S.Xi[l];
-          S.owncol[cl] = w;
-          p.xrow[c] = w;
+          float c1 = 0.f, c2 = 0.f;
+          if (lane < j) {
+            const float yl = S.YS[lc * kLD + lane], vl = S.VTS[lc * kLD + lane];
+            c1 = yl * S.p1[lane] + vl * S.p2[lane];
+            c2 = yl * S.Wi[lane] + vl * S.Xi[lane];
+          }
+          c1 = warp_sum(c1);
+          c2 = warp_sum(c2);
+          if (lane == 0) {
+            const float wic = S.pre[cl];
+            const float ycj = tq * (wic + sq * ydot - c1);
+            Y[c + (size_t)j * ldn] = ycj;
+            S.YS[lc * kLD + j] = ycj;
+            const float w = wic - ycj - c2;
+            S.owncol[cl] = w;
+            p.xrow[c] = w;
+          }
         }
-      } else {
-        __syncthreads();
       }
       __syncthreads();
       // partials over own columns c > i+1: [0] ||w||^2, [1..j+1] Y^T w, [j+2..2j+1] VT^T w
       const int c1 = max(c_s, i + 2);
-      for (int q = wid; q < 2 * j + 2; q += nw) {
-        if (q == 0) {
-          double acc = 0.0;
-          for (int c = c1 + lane; c < cb; c += 32) {
-            double w = S.owncol[c - c_s];
-            acc += w * w;
-          }
-          acc = warp_sum(acc);
-          if (lane == 0) p.rownrm[b] = acc;
-        } else {
-          const float* src = (q <= j + 1) ? (Y + (size_t)(q - 1) * ldn) : (VT + (size_t)(q - j - 2) * ldn);
-          float acc = 0.f;
-          for (int c = c1 + lane; c < cb; c += 32) acc += __ldcg(src + c) * S.owncol[c - c_s];
-          acc = warp_sum(acc);
-          if (lane == 0) p.rowpart[(size_t)b * kPS + q] = acc;
+      if (wid == 0) {
+        double acc = 0.0;
+        for (int c = c1 + lane; c < cb; c += 32) {
+          double w = S.owncol[c - c_s];
+          acc += w * w;
         }
+        acc = warp_sum(acc);
+        if (lane == 0) p.rownrm[b] = acc;
+      }
+      if (t >= 32 && t < 32 + 2 * j + 1) {
+        const int q = t - 32;
+        const float* src = (q <= j) ? (S.YS + q) : (S.VTS + (q - j - 1));
+        float acc = 0.f;
+        for (int c = c1; c < cb; c++) acc += src[(c - ca) * kLD] * S.owncol[c - c_s];
+        p.rowpart[(size_t)b * kPS + 1 + q] = acc;
       }
     }
     if (!grid_sync(p.bar, p.P, p.st, 2)) return;
 
     // ---------------- S5: row reflector
-    if (t < 2 * j + 2) {
-      if (t == 0) {
-        double acc = 0.0;
-        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.rownrm + bb);
-        S.dred[0] = acc;
-      } else {
-        float acc = 0.f;
-        for (int bb = 0; bb < p.P; bb++) acc += __ldcg(p.rowpart + (size_t)bb * kPS + t);
-        S.tot[t] = acc;
-      }
-    }
-    __syncthreads();
+    if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
+    if (t >= 96 && t < 96 + j + 1) S.q1[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
+    if (t >= 160 && t < 160 + j) S.q2[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
+    reduce_partials(p.rowpart, p.rownrm, p.P, 2 * j + 2, S.stage, S.tot, S.dred);
     if (t == 0) {
-      float x0 = __ldcg(p.xrow + i + 1), beta, tau, scale;
+      float x0 = S.misc[1], beta, tau, scale;
       if (i < n - 2) {
         householder(x0, S.dred[0], &beta, &tau, &scale);
       } else {  // one element left: no reflection (bidiag.c:125-129)
@@ -381,8 +452,8 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     __syncthreads();
     const float tp = S.scal[4], sp = S.scal[5];
     prev_taup = tp;
-    if (t <= j) S.q1[t] = __ldcg(Y + i + 1 + (size_t)t * ldn) + sp * S.tot[1 + t];
-    if (t < j) S.q2[t] = __ldcg(VT + i + 1 + (size_t)t * ldn) + sp * S.tot[j + 2 + t];
+    if (t <= j) S.q1[t] += sp * S.tot[1 + t];
+    if (t < j) S.q2[t] += sp * S.tot[j + 2 + t];
     {
       const int c_s = max(ca, i + 1);
       for (int c = c_s + t; c < cb; c += blockDim.x) {
@@ -391,33 +462,34 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         else v = S.owncol[c - c_s] * sp;
         W[i + (size_t)c * ldw] = v;
         VT[c + (size_t)j * ldn] = v;
+        S.VTS[(c - ca) * kLD + j] = v;
       }
     }
-    // stage the unscaled row for x = A v
-    for (int c = i + 2 + t; c < n; c += blockDim.x) S.big[c] = __ldcg(p.xrow + c);
+    // stage the unscaled row for x = A v; prefetch the original column i+1 of own rows
+    if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
+    {
+      const int r_lo = max(ra, i + 1);
+      for (int r = r_lo + t; r < rb; r += blockDim.x) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
+    }
     __syncthreads();
     // ---------------- S6: x = A v on own rows, X column j
     {
       const int r_lo = max(ra, i + 1);
       if (rb > r_lo) {
         const int R4 = (rb - ra + 3) >> 2;
-        if (tp != 0.f) {
-          block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
-        } else {
-          __syncthreads();
-          __syncthreads();
-        }
-        for (int r = r_lo + t; r < rb; r += blockDim.x) {
-          float xv = 0.f;
-          if (tp != 0.f) {
-            float tv = __ldcg(W + r + (size_t)(i + 1) * ldw) + sp * S.own[r - ra];
-            tv -= __ldcg(W + r + (size_t)i * ldw) * S.q1[j];
-            for (int l = 0; l < j; l++)
-              tv -= __ldcg(W + r + (size_t)(k0 + l) * ldw) * S.q1[l] +
-                    __ldcg(X + r + (size_t)l * ldw) * S.q2[l];
-            xv = tp * tv;
+        if (tp != 0.f) block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
+        for (int r = r_lo + wid; r < rb; r += nw) {  // warp per row, lanes over l
+          const int lr = r - ra;
+          float part = 0.f;
+          if (lane <= j) part = S.UpS[lr * kLD + lane] * S.q1[lane];
+          if (lane < j) part += S.XS[lr * kLD + lane] * S.q2[lane];
+          part = warp_sum(part);
+          if (lane == 0) {
+            float xv = 0.f;
+            if (tp != 0.f) xv = tp * (S.pre[lr] + sp * S.own[lr] - part);
+            X[r + (size_t)j * ldw] = xv;
+            S.XS[lr * kLD + j] = xv;
           }
-          X[r + (size_t)j * ldw] = xv;
         }
       }
     }
@@ -616,6 +688,9 @@ void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWo
   w->rowpart = a.take<float>((size_t)P * kPS + 2 * P);
   w->bar = a.take<GridBarrier>(4);
   w->gemm_scratch = a.take<char>(gemm_scratch_bytes(kind, m, n, 2 * kPanel));
+  const bool tc = (kind != GEMM_SIMT);
+  w->Apk = a.take<float>(tc ? (size_t)m * 2 * kPanel + 64 : 16);
+  w->Bpk = a.take<float>(tc ? (size_t)n * 2 * kPanel + 64 : 16);
 }
 
 static int launch_coop(const void* fn, int P, int threads, size_t smem, void* args,
@@ -649,7 +724,7 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
     pp.bar = w.bar;
     pp.st = ctx->d_status;
     DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
-    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads);
+    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads, P);
     ktimer_begin(ctx, KC_BIDIAG);
     DDC_TRY(launch_coop((const void*)bidiag_panel_kernel, P, kBidiagThreads, smem, &pp, ctx->stream));
     ktimer_end(ctx);
@@ -662,8 +737,16 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
       Mat A2{w.X + kn, 1, ldw};
       Mat B2{w.VT + kn, w.ldn, 1};
       ktimer_begin(ctx, KC_TRAIL_GEMM);
-      DDC_TRY(gemm(ctx, kind, M, N, nb, A1, B1, nb, A2, B2, -1.f, 1.f, W + kn + (size_t)kn * ldw,
-                   ldw, scratch));
+      if (kind == GEMM_SIMT) {
+        DDC_TRY(gemm(ctx, kind, M, N, nb, A1, B1, nb, A2, B2, -1.f, 1.f, W + kn + (size_t)kn * ldw,
+                     ldw, scratch));
+      } else {
+        // tensor cores read K-major operands: [U_p X] and [Y VT] as rows of 2*nb
+        DDC_TRY(pack_kmajor(ctx, M, nb, W + kn + (size_t)k0 * ldw, ldw, nb, w.X + kn, ldw, w.Apk, 2 * kPanel));
+        DDC_TRY(pack_kmajor(ctx, N, nb, w.Y + kn, w.ldn, nb, w.VT + kn, w.ldn, w.Bpk, 2 * kPanel));
+        DDC_TRY(gemm_tc_kmajor(ctx, kind, M, N, 2 * nb, w.Apk, 2 * kPanel, 0, w.Bpk, 2 * kPanel, 0,
+                               W + kn + (size_t)kn * ldw, ldw, -1.f, 1.f, scratch));
+      }
       ktimer_end(ctx);
     }
   }

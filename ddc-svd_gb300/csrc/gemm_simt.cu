@@ -124,6 +124,45 @@ __global__ void splitk_reduce_kernel(int M, int N, int ksplit, const float* part
 
 int gemm_tc(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2,
             Mat A2, Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch);
+
+void splitk_reduce(ddcsvd_context* ctx, int M, int N, int ksplit, const float* partial, float alpha,
+                   float beta, float* C, int ldc) {
+  const int blocks = std::min(4 * ctx->num_sms, ceil_div(M * N, 256));
+  splitk_reduce_kernel<<<blocks, 256, 0, ctx->stream>>>(M, N, ksplit, partial, alpha, beta, C, ldc);
+  count_launch();
+}
+
+// out[r * ldo + k] = k < K1 ? P1[r + k*ld1] : P2[r + (k-K1)*ld2]  (column blocks -> K-major rows)
+__global__ void pack_kmajor_kernel(int rows, int K1, const float* __restrict__ P1, int ld1, int K2,
+                                   const float* __restrict__ P2, int ld2, float* out, int ldo) {
+  __shared__ float tile[64][33];
+  const int r0 = blockIdx.x * 32;
+  const int K = K1 + K2;
+  for (int kb = 0; kb < K; kb += 64) {
+    const int kc = min(64, K - kb);
+    for (int idx = threadIdx.x; idx < kc * 32; idx += blockDim.x) {
+      const int kk = idx / 32, rr = idx % 32, r = r0 + rr, k = kb + kk;
+      float v = 0.f;
+      if (r < rows) v = (k < K1) ? P1[r + (size_t)k * ld1] : P2[r + (size_t)(k - K1) * ld2];
+      tile[kk][rr] = v;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kc * 32; idx += blockDim.x) {
+      const int rr = idx / kc, kk = idx % kc, r = r0 + rr;
+      if (r < rows) out[(size_t)r * ldo + kb + kk] = tile[kk][rr];
+    }
+    __syncthreads();
+  }
+}
+
+int pack_kmajor(ddcsvd_context* ctx, int rows, int K1, const float* P1, int ld1, int K2, const float* P2, int ld2,
+                float* out, int ldo) {
+  if (rows <= 0) return DDCSVD_OK;
+  pack_kmajor_kernel<<<ceil_div(rows, 32), 256, 0, ctx->stream>>>(rows, K1, P1, ld1, K2, P2, ld2, out, ldo);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
 size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K);
 
 size_t gemm_scratch_bytes(GemmKind kind, int M, int N, int K) {

@@ -1,24 +1,450 @@
-// gemm_tc.cu -- tcgen05 tensor-core GEMM back ends (split TF32 / split BF16).
+// gemm_tc.cu -- tcgen05 tensor-core GEMM in split TF32 (3xTF32) for sm_103a.
+//
+//   C (M x N, col-major) = beta * C + alpha * A B,   A: M x K, B: K x N,
+//   both operands K-major in global memory (row r of A at A + r*lda, column
+//   n of B at B + n*ldb, K contiguous).
+//
+// FP32 accuracy from TF32 tensor cores: each FP32 operand x is split into
+// hi = tf32(x) and lo = tf32(x - hi) (both round-to-nearest), and the product
+// is accumulated as hi*hi + hi*lo + lo*hi in FP32 in TMEM (the lo*lo term,
+// ~2^-22 relative, is dropped).
+//
+// One CTA computes a 128 x BN tile (BN = 128 or 64), 6 warps:
+//   warp 0      TMA producer: raw FP32 K-slabs (32 wide, 128-byte swizzle)
+//               of A and B into a 3-stage shared-memory ring;
+//   warps 2-5   split each landed slab in place into hi (overwriting the raw
+//               copy) and lo (second buffer), then release it to the MMA;
+//   warp 1      TMEM allocation and the single MMA-issuing thread:
+//               tcgen05.mma.kind::tf32 over 4 K-steps x 3 products per slab,
+//               tcgen05.commit frees the stage;
+//   warps 2-5   epilogue: tcgen05.ld of the accumulator (lane = row), scaled
+//               update of C (coalesced along columns of col-major C).
+// Split-K over blockIdx.z writes FP32 partials that a second kernel reduces
+// in a fixed order (deterministic).
+//
+// Every mbarrier wait is bounded by wall-clock time; on expiry the CTA
+// records DDCSVD_ERR_TIMEOUT, skips its stores, waits (bounded) for its own
+// TMA copies in flight and frees its TMEM before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "internal.hpp"
 
 namespace ddcsvd {
 
+void splitk_reduce(ddcsvd_context* ctx, int M, int N, int ksplit, const float* partial, float alpha,
+                   float beta, float* C, int ldc);
+
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BK = 32;  // FP32 elements per slab row: 128 bytes = one swizzle span
+constexpr int STAGES = 3;
+constexpr int THREADS = 192;
+constexpr unsigned long long kTcWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity.  Returns false when the CTA
+// aborts (another role gave up, or this wait ran out of time).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          DevStatus* st, int where) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (global_ns() - t0 > kTcWaitNs) {
+      *abort_flag = 1;
+      set_error(st, DDCSVD_ERR_TIMEOUT, where);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
+// 8-row core groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)(16 >> 4) << 16;           // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset
+  d |= (uint64_t)1 << 46;                   // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D = FP32, A = B = TF32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// In-place split of a raw FP32 tile: raw -> hi, lo buffer <- tf32(raw - hi).
+__device__ __forceinline__ void split_tile(float4* raw, float4* lo, int n16, int t, int nt) {
+  for (int q = t; q < n16; q += nt) {
+    float4 v = raw[q];
+    float4 h, l;
+    h.x = __uint_as_float(to_tf32(v.x));
+    h.y = __uint_as_float(to_tf32(v.y));
+    h.z = __uint_as_float(to_tf32(v.z));
+    h.w = __uint_as_float(to_tf32(v.w));
+    l.x = __uint_as_float(to_tf32(v.x - h.x));
+    l.y = __uint_as_float(to_tf32(v.y - h.y));
+    l.z = __uint_as_float(to_tf32(v.z - h.z));
+    l.w = __uint_as_float(to_tf32(v.w - h.w));
+    raw[q] = h;
+    lo[q] = l;
+  }
+}
+
+struct TcParams {
+  int M, N;
+  int a_koff, b_koff;  // K coordinate of the first slab in the A / B maps
+  int nslab;           // slabs of 32 along K in total
+  int per_split;       // slabs per blockIdx.z
+  float* C;
+  int ldc;
+  float alpha, beta;
+  float* partial;  // split-K partials (M x N per split, ld M) or null
+  DevStatus* st;
+};
+
+template <int BN>
+struct Layout {
+  static constexpr int A_BYTES = BM * BK * 4;
+  static constexpr int B_BYTES = BN * BK * 4;
+  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int TMEM_COLS = BN < 32 ? 32 : BN;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(THREADS, 1)
+    tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                          TcParams p) {
+  using L = Layout<BN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(round_up(reinterpret_cast<uintptr_t>(smem_raw), 1024));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::STAGE);
+  uint64_t* full = bars;
+  uint64_t* conv = bars + STAGES;
+  uint64_t* empty = bars + 2 * STAGES;
+  uint64_t* accum = bars + 3 * STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * STAGES + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&conv[s], 128);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(L::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int s_begin = blockIdx.z * p.per_split;
+  const int s_end = min(p.nslab, s_begin + p.per_split);
+  const int nsl = max(0, s_end - s_begin);
+  auto a_hi = [&](int s) { return smem + s * L::STAGE; };
+  auto a_lo = [&](int s) { return smem + s * L::STAGE + L::A_BYTES; };
+  auto b_hi = [&](int s) { return smem + s * L::STAGE + 2 * L::A_BYTES; };
+  auto b_lo = [&](int s) { return smem + s * L::STAGE + 2 * L::A_BYTES + L::B_BYTES; };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int i = 0; i < nsl; i++) {
+        const int s = i % STAGES;
+        if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1, abort_flag, p.st, 901)) break;
+        mbar_arrive_expect_tx(&full[s], L::A_BYTES + L::B_BYTES);
+        const int sl = s_begin + i;
+        tma_load_2d(a_hi(s), &tmA, p.a_koff + sl * BK, m0, &full[s]);
+        tma_load_2d(b_hi(s), &tmB, p.b_koff + sl * BK, n0, &full[s]);
+        issued = i + 1;
+      }
+      // make sure no copy of ours is still landing before the CTA may exit
+      for (int i = max(0, issued - STAGES); i < issued; i++) {
+        const int s = i % STAGES;
+        const unsigned long long t0 = global_ns();
+        while (!mbar_try_wait(&full[s], (i / STAGES) & 1) && global_ns() - t0 < kTcWaitNs) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      for (int i = 0; i < nsl; i++) {
+        const int s = i % STAGES;
+        if (!mbar_wait(&conv[s], (i / STAGES) & 1, abort_flag, p.st, 902)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t ah = smem_u32(a_hi(s)), al = smem_u32(a_lo(s));
+        const uint32_t bh = smem_u32(b_hi(s)), bl = smem_u32(b_lo(s));
+#pragma unroll
+        for (int kk = 0; kk < BK / 8; kk++) {
+          const uint32_t off = kk * 32;  // 8 TF32 elements = 32 bytes along K
+          const uint64_t dah = smem_desc_sw128(ah + off), dal = smem_desc_sw128(al + off);
+          const uint64_t dbh = smem_desc_sw128(bh + off), dbl = smem_desc_sw128(bl + off);
+          mma_tf32(tmem, dal, dbh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+          mma_tf32(tmem, dah, dbl, idesc, 1u);
+          mma_tf32(tmem, dah, dbh, idesc, 1u);
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(accum);
+    }
+  } else {
+    const int ct = threadIdx.x - 64;
+    for (int i = 0; i < nsl; i++) {
+      const int s = i % STAGES;
+      if (!mbar_wait(&full[s], (i / STAGES) & 1, abort_flag, p.st, 903)) break;
+      split_tile(reinterpret_cast<float4*>(a_hi(s)), reinterpret_cast<float4*>(a_lo(s)), L::A_BYTES / 16, ct, 128);
+      split_tile(reinterpret_cast<float4*>(b_hi(s)), reinterpret_cast<float4*>(b_lo(s)), L::B_BYTES / 16, ct, 128);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&conv[s]);
+    }
+    // ---------------- epilogue: TMEM -> C
+    const bool ok = mbar_wait(accum, 0, abort_flag, p.st, 904) && !*abort_flag && nsl > 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = m0 + q * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+      if (!ok || row >= p.M) continue;
+#pragma unroll
+      for (int jj = 0; jj < 16; jj++) {
+        const int col = n0 + c0 + jj;
+        if (col >= p.N) break;
+        const float v = __uint_as_float(r[jj]);
+        if (p.partial) {
+          p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = v;
+        } else {
+          float* cp = p.C + row + (size_t)col * p.ldc;
+          *cp = (p.beta == 0.f ? 0.f : p.beta * *cp) + p.alpha * v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- host side
+using EncodeFn = PFN_cuTensorMapEncodeTiled_v12000;
+
+static EncodeFn encode_fn() {
+  static EncodeFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeFn>(ptr);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 2-D map over a K-major operand: `rows` rows of `kext` FP32 elements,
+// row stride `ld` elements; box = 32 (K) x box_rows, 128-byte swizzle.
+static int make_map(CUtensorMap* map, const float* base, long long kext, long long rows, long long ld,
+                    int box_rows) {
+  EncodeFn enc = encode_fn();
+  if (!enc) {
+    set_last_error("cuTensorMapEncodeTiled unavailable");
+    return DDCSVD_ERR_UNSUPPORTED;
+  }
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((ld * 4) & 15)) {
+    set_last_error("tensor-core operand not 16-byte aligned");
+    return DDCSVD_ERR_ARG;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)kext, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_last_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return DDCSVD_ERR_CUDA;
+  }
+  return DDCSVD_OK;
+}
+
+template <int BN>
+static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long long lda, int a_koff,
+                  const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha, float beta,
+                  Arena* scratch) {
+  using L = Layout<BN>;
+  CUtensorMap ma, mb;
+  DDC_TRY(make_map(&ma, A, (long long)a_koff + K, M, lda, BM));
+  DDC_TRY(make_map(&mb, B, (long long)b_koff + K, N, ldb, BN));
+  static bool attr_set = false;
+  if (!attr_set) {
+    DDC_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      L::SMEM));
+    attr_set = true;
+  }
+  TcParams p;
+  p.M = M;
+  p.N = N;
+  p.a_koff = a_koff;
+  p.b_koff = b_koff;
+  p.nslab = ceil_div(K, BK);
+  p.C = C;
+  p.ldc = ldc;
+  p.alpha = alpha;
+  p.beta = beta;
+  p.st = ctx->d_status;
+  const int tiles = ceil_div(M, BM) * ceil_div(N, BN);
+  int ksplit = 1;
+  if (scratch && !scratch->plan && tiles < ctx->num_sms && p.nslab >= 8) {
+    ksplit = std::min(16, std::max(1, (2 * ctx->num_sms) / tiles));
+    ksplit = std::min(ksplit, p.nslab / 4);
+    while (ksplit > 1 && (size_t)ksplit * M * N * sizeof(float) > scratch->cap) ksplit--;
+  }
+  p.per_split = ceil_div(p.nslab, ksplit);
+  ksplit = ceil_div(p.nslab, p.per_split);
+  p.partial = (ksplit > 1) ? reinterpret_cast<float*>(scratch->base) : nullptr;
+  dim3 grid(ceil_div(M, BM), ceil_div(N, BN), ksplit);
+  tc_gemm_tf32x3_kernel<BN><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, p);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  if (ksplit > 1) splitk_reduce(ctx, M, N, ksplit, p.partial, alpha, beta, C, ldc);
+  return DDCSVD_OK;
+}
+
+}  // namespace tc
+
 bool tc_available(ddcsvd_context* ctx) {
   (void)ctx;
-  return false;
+  int dev = 0, major = 0, minor = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  return major == 10 && minor == 3 && tc::encode_fn() != nullptr;
 }
 
 size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K) {
   (void)kind;
-  return (size_t)2 * ((size_t)M * K + (size_t)K * N) * sizeof(float) + 4096;
+  (void)K;
+  return (size_t)16 * M * N * sizeof(float) + 4096;
 }
 
+int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                   int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
+                   float beta, Arena* scratch) {
+  if (kind != GEMM_TF32X3) {
+    set_last_error("split-BF16 tensor-core GEMM is not implemented");
+    return DDCSVD_ERR_UNSUPPORTED;
+  }
+  if (M <= 0 || N <= 0) return DDCSVD_OK;
+  if ((a_koff & 3) || (b_koff & 3)) return DDCSVD_ERR_ARG;
+  if (N <= 64) return tc::launch<64>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+  return tc::launch<128>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+}
+
+// Strided-operand entry used by gemm(): only the K-major layouts map onto the
+// tensor-core kernel directly; callers with other layouts pack first.
 int gemm_tc(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2, Mat A2,
             Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch) {
-  (void)ctx; (void)kind; (void)M; (void)N; (void)K1; (void)A1; (void)B1; (void)K2; (void)A2; (void)B2;
-  (void)alpha; (void)beta; (void)C; (void)ldc; (void)scratch;
-  set_last_error("tensor-core GEMM not built");
-  return DDCSVD_ERR_UNSUPPORTED;
+  if (K2 > 0 && A2.p) {
+    set_last_error("two-term tensor-core GEMM must be packed by the caller");
+    return DDCSVD_ERR_ARG;
+  }
+  if (A1.cs != 1 || B1.rs != 1) {
+    set_last_error("tensor-core GEMM needs K-major operands");
+    return DDCSVD_ERR_ARG;
+  }
+  return gemm_tc_kmajor(ctx, kind, M, N, K1, A1.p, A1.rs, 0, B1.p, B1.cs, 0, C, ldc, alpha, beta, scratch);
 }
 
 }  // namespace ddcsvd

@@ -79,6 +79,15 @@ int gemm(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B
          Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch);
 size_t gemm_scratch_bytes(GemmKind kind, int M, int N, int K);
 bool tc_available(ddcsvd_context* ctx);
+// Tensor-core GEMM on K-major operands: A row r at A + r*lda (K from a_koff),
+// B column n at B + n*ldb (K from b_koff); koffs multiples of 4, ld*4 and the
+// base pointers 16-byte aligned.
+int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                   int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
+                   float beta, Arena* scratch);
+// rows x (K1 + K2) K-major copy of two column-major blocks.
+int pack_kmajor(ddcsvd_context* ctx, int rows, int K1, const float* P1, int ld1, int K2, const float* P2, int ld2,
+                float* out, int ldo);
 
 // ---------------------------------------------------------------- stage 1
 struct BidiagWork {
@@ -89,6 +98,7 @@ struct BidiagWork {
   GridBarrier* bar;
   int P;  // CTAs of the cooperative launch
   char* gemm_scratch;
+  float *Apk, *Bpk;  // K-major packed trailing-update operands (tensor-core modes)
 };
 constexpr int kPanel = 32;       // bidiagonalisation panel width
 constexpr int kBidiagThreads = 512;
