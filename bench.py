@@ -191,6 +191,81 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
                        f"stages on its leading 1024^2 block ({max(tfull - tbb, 0):.2f} s, scaled by (4096/1024)^3)")}
 
 
+def batched_workload(seed=3, count=2048):
+    """2048 FP32 problems, m ~ U{16..256}, n ~ U{8..m}, entries U[-1, 1] (seeded)."""
+    rng = np.random.default_rng(seed)
+    mats = []
+    for _ in range(count):
+        m = int(rng.integers(16, 257))
+        n = int(rng.integers(8, m + 1))
+        mats.append(rng.uniform(-1, 1, (m, n)).astype(np.float32))
+    return mats
+
+
+def bench_batched(torch, lib, h, steps, flush):
+    mats = batched_workload()
+    plan = lib.BatchPlan([a.shape for a in mats], handle=h)
+    plan.load([torch.from_numpy(a).cuda() for a in mats])
+    plan.run()
+    torch.cuda.synchronize()
+    # accuracy (worst over the batch, FP64 on the GPU)
+    worst = 0.0
+    for b in range(0, len(mats), 16):
+        s, U, V = (x.double() for x in plan.result(b))
+        A = torch.from_numpy(mats[b]).cuda().double()
+        worst = max(worst, float(torch.linalg.norm(A - (U * s) @ V.T) / torch.linalg.norm(A)))
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.run()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ms = float(np.mean(ts))
+    # the single-matrix path looped over the first 128 problems (same inputs)
+    sub = [torch.from_numpy(a).cuda() for a in mats[:128]]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a in sub:
+        lib.svd_device(a, mode="plain", handle=h)
+    torch.cuda.synchronize()
+    loop_ms = 1e3 * (time.perf_counter() - t0) / len(sub)
+    mn = sum(a.shape[0] * a.shape[1] for a in mats)
+    comp = sum(4 * (2 * a.shape[0] * a.shape[1] + a.shape[1] + a.shape[1] ** 2) for a in mats)
+    flops = sum(8.0 * a.shape[0] * a.shape[1] ** 2 - 4.0 / 3.0 * a.shape[1] ** 3 for a in mats)
+    hbm, _ = measured_peaks()
+    return {"svds_per_s": round(len(mats) / (ms * 1e-3), 1), "ms": round(ms, 3), "count": len(mats),
+            "loop_single_svds_per_s": round(1e3 / loop_ms, 1), "compulsory_bytes": comp, "elements": mn,
+            "hbm_frac": round(comp / (ms * 1e-3) / 1e9 / hbm, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
+            "worst_resid": float(f"{worst:.3e}")}
+
+
+def bench_adjoint(torch, lib, h, steps):
+    out = {}
+    rng = np.random.default_rng(4)
+    B, m, n = 256, 128, 64
+    for dt, name in ((torch.float64, "f64"), (torch.float32, "f32")):
+        U = torch.linalg.qr(torch.randn(B, m, n, dtype=dt, device="cuda"))[0]
+        V = torch.linalg.qr(torch.randn(B, n, n, dtype=dt, device="cuda"))[0]
+        S = (1.0 + torch.arange(n, dtype=dt, device="cuda") / 64.0).expand(B, n).contiguous()
+        gU, gV, gS = torch.randn_like(U), torch.randn_like(V), torch.randn_like(S)
+        lib.svd_backward_device(U, S, V, gU, gS, gV, handle=h)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            lib.svd_backward_device(U, S, V, gU, gS, gV, handle=h)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out[f"bwd_ms_{name}"] = round(float(np.mean(ts)), 4)
+    out["shape"] = "256 x (128x64)"
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path (FP64 port) timed on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -255,7 +330,7 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     # accuracy + stage / kernel times of each mode (one extra untimed run each)
-    modes = ["tf32x3", "blocked", "plain"] if not args.quick else ["tf32x3"]
+    modes = ["tf32x6", "tf32x3", "blocked", "plain"] if not args.quick else ["tf32x6"]
     avail = []
     info = {}
     for mode in modes:
@@ -332,6 +407,9 @@ def main():
         e2e.append(1e3 * (time.perf_counter() - t0))
     e2e_ms = float(np.mean(e2e))
 
+    batched = bench_batched(torch, lib, h, max(3, args.steps), flush) if not args.quick else None
+    adjoint = bench_adjoint(torch, lib, h, max(3, args.steps)) if not args.quick else None
+
     # roofline of the dominant kernel class (bidiagonalisation GEMV kernels)
     hbm, peak_kind = measured_peaks()
     kinfo = info[head]
@@ -363,6 +441,7 @@ def main():
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": M * N * 4,
                 "d2h_bytes_per_step": (N + M * N + N * N) * 4, "api": "ddcsvd_svd_f32 (pinned host buffers)"},
         "roofline": roof, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cb,
+        "batched": batched, "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

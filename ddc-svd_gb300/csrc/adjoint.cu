@@ -1,15 +1,158 @@
-// adjoint.cu -- reverse-mode derivative of the thin SVD.
+// adjoint.cu -- reverse-mode derivative of the thin SVD A = U diag(s) V^T
+// (m >= n, k = n) for a batch of equally sized problems, FP64 or FP32.
+//
+//   J = U^T gU,  K = V^T gV                                (k x k)
+//   F_ij = 1 / (s_j^2 - s_i^2) for i != j, 0 on the diagonal
+//   M = diag(gs) + (F o (J - J^T)) S + S (F o (K - K^T)) - J S^-1
+//   gA = (U M + gU S^-1) V^T
+// which equals U [diag(gs) + (F o (J - J^T)) S + S (F o (K - K^T))] V^T
+// + (I - U U^T) gU S^-1 V^T.  (The reference has no derivative; this is the
+// standard SVD adjoint.)  Any of gU, gs, gV may be null (zero).
+//
+// Four kernels per call: a batched tiled GEMM for J and K, an elementwise
+// kernel for M, the batched GEMM for U M (+ gU S^-1 as its C input) and for
+// (U M + gU S^-1) V^T.
 #include "internal.hpp"
 
-extern "C" int ddcsvd_svd_backward_f64_device(ddcsvd_handle_t, int, int, int, const double*, const double*,
-                                              const double*, const double*, const double*, const double*,
-                                              double*) {
-  ddcsvd::set_last_error("adjoint not built yet");
-  return DDCSVD_ERR_UNSUPPORTED;
+namespace ddcsvd {
+
+// C[b] (M x N, col-major, ldc) = beta * C[b] + alpha * A[b] B[b], element
+// (r, k) of A[b] at A + b*as + r*ars + k*acs, element (k, c) of B[b] at
+// B + b*bs + k*brs + c*bcs.  32 x 32 tiles, 16 x 16 threads, 2 x 2 outputs each.
+template <typename T>
+__global__ void bgemm_kernel(int M, int N, int K, const T* __restrict__ A, long long ars, long long acs,
+                             long long as, const T* __restrict__ B, long long brs, long long bcs, long long bs,
+                             T* C, int ldc, long long cs, T alpha, T beta) {
+  __shared__ T At[32][33];
+  __shared__ T Bt[32][33];
+  const int b = blockIdx.z;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const T* Ab = A + b * as;
+  const T* Bb = B + b * bs;
+  T acc[2][2] = {{0, 0}, {0, 0}};
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    for (int idx = ty * 16 + tx; idx < 32 * 32; idx += 256) {
+      const int i = idx % 32, kk = idx / 32;
+      const int r = r0 + i, k = k0 + kk;
+      At[kk][i] = (r < M && k < K) ? Ab[r * ars + k * acs] : T(0);
+      const int c = c0 + i;
+      Bt[kk][i] = (c < N && k < K) ? Bb[k * brs + c * bcs] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; kk++) {
+      const T a0 = At[kk][ty], a1 = At[kk][ty + 16];
+      const T b0 = Bt[kk][tx], b1 = Bt[kk][tx + 16];
+      acc[0][0] += a0 * b0;
+      acc[0][1] += a0 * b1;
+      acc[1][0] += a1 * b0;
+      acc[1][1] += a1 * b1;
+    }
+    __syncthreads();
+  }
+  T* Cb = C + b * cs;
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+      if (r < M && c < N) {
+        T* p = Cb + r + (size_t)c * ldc;
+        *p = (beta == T(0) ? T(0) : beta * *p) + alpha * acc[i][j];
+      }
+    }
 }
-extern "C" int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t, int, int, int, const float*, const float*,
-                                              const float*, const float*, const float*, const float*,
-                                              float*) {
-  ddcsvd::set_last_error("adjoint not built yet");
-  return DDCSVD_ERR_UNSUPPORTED;
+
+// M (k x k per problem) from J, K, s, gs; P := gU S^-1 (m x k) in the same pass.
+template <typename T>
+__global__ void adjoint_core_kernel(int k, int m, const T* __restrict__ J, const T* __restrict__ Kv,
+                                    const T* __restrict__ s, const T* __restrict__ gs, const T* __restrict__ gU,
+                                    T* Mo, T* P) {
+  const int b = blockIdx.y;
+  const T* Jb = J ? J + (size_t)b * k * k : nullptr;
+  const T* Kb = Kv ? Kv + (size_t)b * k * k : nullptr;
+  const T* sb = s + (size_t)b * k;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < k * k; idx += gridDim.x * blockDim.x) {
+    const int i = idx % k, j = idx / k;
+    const T si = sb[i], sj = sb[j];
+    T v = T(0);
+    if (i == j) {
+      if (gs) v += gs[(size_t)b * k + i];
+    } else {
+      const T f = T(1) / ((sj - si) * (sj + si));
+      if (Jb) v += f * (Jb[i + (size_t)j * k] - Jb[j + (size_t)i * k]) * sj;
+      if (Kb) v += si * f * (Kb[i + (size_t)j * k] - Kb[j + (size_t)i * k]);
+    }
+    if (Jb) v -= Jb[i + (size_t)j * k] / sj;
+    Mo[(size_t)b * k * k + idx] = v;
+  }
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * k; idx += gridDim.x * blockDim.x) {
+    const int j = idx / m;
+    P[(size_t)b * m * k + idx] = gU ? gU[(size_t)b * m * k + idx] / sb[j] : T(0);
+  }
+}
+
+template <typename T>
+static int bgemm(ddcsvd_context* ctx, int batch, int M, int N, int K, const T* A, long long ars, long long acs,
+                 long long as, const T* B, long long brs, long long bcs, long long bs, T* C, int ldc, long long cs,
+                 T alpha, T beta) {
+  dim3 grid(ceil_div(M, 32), ceil_div(N, 32), batch);
+  bgemm_kernel<T><<<grid, dim3(16, 16), 0, ctx->stream>>>(M, N, K, A, ars, acs, as, B, brs, bcs, bs, C, ldc, cs,
+                                                          alpha, beta);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+template <typename T>
+static int svd_backward(ddcsvd_context* h, int batch, int m, int n, const T* U, const T* S, const T* V, const T* gU,
+                        const T* gS, const T* gV, T* gA) {
+  if (!h || batch <= 0 || m <= 0 || n <= 0 || m < n || !U || !S || !V || !gA) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  const int k = n;
+  const size_t kk = (size_t)k * k * batch, mk = (size_t)m * k * batch;
+  Arena plan;
+  plan.take<T>(kk);
+  plan.take<T>(kk);
+  plan.take<T>(kk);
+  plan.take<T>(mk);
+  DDC_TRY(ensure_workspace(h, plan.off + 4096));
+  Arena a;
+  a.plan = false;
+  a.base = (char*)h->ws;
+  T* J = a.take<T>(kk);
+  T* Kv = a.take<T>(kk);
+  T* Mm = a.take<T>(kk);
+  T* P = a.take<T>(mk);
+  DDC_TRY(reset_status(h));
+  const long long sU = (long long)m * k, sV = (long long)n * k, sK = (long long)k * k;
+  // J = U^T gU, K = V^T gV
+  if (gU) DDC_TRY(bgemm<T>(h, batch, k, k, m, U, m, 1, sU, gU, 1, m, sU, J, k, sK, T(1), T(0)));
+  if (gV) DDC_TRY(bgemm<T>(h, batch, k, k, n, V, n, 1, sV, gV, 1, n, sV, Kv, k, sK, T(1), T(0)));
+  dim3 g2(std::max(1, std::min(64, ceil_div(std::max(k * k, m * k), 256))), batch);
+  adjoint_core_kernel<T><<<g2, 256, 0, h->stream>>>(k, m, gU ? J : nullptr, gV ? Kv : nullptr, S, gS, gU, Mm, P);
+  count_launch();
+  // P += U M
+  DDC_TRY(bgemm<T>(h, batch, m, k, k, U, 1, m, sU, Mm, 1, k, sK, P, m, sU, T(1), T(1)));
+  // gA = P V^T
+  DDC_TRY(bgemm<T>(h, batch, m, n, k, P, 1, m, sU, V, n, 1, sV, gA, m, (long long)m * n, T(1), T(0)));
+  return check_status(h, "svd_backward");
+}
+
+}  // namespace ddcsvd
+
+using namespace ddcsvd;
+
+extern "C" int ddcsvd_svd_backward_f64_device(ddcsvd_handle_t h, int batch, int m, int n, const double* dU,
+                                              const double* dS, const double* dV, const double* gU,
+                                              const double* gS, const double* gV, double* gA) {
+  return svd_backward<double>(h, batch, m, n, dU, dS, dV, gU, gS, gV, gA);
+}
+
+extern "C" int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t h, int batch, int m, int n, const float* dU,
+                                              const float* dS, const float* dV, const float* gU, const float* gS,
+                                              const float* gV, float* gA) {
+  return svd_backward<float>(h, batch, m, n, dU, dS, dV, gU, gS, gV, gA);
 }

@@ -14,6 +14,7 @@
 #include <string>
 
 #include "internal.hpp"
+#include "prep.hpp"
 
 namespace ddcsvd {
 
@@ -118,6 +119,7 @@ static GemmKind kind_of(int mode) {
   switch (mode) {
     case DDCSVD_MODE_BLOCKED_TF32X3: return GEMM_TF32X3;
     case DDCSVD_MODE_BLOCKED_BF16X3: return GEMM_BF16X3;
+    case DDCSVD_MODE_BLOCKED_TF32X6: return GEMM_TF32X6;
     default: return GEMM_SIMT;
   }
 }
@@ -130,8 +132,9 @@ static int resolve_mode(int mode) {
     if (!strcmp(e, "blocked")) return DDCSVD_MODE_BLOCKED_FP32;
     if (!strcmp(e, "tf32x3")) return DDCSVD_MODE_BLOCKED_TF32X3;
     if (!strcmp(e, "bf16x3")) return DDCSVD_MODE_BLOCKED_BF16X3;
+    if (!strcmp(e, "tf32x6")) return DDCSVD_MODE_BLOCKED_TF32X6;
   }
-  return DDCSVD_MODE_BLOCKED_TF32X3;
+  return DDCSVD_MODE_BLOCKED_TF32X6;
 }
 
 // ---------------------------------------------------------------- small kernels
@@ -166,49 +169,9 @@ __global__ void finite_check_kernel(int m, int n, const float* A, int lda, DevSt
 struct Plan {
   float *W, *d, *e, *tauq, *taup;
   double *sig_slot, *sig;
-  char* blob;  // device copy of the bidiagonal preparation (see BdBlob)
+  char* blob;  // device copy of the bidiagonal preparation (prep.hpp)
   BidiagWork bw;
 };
-
-// Prepared bidiagonal: split FP64 copy, block bounds per row and the D&C
-// node table, laid out identically in pinned host memory and on the device.
-struct BdBlob {
-  size_t off_b1, off_b2, off_lo, off_hi, off_ints, bytes;
-  static BdBlob layout(int N) {
-    BdBlob L;
-    size_t o = 0;
-    auto take = [&](size_t b) { o = (size_t)round_up((long long)o, 256); size_t r = o; o += b; return r; };
-    L.off_b1 = take(sizeof(double) * N);
-    L.off_b2 = take(sizeof(double) * N);
-    L.off_lo = take(sizeof(int) * N);
-    L.off_hi = take(sizeof(int) * N);
-    L.off_ints = take(sizeof(int) * dc_max_ints(N));
-    L.bytes = (size_t)round_up((long long)o, 256);
-    return L;
-  }
-};
-
-// Fills the pinned blob from host copies of the bidiagonal (a, b: N each; b is
-// split in place), builds the D&C forest and uploads the blob.  `eps` is the
-// precision the bidiagonal was computed in.
-static int prepare_bidiagonal(ddcsvd_context* ctx, int N, char* hblob, char* dblob, double eps, DcHost* H) {
-  const BdBlob L = BdBlob::layout(N);
-  double* a = (double*)(hblob + L.off_b1);
-  double* b = (double*)(hblob + L.off_b2);
-  int* lo = (int*)(hblob + L.off_lo);
-  int* hi = (int*)(hblob + L.off_hi);
-  std::vector<int> starts;
-  split_bidiagonal(N, a, b, eps, starts, lo, hi);
-  dc_build_host(N, starts, *H);
-  if (H->ints.size() > dc_max_ints(N)) {
-    set_last_error("D&C node table larger than its bound");
-    return DDCSVD_ERR_ARG;
-  }
-  memcpy(hblob + L.off_ints, H->ints.data(), sizeof(int) * H->ints.size());
-  const size_t used = L.off_ints + sizeof(int) * H->ints.size();
-  DDC_CUDA_TRY(cudaMemcpyAsync(dblob, hblob, used, cudaMemcpyHostToDevice, ctx->stream));
-  return DDCSVD_OK;
-}
 
 static int stage_event(ddcsvd_context* ctx, int k) {
   if (ctx->timing) DDC_CUDA_TRY(cudaEventRecord(ctx->ev[k], ctx->stream));
@@ -232,7 +195,7 @@ __global__ void copy2d_kernel(int rows, int cols, const float* __restrict__ src,
 // aligned staging buffers.
 static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                     int ldu, float* dV, int ldv, int mode, bool check_finite) {
-  const bool tcmode = (mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3);
+  const bool tcmode = (mode >= DDCSVD_MODE_BLOCKED_TF32X3);
   auto ok = [](const float* p, int ld) { return ((reinterpret_cast<uintptr_t>(p) & 15) == 0) && (ld % 4 == 0); };
   if (!tcmode || (ok(dU, ldu) && ok(dV, ldv)))
     return svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
@@ -256,7 +219,7 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
                          int ldu, float* dV, int ldv, int mode, bool check_finite) {
   const bool plain = (mode == DDCSVD_MODE_PLAIN_FP32);
   const GemmKind kind = kind_of(mode);
-  const int P = bidiag_coop_ctas(ctx, m, n);
+  const int nctas = bidiag_coop_ctas(ctx, m, n);
   const int ldw = (int)round_up(m, 32);
   const size_t gsc = gemm_scratch_bytes(kind, m, n, 2 * kPanel);
   auto region_a = [&](Arena& a, Plan& pl) {
@@ -267,7 +230,7 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     pl.taup = a.take<float>(n + 4);
     pl.sig_slot = a.take<double>(n + 4);
     pl.sig = a.take<double>(n + 4);
-    pl.blob = a.take<char>(BdBlob::layout(n).bytes);
+    pl.blob = a.take<char>(prep_bounds({n}).blob_bytes);
   };
   // ---- size
   Plan pl;
@@ -276,12 +239,12 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     Arena a;
     region_a(a, pl);
     Arena b1 = a;
-    plan_bidiag(b1, m, n, ldw, P, kind, &pl.bw);
+    plan_bidiag(b1, m, n, ldw, nctas, kind, &pl.bw);
     b1.take<char>(gsc);
     Arena b2 = a;
     DDC_TRY(dc_sigma(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, b2, true));
     Arena b3 = a;
-    DDC_TRY(bd_vectors(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, dV, ldv, dU, ldu, nullptr, b3, true));
+    DDC_TRY(bd_vectors(ctx, n, (long long)n * n, nullptr, nullptr, nullptr, nullptr, nullptr, b3, true));
     Arena b4 = a;
     DDC_TRY(apply_left_reflectors(ctx, m, n, nullptr, ldw, nullptr, dU, ldu, n, kind, plain, b4, true));
     Arena b5 = a;
@@ -306,7 +269,7 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   DDC_CUDA_TRY(cudaGetLastError());
   {
     Arena b = a;
-    plan_bidiag(b, m, n, ldw, P, kind, &pl.bw);
+    plan_bidiag(b, m, n, ldw, nctas, kind, &pl.bw);
     Arena sc;
     sc.base = b.take<char>(gsc);
     sc.plan = false;
@@ -316,42 +279,38 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   }
   DDC_TRY(stage_event(ctx, 1));
   // ---- bidiagonal read-back: split at negligible superdiagonal entries and
-  //      build the D&C forest on the host (2n floats down, one blob up)
-  const BdBlob L = BdBlob::layout(n);
-  DcHost H;
+  //      build the D&C forest and vector layout on the host (2n floats down, one blob up)
+  const PrepBounds PB = prep_bounds({n});
+  Prep P;
   {
     const size_t rb = (size_t)round_up(sizeof(float) * 2 * (n + 4), 256);
-    DDC_TRY(ensure_pinned(ctx, rb + L.bytes));
+    const size_t ab = (size_t)round_up(sizeof(double) * 2 * (n + 4), 256);
+    DDC_TRY(ensure_pinned(ctx, rb + ab + PB.blob_bytes));
     float* hd = (float*)ctx->pinned;
     float* he = hd + n + 4;
     DDC_CUDA_TRY(cudaMemcpyAsync(hd, pl.d, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (n > 1)
       DDC_CUDA_TRY(cudaMemcpyAsync(he, pl.e, sizeof(float) * (n - 1), cudaMemcpyDeviceToHost, ctx->stream));
     DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    char* hb = (char*)ctx->pinned + rb;
-    double* a64 = (double*)(hb + L.off_b1);
-    double* b64 = (double*)(hb + L.off_b2);
+    double* a64 = (double*)((char*)ctx->pinned + rb);
+    double* b64 = a64 + n + 4;
     for (int i = 0; i < n; i++) {
       a64[i] = hd[i];
       b64[i] = (i < n - 1) ? (double)he[i] : 0.0;  // beta[N-1] := 0 (square case)
     }
-    DDC_TRY(prepare_bidiagonal(ctx, n, hb, pl.blob, FLT_EPSILON, &H));
+    char* hb = (char*)ctx->pinned + rb + ab;
+    DDC_TRY(prep_build(ctx, {n}, {GroupOut{dV, ldv, dU, ldu}}, a64, b64, FLT_EPSILON, false, hb, pl.blob, &P));
   }
-  const double* b1 = (const double*)(pl.blob + L.off_b1);
-  const double* b2 = (const double*)(pl.blob + L.off_b2);
-  const int* blo = (const int*)(pl.blob + L.off_lo);
-  const int* bhi = (const int*)(pl.blob + L.off_hi);
-  const int* dints = (const int*)(pl.blob + L.off_ints);
   // ---- stage 2
   {
     Arena b = a;
-    DDC_TRY(dc_sigma(ctx, n, b1, b2, pl.sig_slot, &H, dints, b, false));
+    DDC_TRY(dc_sigma(ctx, n, P.b1, P.b2, pl.sig_slot, &P.H, P.dints, b, false));
   }
   DDC_TRY(stage_event(ctx, 2));
   // ---- stages 3-4: X straight into V, Y into the top of U (ascending order)
   {
     Arena b = a;
-    DDC_TRY(bd_vectors(ctx, n, b1, b2, pl.sig_slot, blo, bhi, dV, ldv, dU, ldu, pl.sig, b, false));
+    DDC_TRY(bd_vectors(ctx, n, P.store, P.b1, P.b2, pl.sig_slot, &P.L, pl.sig, b, false));
   }
   if (m > n) {
     zero_rows_kernel<<<dim3(std::min(ceil_div(m - n, 256), 64), n), 256, 0, ctx->stream>>>(n, m, n, dU, ldu);
@@ -394,8 +353,8 @@ __global__ void transpose_f32_kernel(int rows, int cols, const float* __restrict
 static int svd_device(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                       int ldu, float* dV, int ldv, int mode, float* dAT_scratch) {
   mode = resolve_mode(mode);
-  if (mode < DDCSVD_MODE_PLAIN_FP32 || mode > DDCSVD_MODE_BLOCKED_BF16X3) return DDCSVD_ERR_ARG;
-  if ((mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3) && !tc_available(ctx)) {
+  if (mode < DDCSVD_MODE_PLAIN_FP32 || mode > DDCSVD_MODE_BLOCKED_TF32X6) return DDCSVD_ERR_ARG;
+  if (mode >= DDCSVD_MODE_BLOCKED_TF32X3 && !tc_available(ctx)) {
     set_last_error("tensor-core mode requested but tcgen05 kernels are unavailable on this device");
     return DDCSVD_ERR_UNSUPPORTED;
   }
@@ -562,8 +521,7 @@ int ddcsvd_svd_f32_device(ddcsvd_handle_t h, int m, int n, const float* dA, int 
 static int bidiag_device(ddcsvd_context* h, int m, int n, float* dA, int lda, float* dD, float* dE,
                          float* dTauq, float* dTaup, int mode) {
   mode = resolve_mode(mode);
-  if ((mode == DDCSVD_MODE_BLOCKED_TF32X3 || mode == DDCSVD_MODE_BLOCKED_BF16X3) && !tc_available(h))
-    return DDCSVD_ERR_UNSUPPORTED;
+  if (mode >= DDCSVD_MODE_BLOCKED_TF32X3 && !tc_available(h)) return DDCSVD_ERR_UNSUPPORTED;
   const GemmKind kind = kind_of(mode);
   BidiagWork bw;
   size_t scb = gemm_scratch_bytes(kind, m, n, 2 * kPanel);
@@ -599,67 +557,49 @@ int ddcsvd_bidiag_f32_device(ddcsvd_handle_t h, int m, int n, float* dA, int lda
 // (FP64 tolerance), build the forest, run D&C (and the vectors if asked).
 static int bd_standalone(ddcsvd_context* h, int N, const double* dB1, const double* dB2, bool square,
                          const double* dSigmaIn, double* dSigmaOut, float* dX, float* dY) {
-  const BdBlob L = BdBlob::layout(N);
-  // workspace: blob + sigma (slot order) + max(D&C, vectors)
+  const PrepBounds PB = prep_bounds({N});
   size_t need;
   {
     Arena a;
-    a.take<char>(L.bytes);
+    a.take<char>(PB.blob_bytes);
     a.take<double>(N + 4);
     Arena b = a, c = a;
     DDC_TRY(dc_sigma(h, N, nullptr, nullptr, nullptr, nullptr, nullptr, b, true));
-    if (dX) DDC_TRY(bd_vectors(h, N, nullptr, nullptr, nullptr, nullptr, nullptr, dX, N, dY, N, nullptr, c, true));
+    if (dX) DDC_TRY(bd_vectors(h, N, (long long)N * N, nullptr, nullptr, nullptr, nullptr, nullptr, c, true));
+    c.take<int>(N + 8);
     need = std::max(b.off, c.off);
   }
   DDC_TRY(ensure_workspace(h, need + 4096));
   Arena a;
   a.plan = false;
   a.base = (char*)h->ws;
-  char* blob = a.take<char>(L.bytes);
+  char* blob = a.take<char>(PB.blob_bytes);
   double* sig_slot = a.take<double>(N + 4);
-  DDC_TRY(ensure_pinned(h, L.bytes));
-  char* hb = (char*)h->pinned;
-  DDC_CUDA_TRY(cudaMemcpyAsync(hb + L.off_b1, dB1, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
-  DDC_CUDA_TRY(cudaMemcpyAsync(hb + L.off_b2, dB2, sizeof(double) * (square ? std::max(N - 1, 0) : N),
-                               cudaMemcpyDeviceToHost, h->stream));
+  const size_t ab = (size_t)round_up(sizeof(double) * 2 * (N + 4), 256);
+  DDC_TRY(ensure_pinned(h, ab + PB.blob_bytes));
+  double* a64 = (double*)h->pinned;
+  double* b64 = a64 + N + 4;
+  DDC_CUDA_TRY(cudaMemcpyAsync(a64, dB1, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaMemcpyAsync(b64, dB2, sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
   DDC_CUDA_TRY(cudaStreamSynchronize(h->stream));
-  double* b64 = (double*)(hb + L.off_b2);
-  const double last = square ? 0.0 : b64[N - 1];
   if (square) b64[N - 1] = 0.0;
-  DcHost H;
-  {
-    // split keeps the coupling to the extra column of an N x (N+1) bidiagonal
-    const BdBlob& LL = L;
-    double* a64 = (double*)(hb + LL.off_b1);
-    std::vector<int> starts;
-    split_bidiagonal(N, a64, b64, DBL_EPSILON, starts, (int*)(hb + LL.off_lo), (int*)(hb + LL.off_hi));
-    b64[N - 1] = last;
-    dc_build_host(N, starts, H);
-    memcpy(hb + LL.off_ints, H.ints.data(), sizeof(int) * H.ints.size());
-    DDC_CUDA_TRY(cudaMemcpyAsync(blob, hb, LL.off_ints + sizeof(int) * H.ints.size(), cudaMemcpyHostToDevice,
-                                 h->stream));
-  }
-  const double* b1 = (const double*)(blob + L.off_b1);
-  const double* b2 = (const double*)(blob + L.off_b2);
-  const int* blo = (const int*)(blob + L.off_lo);
-  const int* bhi = (const int*)(blob + L.off_hi);
-  const int* dints = (const int*)(blob + L.off_ints);
+  Prep P;
+  DDC_TRY(prep_build(h, {N}, {GroupOut{dX, N, dY, N}}, a64, b64, DBL_EPSILON, !square, (char*)h->pinned + ab, blob,
+                     &P));
   DDC_TRY(reset_status(h));
-  // node 0 is the first block's root; it spans all rows iff nothing split
-  const int root_rows = H.ints[H.nnodes];
-  const bool single = dSigmaIn != nullptr && root_rows == N;
-  if (dX && single) {
+  if (dX && P.single_block && dSigmaIn) {
     // one unreduced block: the caller's ascending sigma is already in slot order
     DDC_CUDA_TRY(cudaMemcpyAsync(sig_slot, dSigmaIn, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->stream));
   } else {
     Arena b = a;
-    DDC_TRY(dc_sigma(h, N, b1, b2, sig_slot, &H, dints, b, false));
+    DDC_TRY(dc_sigma(h, N, P.b1, P.b2, sig_slot, &P.H, P.dints, b, false));
   }
   if (dX) {
     Arena c = a;
-    DDC_TRY(bd_vectors(h, N, b1, b2, sig_slot, blo, bhi, dX, N, dY, N, dSigmaOut, c, false));
+    DDC_TRY(bd_vectors(h, N, P.store, P.b1, P.b2, sig_slot, &P.L, dSigmaOut, c, false));
   } else {
-    DDC_TRY(sort_values(h, N, sig_slot, dSigmaOut, a));
+    Arena c = a;
+    DDC_TRY(sort_values(h, N, sig_slot, dSigmaOut, &P.L, c));
   }
   return check_status(h, dX ? "bdvec" : "bdsdc");
 }

@@ -1,12 +1,402 @@
-// batched.cu -- many uneven SVDs per launch sequence.
+// batched.cu -- many independent SVDs of uneven sizes in one launch sequence.
+//
+// Stage 1 (bidiagonalisation) and stage 5 (back-transformation) run one CTA
+// per problem: a persistent kernel pulls problems from an atomic work counter
+// in decreasing-size order (host-sorted), keeps the problem in shared memory
+// when it fits (global memory, L1/L2-resident, otherwise) and runs the
+// reference's unblocked algorithm (bidiag.c:33-186; rank-1 left and right
+// updates per step) with CTA-wide synchronisation only.  Stages 2-4 reuse the
+// single-matrix machinery unchanged: every problem's bidiagonal becomes one
+// or more trees of the D&C forest (one cooperative launch for the whole
+// batch) and one output group of the vector stage.
+//
+// Problems with m < n are decomposed through A^T (U and V swap roles).
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
 #include "internal.hpp"
+#include "prep.hpp"
+
+namespace ddcsvd {
+
+struct BatchTask {
+  int m, n;      // oriented problem: m >= n
+  int trans;     // 1 if the caller's matrix is n x m (decomposed as its transpose)
+  int pad;
+  long long offW;  // working copy (m x n, ld m)
+  long long offD;  // first slot of the bidiagonal (sum of previous n)
+  long long offA;  // caller's input
+  long long offU;  // core left vectors (m x n, ld m) -> caller's U or V
+  long long offV;  // core right vectors (n x n, ld n) -> caller's V or U
+  long long offS;  // caller's sigma
+};
+
+constexpr int kBatchThreads = 256;
+
+__device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
+
+// Reflector parameters from x0 and the squared norm of the rest (FP64).
+__device__ __forceinline__ void bhouse(float x0, double t2, float* alpha, float* tau, float* scale) {
+  const double nrm = sqrt((double)x0 * (double)x0 + t2);
+  if (nrm == 0.0) {
+    *alpha = 0.f;
+    *tau = 0.f;
+    *scale = 0.f;
+    return;
+  }
+  const double a = -(x0 < 0.f ? -1.0 : 1.0) * nrm;
+  *alpha = (float)a;
+  *tau = (float)((nrm + fabs((double)x0)) / nrm);
+  *scale = (float)(1.0 / ((double)x0 - a));
+}
+
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int k = 0; k < nw; k++) r += red[k];
+  __syncthreads();
+  return r;
+}
+
+// Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA.
+// Reflectors stay in M in LAPACK form (unit leading entry stored).
+__device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, float* tq, float* tp,
+                           float* vrow, double* red, float* scal) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  for (int i = 0; i < n; i++) {
+    // ---- left reflector from column i
+    double s2 = 0.0;
+    for (int r = i + 1 + t; r < m; r += blockDim.x) {
+      const double x = M[r + (size_t)i * ld];
+      s2 += x * x;
+    }
+    s2 = cta_sum(s2, red);
+    if (t == 0) {
+      float a, ta, sc;
+      bhouse(M[i + (size_t)i * ld], s2, &a, &ta, &sc);
+      scal[0] = ta;
+      scal[1] = sc;
+      d[i] = a;
+      tq[i] = ta;
+    }
+    __syncthreads();
+    const float tauq = scal[0], sq = scal[1];
+    for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
+    __syncthreads();
+    if (t == 0) M[i + (size_t)i * ld] = 1.f;
+    __syncthreads();
+    if (i == n - 1) break;
+    // ---- left update of columns > i (left_dotprods + left_update_mat)
+    if (tauq != 0.f) {
+      const float* u = M + (size_t)i * ld;
+      for (int c = i + 1 + wid; c < n; c += nw) {
+        float* col = M + (size_t)c * ld;
+        float w = 0.f;
+        for (int r = i + lane; r < m; r += 32) w += u[r] * col[r];
+        w = warp_sum(w) * tauq;
+        for (int r = i + lane; r < m; r += 32) col[r] -= w * u[r];
+      }
+    }
+    __syncthreads();
+    // ---- right reflector from row i
+    double r2 = 0.0;
+    for (int c = i + 2 + t; c < n; c += blockDim.x) {
+      const double x = M[i + (size_t)c * ld];
+      r2 += x * x;
+    }
+    r2 = cta_sum(r2, red);
+    if (t == 0) {
+      float b, ta, sc;
+      const float x0 = M[i + (size_t)(i + 1) * ld];
+      if (i < n - 2) {
+        bhouse(x0, r2, &b, &ta, &sc);
+      } else {  // one element left: no reflection (bidiag.c:125-129)
+        b = x0;
+        ta = 0.f;
+        sc = 0.f;
+      }
+      scal[2] = ta;
+      scal[3] = sc;
+      e[i] = b;
+      tp[i] = ta;
+    }
+    __syncthreads();
+    const float taup = scal[2], sp = scal[3];
+    for (int c = i + 1 + t; c < n; c += blockDim.x) {
+      float v;
+      if (c == i + 1) v = (taup != 0.f) ? 1.f : 0.f;
+      else v = M[i + (size_t)c * ld] * sp;
+      M[i + (size_t)c * ld] = v;
+      vrow[c] = v;
+    }
+    __syncthreads();
+    // ---- right update of rows > i (right_dotprods + right_update_mat)
+    if (taup != 0.f) {
+      for (int r = i + 1 + t; r < m; r += blockDim.x) {
+        float z = 0.f;
+        for (int c = i + 1; c < n; c++) z += M[r + (size_t)c * ld] * vrow[c];
+        z *= taup;
+        for (int c = i + 1; c < n; c++) M[r + (size_t)c * ld] -= z * vrow[c];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads) batch_bidiag_kernel(const BatchTask* __restrict__ tasks,
+                                                                     const int* __restrict__ order, int ntask,
+                                                                     int* counter, const float* __restrict__ A,
+                                                                     float* W, float* d, float* e, float* tq,
+                                                                     float* tp, int smem_floats, int maxn) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int s_task;
+  __shared__ double red[32];
+  __shared__ float scal[8];
+  float* vrow = sm;                 // maxn
+  float* Ms = sm + ((maxn + 3) & ~3);  // problem copy when it fits
+  while (true) {
+    if (threadIdx.x == 0) s_task = atomicAdd(counter, 1);
+    __syncthreads();
+    const int q = s_task;
+    __syncthreads();
+    if (q >= ntask) break;
+    const BatchTask T = tasks[order[q]];
+    const int m = T.m, n = T.n, ld = m;
+    const bool fits = (long long)m * n <= smem_floats;
+    float* Wg = W + T.offW;
+    float* M = fits ? Ms : Wg;
+    // load the (oriented) problem
+    const float* src = A + T.offA;
+    for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
+      const int r = idx % m, c = idx / m;
+      M[r + (size_t)c * ld] = T.trans ? src[c + (size_t)r * n] : src[idx];
+    }
+    __syncthreads();
+    cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, scal);
+    __syncthreads();
+    if (fits)
+      for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) Wg[idx] = M[idx];
+    __syncthreads();
+  }
+}
+
+// U_core = Q [Y; 0], V_core = P X for one problem per CTA (multU / multV).
+__global__ void __launch_bounds__(kBatchThreads) batch_backxform_kernel(const BatchTask* __restrict__ tasks,
+                                                                        int ntask, const float* __restrict__ W,
+                                                                        const float* __restrict__ tq,
+                                                                        const float* __restrict__ tp, float* U,
+                                                                        float* V, int smem_floats) {
+  extern __shared__ __align__(16) float sm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int q = blockIdx.x; q < ntask; q += gridDim.x) {
+    const BatchTask T = tasks[q];
+    const int m = T.m, n = T.n;
+    const bool fits = (long long)m * n <= smem_floats;
+    const float* Wg = W + T.offW;
+    if (fits)
+      for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) sm[idx] = Wg[idx];
+    const float* R = fits ? sm : Wg;
+    // core U / V of a transposed problem are the caller's V / U
+    float* Uc = (T.trans ? V : U) + T.offU;
+    float* Vc = (T.trans ? U : V) + T.offV;
+    // rows n..m-1 of [Y; 0]
+    for (int idx = threadIdx.x; idx < (m - n) * n; idx += blockDim.x) {
+      const int r = n + idx % (m - n), c = idx / (m - n);
+      Uc[r + (size_t)c * m] = 0.f;
+    }
+    __syncthreads();
+    const float* tauq = tq + T.offD;
+    const float* taup = tp + T.offD;
+    for (int c = wid; c < n; c += nw) {
+      float* col = Uc + (size_t)c * m;
+      for (int j = n - 1; j >= 0; j--) {
+        const float t = tauq[j];
+        if (t == 0.f) continue;
+        const float* u = R + (size_t)j * m;  // unit stored at u[j]
+        float s = 0.f;
+        for (int r = j + lane; r < m; r += 32) s += u[r] * col[r];
+        s = warp_sum(s) * t;
+        for (int r = j + lane; r < m; r += 32) col[r] -= s * u[r];
+        __syncwarp();
+      }
+      float* vc = Vc + (size_t)c * n;
+      for (int j = n - 3; j >= 0; j--) {
+        const float t = taup[j];
+        if (t == 0.f) continue;
+        float s = 0.f;  // right reflector j: row j of R from column j+1 (unit stored)
+        for (int k = j + 1 + lane; k < n; k += 32) s += R[j + (size_t)k * m] * vc[k];
+        s = warp_sum(s) * t;
+        for (int k = j + 1 + lane; k < n; k += 32) vc[k] -= s * R[j + (size_t)k * m];
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void batch_sigma_out_kernel(const BatchTask* __restrict__ tasks, int ntask, const double* sig,
+                                       float* S) {
+  for (int q = blockIdx.x; q < ntask; q += gridDim.x) {
+    const BatchTask T = tasks[q];
+    for (int i = threadIdx.x; i < T.n; i += blockDim.x) S[T.offS + i] = (float)sig[T.offD + i];
+  }
+}
+
+}  // namespace ddcsvd
+
+using namespace ddcsvd;
 
 extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const int* m, const int* n,
                                              const float* dA, const long long* offA, float* dSigma,
                                              const long long* offS, float* dU, const long long* offU,
                                              float* dV, const long long* offV) {
-  (void)h; (void)batch; (void)m; (void)n; (void)dA; (void)offA; (void)dSigma; (void)offS; (void)dU;
-  (void)offU; (void)dV; (void)offV;
-  ddcsvd::set_last_error("batched path not built yet");
-  return DDCSVD_ERR_UNSUPPORTED;
+  if (!h || batch <= 0 || !m || !n || !dA || !offA || !dSigma || !offS || !dU || !offU || !dV || !offV)
+    return DDCSVD_ERR_ARG;
+  for (int b = 0; b < batch; b++)
+    if (m[b] <= 0 || n[b] <= 0) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  // ---- task table (oriented so that m >= n)
+  std::vector<BatchTask> tasks(batch);
+  std::vector<int> gn(batch);
+  std::vector<GroupOut> gout(batch);
+  long long offW = 0, offD = 0;
+  int maxn = 0;
+  long long maxmn = 0;
+  for (int b = 0; b < batch; b++) {
+    BatchTask& T = tasks[b];
+    T.trans = m[b] < n[b];
+    T.m = std::max(m[b], n[b]);
+    T.n = std::min(m[b], n[b]);
+    T.pad = 0;
+    T.offW = offW;
+    T.offD = offD;
+    T.offA = offA[b];
+    T.offS = offS[b];
+    // core U (m x n) is the caller's U, or V when transposed; same for core V
+    T.offU = T.trans ? offV[b] : offU[b];
+    T.offV = T.trans ? offU[b] : offV[b];
+    offW += (long long)T.m * T.n;
+    offD += T.n;
+    maxn = std::max(maxn, T.n);
+    maxmn = std::max(maxmn, (long long)T.m * T.n);
+    gn[b] = T.n;
+    float* Ucore = T.trans ? dV : dU;
+    float* Vcore = T.trans ? dU : dV;
+    gout[b] = GroupOut{Vcore + T.offV, T.n, Ucore + T.offU, T.m};
+  }
+  const int Ntot = (int)offD;
+  std::vector<int> order(batch);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (long long)tasks[x].m * tasks[x].n > (long long)tasks[y].m * tasks[y].n;
+  });
+  const PrepBounds PB = prep_bounds(gn);
+  // ---- workspace
+  auto layout = [&](Arena& a, float** W, float** d, float** e, float** tq, float** tp, BatchTask** dt, int** dord,
+                    int** counter, char** blob, double** sig_slot, double** sig) {
+    *W = a.take<float>(offW + 64);
+    *d = a.take<float>(Ntot + 8);
+    *e = a.take<float>(Ntot + 8);
+    *tq = a.take<float>(Ntot + 8);
+    *tp = a.take<float>(Ntot + 8);
+    *dt = a.take<BatchTask>(batch);
+    *dord = a.take<int>(batch);
+    *counter = a.take<int>(8);
+    *blob = a.take<char>(PB.blob_bytes);
+    *sig_slot = a.take<double>(Ntot + 8);
+    *sig = a.take<double>(Ntot + 8);
+  };
+  float *W, *d, *e, *tq, *tp;
+  BatchTask* dt;
+  int *dord, *counter;
+  char* blob;
+  double *sig_slot, *sig;
+  size_t need;
+  {
+    Arena a;
+    layout(a, &W, &d, &e, &tq, &tp, &dt, &dord, &counter, &blob, &sig_slot, &sig);
+    Arena b = a, c = a;
+    DDC_TRY(dc_sigma(h, Ntot, nullptr, nullptr, nullptr, nullptr, nullptr, b, true));
+    DDC_TRY(bd_vectors(h, Ntot, PB.store, nullptr, nullptr, nullptr, nullptr, nullptr, c, true));
+    need = std::max(b.off, c.off);
+  }
+  DDC_TRY(ensure_workspace(h, need + 4096));
+  Arena a;
+  a.plan = false;
+  a.base = (char*)h->ws;
+  layout(a, &W, &d, &e, &tq, &tp, &dt, &dord, &counter, &blob, &sig_slot, &sig);
+  // ---- pinned staging: tasks + order, then (after stage 1) the bidiagonal and the prep blob
+  const size_t tb = (size_t)round_up(sizeof(BatchTask) * batch + sizeof(int) * batch + 64, 256);
+  const size_t rb = (size_t)round_up(sizeof(float) * 2 * (Ntot + 8), 256);
+  const size_t ab = (size_t)round_up(sizeof(double) * 2 * (Ntot + 8), 256);
+  DDC_TRY(ensure_pinned(h, tb + rb + ab + PB.blob_bytes));
+  char* pin = (char*)h->pinned;
+  memcpy(pin, tasks.data(), sizeof(BatchTask) * batch);
+  memcpy(pin + sizeof(BatchTask) * batch, order.data(), sizeof(int) * batch);
+  DDC_TRY(reset_status(h));
+  DDC_CUDA_TRY(cudaMemcpyAsync(dt, pin, sizeof(BatchTask) * batch, cudaMemcpyHostToDevice, h->stream));
+  DDC_CUDA_TRY(cudaMemcpyAsync(dord, pin + sizeof(BatchTask) * batch, sizeof(int) * batch, cudaMemcpyHostToDevice,
+                               h->stream));
+  DDC_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), h->stream));
+  // ---- stage 1: persistent CTAs over the size-sorted work list
+  const int smem_floats = 24 * 1024;  // problems up to 24K entries live in shared memory
+  const size_t smem = sizeof(float) * ((size_t)((maxn + 3) & ~3) + smem_floats);
+  DDC_CUDA_TRY(cudaFuncSetAttribute(batch_bidiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 1;
+  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_bidiag_kernel, kBatchThreads, smem));
+  const int grid1 = std::max(1, std::min(batch, h->num_sms * std::max(occ, 1)));
+  ktimer_begin(h, KC_BIDIAG);
+  batch_bidiag_kernel<<<grid1, kBatchThreads, smem, h->stream>>>(dt, dord, batch, counter, dA, W, d, e, tq, tp,
+                                                                 smem_floats, maxn);
+  ktimer_end(h);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  // ---- bidiagonal read-back and preparation (one forest, one group per problem)
+  float* hd = (float*)(pin + tb);
+  float* he = hd + Ntot + 8;
+  DDC_CUDA_TRY(cudaMemcpyAsync(hd, d, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaMemcpyAsync(he, e, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  double* a64 = (double*)(pin + tb + rb);
+  double* b64 = a64 + Ntot + 8;
+  for (int b = 0; b < batch; b++) {
+    const long long o = tasks[b].offD;
+    const int nb = tasks[b].n;
+    for (int i = 0; i < nb; i++) {
+      a64[o + i] = hd[o + i];
+      b64[o + i] = (i < nb - 1) ? (double)he[o + i] : 0.0;
+    }
+  }
+  Prep P;
+  DDC_TRY(prep_build(h, gn, gout, a64, b64, FLT_EPSILON, false, pin + tb + rb + ab, blob, &P));
+  // ---- stages 2-4
+  {
+    Arena b = a;
+    DDC_TRY(dc_sigma(h, Ntot, P.b1, P.b2, sig_slot, &P.H, P.dints, b, false));
+  }
+  {
+    Arena c = a;
+    DDC_TRY(bd_vectors(h, Ntot, P.store, P.b1, P.b2, sig_slot, &P.L, sig, c, false));
+  }
+  // ---- stage 5 and sigma
+  const size_t smem5 = sizeof(float) * (size_t)std::min<long long>(maxmn, smem_floats);
+  DDC_CUDA_TRY(cudaFuncSetAttribute(batch_backxform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)std::max<size_t>(smem5, 16)));
+  ktimer_begin(h, KC_BACKXFORM);
+  batch_backxform_kernel<<<std::min(batch, 8 * h->num_sms), kBatchThreads, smem5, h->stream>>>(dt, batch, W, tq, tp,
+                                                                                             dU, dV, smem_floats);
+  count_launch();
+  ktimer_end(h);
+  batch_sigma_out_kernel<<<std::min(batch, 1024), 128, 0, h->stream>>>(dt, batch, sig, dSigma);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return check_status(h, "svd_batched");
 }

@@ -1,13 +1,16 @@
-// gemm_tc.cu -- tcgen05 tensor-core GEMM in split TF32 (3xTF32) for sm_103a.
+// gemm_tc.cu -- tcgen05 tensor-core GEMM in split TF32 for sm_103a.
 //
 //   C (M x N, col-major) = beta * C + alpha * A B,   A: M x K, B: K x N,
 //   both operands K-major in global memory (row r of A at A + r*lda, column
 //   n of B at B + n*ldb, K contiguous).
 //
-// FP32 accuracy from TF32 tensor cores: each FP32 operand x is split into
-// hi = tf32(x) and lo = tf32(x - hi) (both round-to-nearest), and the product
-// is accumulated as hi*hi + hi*lo + lo*hi in FP32 in TMEM (the lo*lo term,
-// ~2^-22 relative, is dropped).
+// FP32 accuracy from TF32 tensor cores.  Each FP32 operand x is split into
+// TF32 parts (round-to-nearest) and the products of the parts are summed in
+// FP32 in TMEM:
+//   2 parts (GEMM_TF32X3): x = h + l, h*h' + h*l' + l*h'      ~2^-21 relative
+//   3 parts (GEMM_TF32X6): x = h + m + l,
+//                          h*h' + h*m' + m*h' + m*m' + h*l' + l*h'  below FP32
+// (smallest products are issued first).
 //
 // One CTA computes a 128 x BN tile (BN = 128 or 64), 6 warps:
 //   warp 0      TMA producer: raw FP32 K-slabs (32 wide, 128-byte swizzle)
@@ -39,7 +42,6 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BK = 32;  // FP32 elements per slab row: 128 bytes = one swizzle span
-constexpr int STAGES = 3;
 constexpr int THREADS = 192;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
@@ -143,21 +145,23 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
   return r;
 }
 
-// In-place split of a raw FP32 tile: raw -> hi, lo buffer <- tf32(raw - hi).
-__device__ __forceinline__ void split_tile(float4* raw, float4* lo, int n16, int t, int nt) {
+// In-place split of a raw FP32 tile into NP TF32 parts: raw -> part 0, the
+// others into part buffers 1 (and 2), all in the same (swizzled) positions.
+template <int NP>
+__device__ __forceinline__ void split_tile(float4* raw, float4* p1, float4* p2, int n16, int t, int nt) {
   for (int q = t; q < n16; q += nt) {
-    float4 v = raw[q];
-    float4 h, l;
-    h.x = __uint_as_float(to_tf32(v.x));
-    h.y = __uint_as_float(to_tf32(v.y));
-    h.z = __uint_as_float(to_tf32(v.z));
-    h.w = __uint_as_float(to_tf32(v.w));
-    l.x = __uint_as_float(to_tf32(v.x - h.x));
-    l.y = __uint_as_float(to_tf32(v.y - h.y));
-    l.z = __uint_as_float(to_tf32(v.z - h.z));
-    l.w = __uint_as_float(to_tf32(v.w - h.w));
-    raw[q] = h;
-    lo[q] = l;
+    const float4 v = raw[q];
+    float x[4] = {v.x, v.y, v.z, v.w}, h[4], m[4], l[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      h[c] = __uint_as_float(to_tf32(x[c]));
+      const float r = x[c] - h[c];
+      m[c] = __uint_as_float(to_tf32(r));
+      if (NP == 3) l[c] = __uint_as_float(to_tf32(r - m[c]));
+    }
+    raw[q] = make_float4(h[0], h[1], h[2], h[3]);
+    p1[q] = make_float4(m[0], m[1], m[2], m[3]);
+    if (NP == 3) p2[q] = make_float4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -173,20 +177,22 @@ struct TcParams {
   DevStatus* st;
 };
 
-template <int BN>
+template <int BN, int NP>
 struct Layout {
   static constexpr int A_BYTES = BM * BK * 4;
   static constexpr int B_BYTES = BN * BK * 4;
-  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = (NP == 2) ? 3 : 2;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
   static constexpr int TMEM_COLS = BN < 32 ? 32 : BN;
 };
 
-template <int BN>
+template <int BN, int NP>
 __global__ void __launch_bounds__(THREADS, 1)
-    tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                          TcParams p) {
-  using L = Layout<BN>;
+    tc_gemm_split_tf32_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                              TcParams p) {
+  using L = Layout<BN, NP>;
+  constexpr int STAGES = L::STAGES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(round_up(reinterpret_cast<uintptr_t>(smem_raw), 1024));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::STAGE);
@@ -223,10 +229,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int s_begin = blockIdx.z * p.per_split;
   const int s_end = min(p.nslab, s_begin + p.per_split);
   const int nsl = max(0, s_end - s_begin);
-  auto a_hi = [&](int s) { return smem + s * L::STAGE; };
-  auto a_lo = [&](int s) { return smem + s * L::STAGE + L::A_BYTES; };
-  auto b_hi = [&](int s) { return smem + s * L::STAGE + 2 * L::A_BYTES; };
-  auto b_lo = [&](int s) { return smem + s * L::STAGE + 2 * L::A_BYTES + L::B_BYTES; };
+  // stage layout: A parts 0..NP-1, then B parts 0..NP-1 (part 0 = raw -> hi)
+  auto a_part = [&](int s, int k) { return smem + s * L::STAGE + k * L::A_BYTES; };
+  auto b_part = [&](int s, int k) { return smem + s * L::STAGE + NP * L::A_BYTES + k * L::B_BYTES; };
+  auto a_hi = [&](int s) { return a_part(s, 0); };
+  auto b_hi = [&](int s) { return b_part(s, 0); };
 
   if (warp == 0) {
     if (lane == 0) {
@@ -255,16 +262,28 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int s = i % STAGES;
         if (!mbar_wait(&conv[s], (i / STAGES) & 1, abort_flag, p.st, 902)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t ah = smem_u32(a_hi(s)), al = smem_u32(a_lo(s));
-        const uint32_t bh = smem_u32(b_hi(s)), bl = smem_u32(b_lo(s));
 #pragma unroll
         for (int kk = 0; kk < BK / 8; kk++) {
           const uint32_t off = kk * 32;  // 8 TF32 elements = 32 bytes along K
-          const uint64_t dah = smem_desc_sw128(ah + off), dal = smem_desc_sw128(al + off);
-          const uint64_t dbh = smem_desc_sw128(bh + off), dbl = smem_desc_sw128(bl + off);
-          mma_tf32(tmem, dal, dbh, idesc, (i > 0 || kk > 0) ? 1u : 0u);
-          mma_tf32(tmem, dah, dbl, idesc, 1u);
-          mma_tf32(tmem, dah, dbh, idesc, 1u);
+          uint64_t da[NP], db[NP];
+#pragma unroll
+          for (int k = 0; k < NP; k++) {
+            da[k] = smem_desc_sw128(smem_u32(a_part(s, k)) + off);
+            db[k] = smem_desc_sw128(smem_u32(b_part(s, k)) + off);
+          }
+          const uint32_t first = (i > 0 || kk > 0) ? 1u : 0u;
+          if (NP == 3) {  // l*h, h*l, m*m, m*h, h*m, h*h
+            mma_tf32(tmem, da[2], db[0], idesc, first);
+            mma_tf32(tmem, da[0], db[2], idesc, 1u);
+            mma_tf32(tmem, da[1], db[1], idesc, 1u);
+            mma_tf32(tmem, da[1], db[0], idesc, 1u);
+            mma_tf32(tmem, da[0], db[1], idesc, 1u);
+            mma_tf32(tmem, da[0], db[0], idesc, 1u);
+          } else {  // l*h, h*l, h*h
+            mma_tf32(tmem, da[1], db[0], idesc, first);
+            mma_tf32(tmem, da[0], db[1], idesc, 1u);
+            mma_tf32(tmem, da[0], db[0], idesc, 1u);
+          }
         }
         mma_commit(&empty[s]);
       }
@@ -275,8 +294,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int i = 0; i < nsl; i++) {
       const int s = i % STAGES;
       if (!mbar_wait(&full[s], (i / STAGES) & 1, abort_flag, p.st, 903)) break;
-      split_tile(reinterpret_cast<float4*>(a_hi(s)), reinterpret_cast<float4*>(a_lo(s)), L::A_BYTES / 16, ct, 128);
-      split_tile(reinterpret_cast<float4*>(b_hi(s)), reinterpret_cast<float4*>(b_lo(s)), L::B_BYTES / 16, ct, 128);
+      split_tile<NP>(reinterpret_cast<float4*>(a_part(s, 0)), reinterpret_cast<float4*>(a_part(s, 1)),
+                     reinterpret_cast<float4*>(a_part(s, NP - 1)), L::A_BYTES / 16, ct, 128);
+      split_tile<NP>(reinterpret_cast<float4*>(b_part(s, 0)), reinterpret_cast<float4*>(b_part(s, 1)),
+                     reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, 128);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&conv[s]);
     }
@@ -359,18 +380,18 @@ static int make_map(CUtensorMap* map, const float* base, long long kext, long lo
   return DDCSVD_OK;
 }
 
-template <int BN>
+template <int BN, int NP>
 static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long long lda, int a_koff,
                   const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha, float beta,
                   Arena* scratch) {
-  using L = Layout<BN>;
+  using L = Layout<BN, NP>;
   CUtensorMap ma, mb;
   DDC_TRY(make_map(&ma, A, (long long)a_koff + K, M, lda, BM));
   DDC_TRY(make_map(&mb, B, (long long)b_koff + K, N, ldb, BN));
   static bool attr_set = false;
   if (!attr_set) {
-    DDC_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      L::SMEM));
+    DDC_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_split_tf32_kernel<BN, NP>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, L::SMEM));
     attr_set = true;
   }
   TcParams p;
@@ -395,7 +416,7 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   ksplit = ceil_div(p.nslab, p.per_split);
   p.partial = (ksplit > 1) ? reinterpret_cast<float*>(scratch->base) : nullptr;
   dim3 grid(ceil_div(M, BM), ceil_div(N, BN), ksplit);
-  tc_gemm_tf32x3_kernel<BN><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, p);
+  tc_gemm_split_tf32_kernel<BN, NP><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, p);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
   if (ksplit > 1) splitk_reduce(ctx, M, N, ksplit, p.partial, alpha, beta, C, ldc);
@@ -422,14 +443,18 @@ size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K) {
 int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
                    int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
                    float beta, Arena* scratch) {
-  if (kind != GEMM_TF32X3) {
+  if (kind != GEMM_TF32X3 && kind != GEMM_TF32X6) {
     set_last_error("split-BF16 tensor-core GEMM is not implemented");
     return DDCSVD_ERR_UNSUPPORTED;
   }
   if (M <= 0 || N <= 0) return DDCSVD_OK;
   if ((a_koff & 3) || (b_koff & 3)) return DDCSVD_ERR_ARG;
-  if (N <= 64) return tc::launch<64>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
-  return tc::launch<128>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+  if (kind == GEMM_TF32X6) {
+    if (N <= 64) return tc::launch<64, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+    return tc::launch<128, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+  }
+  if (N <= 64) return tc::launch<64, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+  return tc::launch<128, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
 }
 
 // Strided-operand entry used by gemm(): only the K-major layouts map onto the

@@ -64,7 +64,7 @@ int check_status(ddcsvd_context* ctx, const char* stage);  // syncs the stream
 int reset_status(ddcsvd_context* ctx);
 
 // ---------------------------------------------------------------- GEMM back ends
-enum GemmKind { GEMM_SIMT = 0, GEMM_TF32X3 = 1, GEMM_BF16X3 = 2 };
+enum GemmKind { GEMM_SIMT = 0, GEMM_TF32X3 = 1, GEMM_BF16X3 = 2, GEMM_TF32X6 = 3 };
 
 // Operand descriptor: element (r, c) of the logical matrix lives at
 // p[r * rs + c * cs]; exactly one of rs / cs is 1.
@@ -128,16 +128,18 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
 // Splits the N x N bidiagonal (host copies a[N], b[N]) at |b_i| <= 4 eps max|B|:
 // zeroes those b_i (and b[N-1]), fills block_starts (ascending, ends with N)
 // and, per row, the bounds of its block.
-int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, Arena& a);
+struct VecLayout;
+int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, const VecLayout* L, Arena& a);
 void split_bidiagonal(int N, double* a, double* b, double eps, std::vector<int>& block_starts,
                       int* blk_lo, int* blk_hi);
 
 // ---------------------------------------------------------------- stages 3-4
-// sigma (slot order: ascending within each block) -> X, Y columns in global
-// ascending order; sigma_sorted receives the sorted values.
-int bd_vectors(ddcsvd_context* ctx, int N, const double* a, const double* b, const double* sigma,
-               const int* blk_lo, const int* blk_hi, float* X, int ldx, float* Y, int ldy,
-               double* sigma_sorted, Arena& arena, bool plan_only);
+struct VecLayout;
+// sigma (slot order: ascending within each block) -> X, Y columns of every
+// group in ascending order; sigma_sorted receives the sorted values (group
+// ranges of slots).  `store` = sum over blocks of nb^2.
+int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, const double* b,
+               const double* sigma, const VecLayout* L, double* sigma_sorted, Arena& arena, bool plan_only);
 
 // ---------------------------------------------------------------- stage 5
 constexpr int kWY = 64;  // reflectors per WY block in the back-transformation

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "internal.hpp"
+#include "prep.hpp"
 
 namespace ddcsvd {
 
@@ -53,11 +54,11 @@ struct TwParams {
   int N;
   const double *dd, *ll, *dl, *dll;
   const double* sigma;
-  const int *blo, *bhi;       // block of each slot
-  double *Lp, *Um, *S, *Pp;  // N x N, interleaved [i * N + k]
-  double* Z;                  // N x N interleaved (zero outside the block)
-  double *xinv, *yinv;        // per vector
-  int* rank;                  // output column of each vector
+  VecLayout L;
+  double *Lp, *Um, *S, *Pp;  // compact block layout
+  double* Z;
+  double *xinv, *yinv;  // per vector
+  int* rank;            // position of each vector within its group (ascending sigma)
   const double *a, *b;
 };
 
@@ -66,7 +67,9 @@ __global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
   const bool act = k < N;
-  const int lo = act ? p.blo[k] : 0, hi = act ? p.bhi[k] : 0;
+  const int lo = act ? p.L.blo[k] : 0, hi = act ? p.L.bhi[k] : 0;
+  const int nb = hi - lo;
+  const long long base = act ? p.L.base[k] + (k - lo) : 0;  // element i at base + (i - lo) * nb
   const double lam = act ? p.sigma[k] * p.sigma[k] : 0.0;
   const double tiny = DBL_MIN / DBL_EPSILON;
   if (w == 0) {
@@ -76,53 +79,56 @@ __global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
       double dp = p.dd[i] + s;
       if (fabs(dp) < tiny) dp = -tiny;
       const double L = p.dl[i] / dp;
-      p.Lp[(size_t)i * N + k] = L;
-      p.S[(size_t)i * N + k] = s;
+      const long long e = base + (long long)(i - lo) * nb;
+      p.Lp[e] = L;
+      p.S[e] = s;
       s = L * p.ll[i] * s - lam;
     }
-    if (hi > lo) p.S[(size_t)(hi - 1) * N + k] = s;
+    if (hi > lo) p.S[base + (long long)(hi - 1 - lo) * nb] = s;
   } else if (hi > lo) {
     // progressive qd on the block: L D L^T - lam = U- D- U-^T, p_{hi-1} = d_{hi-1} - lam
     double pv = p.dd[hi - 1] - lam;
-    p.Pp[(size_t)(hi - 1) * N + k] = pv;
+    p.Pp[base + (long long)(hi - 1 - lo) * nb] = pv;
     for (int i = hi - 2; i >= lo; i--) {
       double dm = p.dll[i] + pv;
       if (fabs(dm) < tiny) dm = -tiny;
       const double tt = p.dd[i] / dm;
-      p.Um[(size_t)i * N + k] = p.ll[i] * tt;
+      const long long e = base + (long long)(i - lo) * nb;
+      p.Um[e] = p.ll[i] * tt;
       pv = pv * tt - lam;
-      p.Pp[(size_t)i * N + k] = pv;
+      p.Pp[e] = pv;
     }
   }
   __syncthreads();
   if (w != 0 || !act) return;
+  auto at = [&](int i) { return base + (long long)(i - lo) * nb; };
   // twist index r = argmin |gamma_i|, gamma_i = s_i + p_i + lam (ties: larger i)
   int r = hi - 1;
-  double gbest = fabs(p.S[(size_t)(hi - 1) * N + k] + p.Pp[(size_t)(hi - 1) * N + k] + lam);
+  double gbest = fabs(p.S[at(hi - 1)] + p.Pp[at(hi - 1)] + lam);
   for (int i = hi - 2; i >= lo; i--) {
-    const double g = fabs(p.S[(size_t)i * N + k] + p.Pp[(size_t)i * N + k] + lam);
+    const double g = fabs(p.S[at(i)] + p.Pp[at(i)] + lam);
     if (g < gbest) { gbest = g; r = i; }
   }
   // solve N_r z = gamma_r e_r with z_r = 1, outwards from r
   double nrm = 1.0;
-  p.Z[(size_t)r * N + k] = 1.0;
+  p.Z[at(r)] = 1.0;
   double z = 1.0;
   for (int i = r - 1; i >= lo; i--) {
-    z = -p.Lp[(size_t)i * N + k] * z;
-    p.Z[(size_t)i * N + k] = z;
+    z = -p.Lp[at(i)] * z;
+    p.Z[at(i)] = z;
     nrm += z * z;
   }
   z = 1.0;
   for (int i = r + 1; i < hi; i++) {
-    z = -p.Um[(size_t)(i - 1) * N + k] * z;
-    p.Z[(size_t)i * N + k] = z;
+    z = -p.Um[at(i - 1)] * z;
+    p.Z[at(i)] = z;
     nrm += z * z;
   }
   // ||B z||^2 for the left vector (b is zero at the block end)
   double by = 0.0;
-  double zi = p.Z[(size_t)lo * N + k];
+  double zi = p.Z[at(lo)];
   for (int i = lo; i < hi; i++) {
-    const double zn = (i + 1 < hi) ? p.Z[(size_t)(i + 1) * N + k] : 0.0;
+    const double zn = (i + 1 < hi) ? p.Z[at(i + 1)] : 0.0;
     const double y = p.a[i] * zi + ((i + 1 < hi) ? p.b[i] * zn : 0.0);
     by += y * y;
     zi = zn;
@@ -131,45 +137,72 @@ __global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
   p.yinv[k] = (by > 0.0) ? 1.0 / sqrt(by) : 0.0;
 }
 
-// rank[k] = position of sigma_k in ascending order (stable); sorted values out.
-__global__ void tw_rank_kernel(int N, const double* __restrict__ sigma, int* rank, double* sorted) {
+// rank of sigma_k among the sigmas of its group (ascending, stable).
+__global__ void tw_rank_kernel(int N, const double* __restrict__ sigma, VecLayout L, int* rank,
+                               double* sorted) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    const int g = L.grp[k];
+    const int g0 = L.g_lo[g], gn = L.g_n[g];
     const double v = sigma[k];
     int r = 0;
-    for (int j = 0; j < N; j++) {
+    for (int j = g0; j < g0 + gn; j++) {
       const double u = sigma[j];
       r += (u < v) || (u == v && j < k);
     }
     rank[k] = r;
-    if (sorted) sorted[r] = v;
+    if (sorted) sorted[g0 + r] = v;
   }
 }
 
-// X[i + rank_k*ldx] = z_k[i] / ||z_k||, Y[i + rank_k*ldy] = (B z_k)[i] / ||B z_k||.
-__global__ void tw_finalize_kernel(TwParams p, float* X, int ldx, float* Y, int ldy) {
+// One 32 x 32 tile (vectors k0.., rows i0.. of a block) per CTA:
+// X[i - g0 + rank_k * ldx] = z_k[i] / ||z_k||, Y[...] = (B z_k)[i] / ||B z_k||
+// (rows are local to the group; rows outside the block are zero).
+__global__ void tw_finalize_kernel(TwParams p) {
   __shared__ double tile[33][33];
-  const int N = p.N;
-  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+  const int4 T = p.L.tiles[blockIdx.x];
+  const int lo = T.x, nb = T.y, k0 = lo + T.z, i0 = lo + T.w, hi = lo + nb;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const long long base = p.L.base[lo];
   for (int rr = ty; rr < 33; rr += 8) {
     const int i = i0 + rr, k = k0 + tx;
-    tile[rr][tx] = (i < N && k < N) ? p.Z[(size_t)i * N + k] : 0.0;
+    tile[rr][tx] = (i < hi && k < hi) ? p.Z[base + (long long)(i - lo) * nb + (k - lo)] : 0.0;
   }
   __syncthreads();
   for (int kk = ty; kk < 32; kk += 8) {
     const int k = k0 + kk, i = i0 + tx;
-    if (k >= N || i >= N) continue;
+    if (k >= hi || i >= hi) continue;
+    const int g = p.L.grp[k];
+    const int g0 = p.L.g_lo[g];
     const int col = p.rank[k];
     const double xi = tile[tx][kk], xn = tile[tx + 1][kk];
-    X[i + (size_t)col * ldx] = (float)(xi * p.xinv[k]);
-    const double y = p.a[i] * xi + ((i + 1 < N) ? p.b[i] * xn : 0.0);
-    Y[i + (size_t)col * ldy] = (float)(y * p.yinv[k]);
+    p.L.g_X[g][(i - g0) + (size_t)col * p.L.g_ldx[g]] = (float)(xi * p.xinv[k]);
+    const double y = p.a[i] * xi + ((i + 1 < hi) ? p.b[i] * xn : 0.0);
+    p.L.g_Y[g][(i - g0) + (size_t)col * p.L.g_ldy[g]] = (float)(y * p.yinv[k]);
   }
 }
 
-int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, Arena& a) {
+// zero the rows of each output column that lie outside the vector's block
+__global__ void tw_zero_outside_kernel(int N, TwParams p) {
+  const int k = blockIdx.x;
+  if (k >= N) return;
+  const int g = p.L.grp[k], g0 = p.L.g_lo[g], gn = p.L.g_n[g];
+  const int lo = p.L.blo[k], hi = p.L.bhi[k];
+  if (hi - lo == gn) return;
+  const int col = p.rank[k];
+  float* X = p.L.g_X[g] + (size_t)col * p.L.g_ldx[g];
+  float* Y = p.L.g_Y[g] + (size_t)col * p.L.g_ldy[g];
+  for (int i = threadIdx.x; i < gn; i += blockDim.x) {
+    const int gi = g0 + i;
+    if (gi < lo || gi >= hi) {
+      X[i] = 0.f;
+      Y[i] = 0.f;
+    }
+  }
+}
+
+int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, const VecLayout* L, Arena& a) {
   int* rank = a.take<int>(N + 8);
-  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, in, rank, out);
+  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, in, *L, rank, out);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
@@ -198,13 +231,12 @@ void split_bidiagonal(int N, double* a, double* b, double eps, std::vector<int>&
     }
 }
 
-int bd_vectors(ddcsvd_context* ctx, int N, const double* a, const double* b, const double* sigma,
-               const int* blk_lo, const int* blk_hi, float* X, int ldx, float* Y, int ldy,
-               double* sigma_sorted, Arena& arena, bool plan_only) {
+int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, const double* b,
+               const double* sigma, const VecLayout* L, double* sigma_sorted, Arena& arena, bool plan_only) {
   if (N <= 0) return DDCSVD_ERR_ARG;
   double* small = arena.take<double>(6 * (size_t)N + 8);
   int* rank = arena.take<int>(N + 8);
-  double* big = arena.take<double>(5 * (size_t)N * N);
+  double* big = arena.take<double>(5 * (size_t)store);
   if (plan_only) return DDCSVD_OK;
   TwParams p;
   p.N = N;
@@ -216,22 +248,21 @@ int bd_vectors(ddcsvd_context* ctx, int N, const double* a, const double* b, con
   p.xinv = small + 4 * (size_t)N;
   p.yinv = small + 5 * (size_t)N;
   p.sigma = sigma;
-  p.blo = blk_lo;
-  p.bhi = blk_hi;
+  p.L = *L;
   p.rank = rank;
   p.a = a;
   p.b = b;
-  const size_t NN = (size_t)N * N;
-  p.Lp = big; p.Um = big + NN; p.S = big + 2 * NN; p.Pp = big + 3 * NN; p.Z = big + 4 * NN;
-  DDC_CUDA_TRY(cudaMemsetAsync(p.Z, 0, sizeof(double) * NN, ctx->stream));
+  p.Lp = big; p.Um = big + store; p.S = big + 2 * store; p.Pp = big + 3 * store; p.Z = big + 4 * store;
   ktimer_begin(ctx, KC_VECTORS);
   tw_setup_kernel<<<1, 256, 0, ctx->stream>>>(N, a, b, dd, ll, dl, dll);
   count_launch();
   twisted_kernel<<<ceil_div(N, 32), 64, 0, ctx->stream>>>(p);
   count_launch();
-  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, rank, sigma_sorted);
+  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, p.L, rank, sigma_sorted);
   count_launch();
-  tw_finalize_kernel<<<dim3(ceil_div(N, 32), ceil_div(N, 32)), dim3(32, 8), 0, ctx->stream>>>(p, X, ldx, Y, ldy);
+  tw_finalize_kernel<<<L->ntiles, dim3(32, 8), 0, ctx->stream>>>(p);
+  count_launch();
+  tw_zero_outside_kernel<<<N, 128, 0, ctx->stream>>>(N, p);
   count_launch();
   ktimer_end(ctx);
   DDC_CUDA_TRY(cudaGetLastError());

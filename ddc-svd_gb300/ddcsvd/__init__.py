@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from ._lib import MODES, DdcsvdError, check, load
 
-__all__ = ["svd_gpu", "bidiag_par", "svd", "Handle", "svd_device", "bidiag_device",
+__all__ = ["svd_gpu", "bidiag_par", "svd", "Handle", "BatchPlan", "svd_device", "bidiag_device",
            "bdsdc_sigma_device", "bdvec_device", "svd_batched_device", "svd_backward_device",
            "launch_count", "DdcsvdError", "MODES"]
 
@@ -228,6 +228,49 @@ def bdvec_device(a, b, sigma, handle: Handle | None = None):
     check(load().ddcsvd_bdvec_device(h.ptr, N, a.contiguous().data_ptr(), bb.data_ptr(),
                                      sigma.contiguous().data_ptr(), Xt.data_ptr(), Yt.data_ptr()), "bdvec")
     return Xt.t(), Yt.t()
+
+
+class BatchPlan:
+    """Device buffers and offset tables for repeated batched SVDs of fixed shapes.
+
+    A (flat, column-major per problem) is filled with `load(mats)`; `run()` is
+    the bare C-ABI call (what a benchmark times)."""
+
+    def __init__(self, shapes, device="cuda", handle: Handle | None = None):
+        import torch
+        self.h = _handle(handle)
+        self.ms = np.array([s[0] for s in shapes], dtype=np.int32)
+        self.ns = np.array([s[1] for s in shapes], dtype=np.int32)
+        ks = np.minimum(self.ms, self.ns).astype(np.int64)
+        m64, n64 = self.ms.astype(np.int64), self.ns.astype(np.int64)
+        def offs(sizes):
+            o = np.zeros(len(sizes), dtype=np.int64)
+            o[1:] = np.cumsum(sizes)[:-1]
+            return o
+        self.offA, self.offS = offs(m64 * n64), offs(ks)
+        self.offU, self.offV = offs(m64 * ks), offs(n64 * ks)
+        self.ks = ks
+        self.A = torch.empty(int((m64 * n64).sum()), dtype=torch.float32, device=device)
+        self.S = torch.empty(int(ks.sum()), dtype=torch.float32, device=device)
+        self.U = torch.empty(int((m64 * ks).sum()), dtype=torch.float32, device=device)
+        self.V = torch.empty(int((n64 * ks).sum()), dtype=torch.float32, device=device)
+
+    def load(self, mats):
+        import torch
+        self.A.copy_(torch.cat([a.t().contiguous().reshape(-1) for a in mats]))
+
+    def run(self):
+        check(load().ddcsvd_svd_batched_f32_device(
+            self.h.ptr, len(self.ms), _addr(self.ms), _addr(self.ns), self.A.data_ptr(), _addr(self.offA),
+            self.S.data_ptr(), _addr(self.offS), self.U.data_ptr(), _addr(self.offU), self.V.data_ptr(),
+            _addr(self.offV)), "svd_batched")
+
+    def result(self, b):
+        m, n, k = int(self.ms[b]), int(self.ns[b]), int(self.ks[b])
+        s = self.S[self.offS[b]: self.offS[b] + k]
+        U = self.U[self.offU[b]: self.offU[b] + m * k].view(k, m).t()
+        V = self.V[self.offV[b]: self.offV[b] + n * k].view(k, n).t()
+        return s, U, V
 
 
 def svd_batched_device(mats, handle: Handle | None = None):

@@ -15,7 +15,7 @@ c_int, c_ll, c_float, c_double, c_void_p = (ctypes.c_int, ctypes.c_longlong, cty
                                             ctypes.c_double, ctypes.c_void_p)
 P = c_void_p  # every pointer crosses the ABI as an untyped address
 
-MODES = {"auto": 0, "plain": 1, "blocked": 2, "tf32x3": 3, "bf16x3": 4}
+MODES = {"auto": 0, "plain": 1, "blocked": 2, "tf32x3": 3, "bf16x3": 4, "tf32x6": 5}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "did not converge", 5: "device wait timed out", 6: "no usable device",
           7: "input holds NaN or Inf", 8: "unsupported"}

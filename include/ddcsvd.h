@@ -44,14 +44,18 @@ extern "C" {
  *   BLOCKED_FP32 panel (WY / Bischof) bidiagonalisation with rank-2b trailing
  *                updates and WY back-transformation, FP32 CUDA-core GEMMs.
  *   BLOCKED_TF32X3 the same with the GEMMs on tcgen05 tensor cores in split
- *                TF32 (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM).
- *   BLOCKED_BF16X3 the same in split BF16.
- *   AUTO         BLOCKED_TF32X3.                                           */
+ *                TF32, two parts per operand (hi*hi + hi*lo + lo*hi, FP32
+ *                accumulation in TMEM): about 21 bits per product.
+ *   BLOCKED_BF16X3 reserved for split BF16 (returns DDCSVD_ERR_UNSUPPORTED).
+ *   BLOCKED_TF32X6 split TF32 with three parts per operand and six products
+ *                (h*h + h*m + m*h + m*m + h*l + l*h): FP32-level accuracy.
+ *   AUTO         BLOCKED_TF32X6.                                           */
 #define DDCSVD_MODE_AUTO 0
 #define DDCSVD_MODE_PLAIN_FP32 1
 #define DDCSVD_MODE_BLOCKED_FP32 2
 #define DDCSVD_MODE_BLOCKED_TF32X3 3
 #define DDCSVD_MODE_BLOCKED_BF16X3 4
+#define DDCSVD_MODE_BLOCKED_TF32X6 5
 
 typedef struct ddcsvd_context *ddcsvd_handle_t;
 

@@ -19,7 +19,7 @@ BASE_MODES = ["plain", "blocked"]
 
 
 def tc_modes(lib):
-    return [m for m in ("tf32x3", "bf16x3") if _mode_available(lib, m)]
+    return [m for m in ("tf32x6", "tf32x3", "bf16x3") if _mode_available(lib, m)]
 
 
 _avail = {}
@@ -169,16 +169,44 @@ def test_bidiag_stage_vs_oracle(lib, cuda, orc, mode, m, n):
         2e-6 * np.linalg.norm(A, 2)
 
 
+def _reflector_factors(A_r, m, n):
+    """Q, P from reflectors stored the reference's way (bidiag_par.c:63-68):
+    left reflector i in A_r[i:, i], right reflector i in A_r[i, i+1:], H = I - 2 v v^T."""
+    Q, P = np.eye(m), np.eye(n)
+    for i in range(n):
+        v = np.zeros(m)
+        v[i:] = A_r[i:, i]
+        Q = Q - 2.0 * np.outer(Q @ v, v)
+    for i in range(max(n - 2, 0)):
+        v = np.zeros(n)
+        v[i + 1:] = A_r[i, i + 1:]
+        P = P - 2.0 * np.outer(P @ v, v)
+    return Q, P
+
+
 @pytest.mark.parametrize("name", [g for g in golden_names("bidiag_") if
                                   (lambda s: int(s.split("_")[1].split("x")[0]) >= int(s.split("x")[1]))(g)])
 def test_bidiag_par_dropin_vs_reference(lib, cuda, name):
     g = golden(name)
-    A_r, al, be = lib.bidiag_par(g["A"])
-    scale = np.abs(g["A"]).max() * max(g["A"].shape)
-    assert np.max(np.abs(al - g["alpha"])) <= 1e-5 * scale
-    assert np.max(np.abs(be - g["beta"])) <= 1e-5 * scale
+    A = g["A"]
+    m, n = A.shape
+    A_r, al, be = lib.bidiag_par(A)
+    scale = np.linalg.norm(A, 2)
+    tol = 1e-5 * np.sqrt(n) * scale
+    assert np.max(np.abs(al - g["alpha"])) <= tol
+    if n > 1:
+        assert np.max(np.abs(be - g["beta"])) <= tol
+    # the exported reflectors (reference storage) reproduce A = Q B P^T
+    Q, P = _reflector_factors(A_r, m, n)
+    B = np.zeros((m, n))
+    B[np.arange(n), np.arange(n)] = al
+    if n > 1:
+        B[np.arange(n - 1), np.arange(1, n)] = be
+    assert np.linalg.norm(A - Q @ B @ P.T) <= 1e-5 * np.linalg.norm(A)
+    assert np.linalg.norm(Q.T @ Q - np.eye(m)) <= 1e-5 * np.sqrt(m)
+    # and agree with the reference's FP64 reflectors to FP32 conditioning
     ok = np.isfinite(g["A_refl"])
-    assert np.max(np.abs(A_r[ok] - g["A_refl"][ok])) <= 1e-4
+    assert np.max(np.abs(A_r[ok] - g["A_refl"][ok])) <= 5e-3
 
 
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 7, 64, 300, 1000])
