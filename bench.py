@@ -38,7 +38,7 @@ for p in (ROOT, os.path.join(ROOT, "ddc-svd_gb300")):
 
 M = N = 4096
 SEED = 1
-METRIC = "4096^2 full-SVD ms (graded cond 1e6, FP32)"
+METRIC = "4096^2 full-SVD ms (graded cond 1e6, FP32)"  # names the default --size
 
 
 def graded_matrix(torch, n, seed, device):
@@ -303,8 +303,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--quick", action="store_true", help="skip the secondary mode timings")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline mode only; skip the secondary modes, batched and adjoint sections")
+    ap.add_argument("--size", type=int, default=4096, help="matrix order (profiling of smaller cases)")
     args = ap.parse_args()
+    global M, N
+    M = N = args.size
     if args.impl == "reference":
         run_reference(args)
         return
@@ -322,6 +326,7 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     A64, s_true = graded_matrix(torch, N, SEED + rank, dev)
+    workload = f"svd_graded_{M}x{N}"
     A32 = A64.float()
     A64r = A32.double()
     Ac = A32.t().contiguous()  # column-major buffer
@@ -434,7 +439,7 @@ def main():
         "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP64 sigma/vector stages)", "data": "synthetic",
-        "config": {"workload": "svd_graded_4096x4096", "m": M, "n": N, "cond": 1e6, "mode": head,
+        "config": {"workload": workload, "m": M, "n": N, "cond": 1e6, "mode": head,
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}"},
         "modes_ms": mode_ms, "modes": info,
         "gflops": round(svd_flops(M, N) / (ms * 1e-3) / 1e9, 1),

@@ -623,6 +623,32 @@ int ddcsvd_bdvec_device(ddcsvd_handle_t h, int N, const double* dA, const double
   return rc;
 }
 
+int ddcsvd_gemm_f32_device(ddcsvd_handle_t h, int mode, int M, int N, int K, const float* A, int lda,
+                           const float* B, int ldb, float* C, int ldc, float alpha, float beta) {
+  if (!h || M < 0 || N < 0 || K < 0 || !A || !B || !C || lda < K || ldb < K || ldc < M) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  t_last_error.clear();
+  if (mode != DDCSVD_MODE_BLOCKED_FP32 && mode != DDCSVD_MODE_BLOCKED_TF32X3 && mode != DDCSVD_MODE_BLOCKED_TF32X6)
+    return DDCSVD_ERR_ARG;
+  if (mode != DDCSVD_MODE_BLOCKED_FP32 && !tc_available(h)) return DDCSVD_ERR_UNSUPPORTED;
+  const GemmKind kind = kind_of(mode);
+  const size_t sb = gemm_scratch_bytes(kind, M, N, K);
+  DDC_TRY(ensure_workspace(h, sb + 4096));
+  Arena sc;
+  sc.base = (char*)h->ws;
+  sc.plan = false;
+  sc.cap = sb;
+  DDC_TRY(reset_status(h));
+  Mat none{nullptr, 0, 0};
+  if (kind == GEMM_SIMT) {
+    DDC_TRY(gemm(h, kind, M, N, K, Mat{A, lda, 1}, Mat{B, 1, ldb}, 0, none, none, alpha, beta, C, ldc, &sc));
+  } else {
+    DDC_TRY(gemm_tc_kmajor(h, kind, M, N, K, A, lda, 0, B, ldb, 0, C, ldc, alpha, beta, &sc));
+  }
+  return check_status(h, "gemm");
+}
+
 // ---------------------------------------------------------------- host-buffer API
 static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda, float* S, float* U, int ldu,
                         float* V, int ldv, int mode) {

@@ -14,14 +14,19 @@
 //
 // One CTA computes a 128 x BN tile (BN = 128 or 64), 6 warps:
 //   warp 0      TMA producer: raw FP32 K-slabs (32 wide, 128-byte swizzle)
-//               of A and B into a 3-stage shared-memory ring;
-//   warps 2-5   split each landed slab in place into hi (overwriting the raw
-//               copy) and lo (second buffer), then release it to the MMA;
+//               of A and B into a shared-memory ring (3 stages for two
+//               parts, 2 for three);
+//   warps 2-5   split each landed slab in place into its TF32 parts (part 0
+//               overwrites the raw copy), then release it to the MMA;
 //   warp 1      TMEM allocation and the single MMA-issuing thread:
-//               tcgen05.mma.kind::tf32 over 4 K-steps x 3 products per slab,
-//               tcgen05.commit frees the stage;
-//   warps 2-5   epilogue: tcgen05.ld of the accumulator (lane = row), scaled
-//               update of C (coalesced along columns of col-major C).
+//               tcgen05.mma.kind::tf32 over 4 K-steps x (3 or 6) products
+//               per slab into one of two TMEM slab accumulators (fresh per
+//               slab); tcgen05.commit frees the stage and the accumulator;
+//   warps 2-5   drain each slab accumulator with tcgen05.ld (lane = row)
+//               into FP32 registers with round-to-nearest adds -- the tensor
+//               core's own accumulation over many MMAs loses ~2-3 bits
+//               against FP32 FMA chains -- and finally update C (coalesced
+//               along columns of col-major C).
 // Split-K over blockIdx.z writes FP32 partials that a second kernel reduces
 // in a fixed order (deterministic).
 //
@@ -183,8 +188,8 @@ struct Layout {
   static constexpr int B_BYTES = BN * BK * 4;
   static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
   static constexpr int STAGES = (NP == 2) ? 3 : 2;
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
-  static constexpr int TMEM_COLS = BN < 32 ? 32 : BN;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;  // + alignment and barriers
+  static constexpr int TMEM_COLS = 2 * BN;  // two slab accumulators
 };
 
 template <int BN, int NP>
@@ -199,8 +204,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* full = bars;
   uint64_t* conv = bars + STAGES;
   uint64_t* empty = bars + 2 * STAGES;
-  uint64_t* accum = bars + 3 * STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * STAGES + 1);
+  uint64_t* accf = bars + 3 * STAGES;      // [2] slab accumulator ready
+  uint64_t* acce = bars + 3 * STAGES + 2;  // [2] slab accumulator drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -210,7 +216,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&conv[s], 128);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 128);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -232,8 +241,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   // stage layout: A parts 0..NP-1, then B parts 0..NP-1 (part 0 = raw -> hi)
   auto a_part = [&](int s, int k) { return smem + s * L::STAGE + k * L::A_BYTES; };
   auto b_part = [&](int s, int k) { return smem + s * L::STAGE + NP * L::A_BYTES + k * L::B_BYTES; };
-  auto a_hi = [&](int s) { return a_part(s, 0); };
-  auto b_hi = [&](int s) { return b_part(s, 0); };
 
   if (warp == 0) {
     if (lane == 0) {
@@ -243,8 +250,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1, abort_flag, p.st, 901)) break;
         mbar_arrive_expect_tx(&full[s], L::A_BYTES + L::B_BYTES);
         const int sl = s_begin + i;
-        tma_load_2d(a_hi(s), &tmA, p.a_koff + sl * BK, m0, &full[s]);
-        tma_load_2d(b_hi(s), &tmB, p.b_koff + sl * BK, n0, &full[s]);
+        tma_load_2d(a_part(s, 0), &tmA, p.a_koff + sl * BK, m0, &full[s]);
+        tma_load_2d(b_part(s, 0), &tmB, p.b_koff + sl * BK, n0, &full[s]);
         issued = i + 1;
       }
       // make sure no copy of ours is still landing before the CTA may exit
@@ -259,9 +266,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BM, BN);
       for (int i = 0; i < nsl; i++) {
-        const int s = i % STAGES;
+        const int s = i % STAGES, b = i & 1;
         if (!mbar_wait(&conv[s], (i / STAGES) & 1, abort_flag, p.st, 902)) break;
+        if (i >= 2 && !mbar_wait(&acce[b], ((i >> 1) - 1) & 1, abort_flag, p.st, 905)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(b * BN);
 #pragma unroll
         for (int kk = 0; kk < BK / 8; kk++) {
           const uint32_t off = kk * 32;  // 8 TF32 elements = 32 bytes along K
@@ -271,56 +280,81 @@ __global__ void __launch_bounds__(THREADS, 1)
             da[k] = smem_desc_sw128(smem_u32(a_part(s, k)) + off);
             db[k] = smem_desc_sw128(smem_u32(b_part(s, k)) + off);
           }
-          const uint32_t first = (i > 0 || kk > 0) ? 1u : 0u;
+          const uint32_t first = (kk > 0) ? 1u : 0u;  // each slab starts a fresh partial sum
           if (NP == 3) {  // l*h, h*l, m*m, m*h, h*m, h*h
-            mma_tf32(tmem, da[2], db[0], idesc, first);
-            mma_tf32(tmem, da[0], db[2], idesc, 1u);
-            mma_tf32(tmem, da[1], db[1], idesc, 1u);
-            mma_tf32(tmem, da[1], db[0], idesc, 1u);
-            mma_tf32(tmem, da[0], db[1], idesc, 1u);
-            mma_tf32(tmem, da[0], db[0], idesc, 1u);
+            mma_tf32(d, da[2], db[0], idesc, first);
+            mma_tf32(d, da[0], db[2], idesc, 1u);
+            mma_tf32(d, da[1], db[1], idesc, 1u);
+            mma_tf32(d, da[1], db[0], idesc, 1u);
+            mma_tf32(d, da[0], db[1], idesc, 1u);
+            mma_tf32(d, da[0], db[0], idesc, 1u);
           } else {  // l*h, h*l, h*h
-            mma_tf32(tmem, da[1], db[0], idesc, first);
-            mma_tf32(tmem, da[0], db[1], idesc, 1u);
-            mma_tf32(tmem, da[0], db[0], idesc, 1u);
+            mma_tf32(d, da[1], db[0], idesc, first);
+            mma_tf32(d, da[0], db[1], idesc, 1u);
+            mma_tf32(d, da[0], db[0], idesc, 1u);
           }
         }
         mma_commit(&empty[s]);
+        mma_commit(&accf[b]);
       }
-      mma_commit(accum);
     }
   } else {
+    // warps 2-5: split landed slabs; drain each slab's partial sum from TMEM
+    // into round-to-nearest FP32 registers (the tensor core's own accumulation
+    // across many MMAs is less accurate than FP32 FMA chains)
     const int ct = threadIdx.x - 64;
-    for (int i = 0; i < nsl; i++) {
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+    float acc[BN];
+#pragma unroll
+    for (int c = 0; c < BN; c++) acc[c] = 0.f;
+    bool ok = true;
+    auto drain = [&](int j) {
+      const int b = j & 1;
+      if (!mbar_wait(&accf[b], (j >> 1) & 1, abort_flag, p.st, 904)) {
+        ok = false;
+        return;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t r[16];
+        tmem_ld16(tmem + lane_base + (uint32_t)(b * BN + c0), r);
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) acc[c0 + jj] += __uint_as_float(r[jj]);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(&acce[b]);
+    };
+    for (int i = 0; i < nsl && ok; i++) {
       const int s = i % STAGES;
-      if (!mbar_wait(&full[s], (i / STAGES) & 1, abort_flag, p.st, 903)) break;
+      if (!mbar_wait(&full[s], (i / STAGES) & 1, abort_flag, p.st, 903)) {
+        ok = false;
+        break;
+      }
       split_tile<NP>(reinterpret_cast<float4*>(a_part(s, 0)), reinterpret_cast<float4*>(a_part(s, 1)),
                      reinterpret_cast<float4*>(a_part(s, NP - 1)), L::A_BYTES / 16, ct, 128);
       split_tile<NP>(reinterpret_cast<float4*>(b_part(s, 0)), reinterpret_cast<float4*>(b_part(s, 1)),
                      reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, 128);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&conv[s]);
+      if (i >= 1) drain(i - 1);
     }
-    // ---------------- epilogue: TMEM -> C
-    const bool ok = mbar_wait(accum, 0, abort_flag, p.st, 904) && !*abort_flag && nsl > 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    if (ok && nsl >= 1) drain(nsl - 1);
+    // ---------------- epilogue: registers -> C
+    ok = ok && !*abort_flag && nsl > 0;
     const int row = m0 + q * 32 + lane;
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t r[16];
-      tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
-      if (!ok || row >= p.M) continue;
+    if (ok && row < p.M) {
 #pragma unroll
-      for (int jj = 0; jj < 16; jj++) {
-        const int col = n0 + c0 + jj;
-        if (col >= p.N) break;
-        const float v = __uint_as_float(r[jj]);
-        if (p.partial) {
-          p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = v;
-        } else {
-          float* cp = p.C + row + (size_t)col * p.ldc;
-          *cp = (p.beta == 0.f ? 0.f : p.beta * *cp) + p.alpha * v;
+      for (int c = 0; c < BN; c++) {
+        const int col = n0 + c;
+        if (col < p.N) {
+          if (p.partial) {
+            p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = acc[c];
+          } else {
+            float* cp = p.C + row + (size_t)col * p.ldc;
+            *cp = (p.beta == 0.f ? 0.f : p.beta * *cp) + p.alpha * acc[c];
+          }
         }
       }
     }

@@ -309,6 +309,19 @@ def svd_batched_device(mats, handle: Handle | None = None):
     return out
 
 
+def gemm_nt_device(A, B, mode="tf32x6", C=None, alpha=1.0, beta=0.0, handle: Handle | None = None):
+    """C = beta*C + alpha * A @ B.T on the library's GEMM back ends (float32 CUDA tensors,
+    A (M, K) and B (N, K) row-major).  Returns C as an (M, N) tensor."""
+    import torch
+    h = _handle(handle)
+    M, K = A.shape
+    N = B.shape[0]
+    Ct = torch.zeros((N, M), dtype=torch.float32, device=A.device) if C is None else C.t().contiguous()
+    check(load().ddcsvd_gemm_f32_device(h.ptr, _mode(mode), M, N, K, A.contiguous().data_ptr(), K,
+                                        B.contiguous().data_ptr(), K, Ct.data_ptr(), M, alpha, beta), "gemm")
+    return Ct.t()
+
+
 def svd_backward_device(U, S, V, gU, gS, gV, handle: Handle | None = None):
     """Adjoint of the thin SVD for a batch: U (B, m, k), S (B, k), V (B, n, k) -> gA (B, m, n)."""
     import torch

@@ -36,6 +36,8 @@ _SIGS = {
     "ddcsvd_svd_batched_f32_device": (c_int, [P, c_int, P, P, P, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f64_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f32_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
+    "ddcsvd_gemm_f32_device": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, c_int, P, c_int, c_float,
+                                       c_float]),
     "ddcsvd_status_string": (ctypes.c_char_p, [c_int]),
     "ddcsvd_last_error": (ctypes.c_char_p, []),
     "ddcsvd_kernel_launch_count": (c_ll, []),

@@ -154,6 +154,17 @@ int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t handle, int batch, int m, int
                                    const float *dU, const float *dS, const float *dV,
                                    const float *gU, const float *gS, const float *gV, float *gA);
 
+/* ---------------------------------------------------------------- GEMM back ends */
+
+/* The GEMM back ends of the pipeline, exposed for validation and reuse:
+ * C (M x N, column-major, ldc) = beta*C + alpha * A B^T, with A (M x K) and
+ * B (N x K) row-major (K contiguous; row r of A at A + r*lda), FP32 device
+ * pointers.  mode: DDCSVD_MODE_BLOCKED_FP32 (CUDA cores), _BLOCKED_TF32X3 or
+ * _BLOCKED_TF32X6 (tcgen05 tensor cores; lda, ldb multiples of 4 and 16-byte
+ * aligned A, B). */
+int ddcsvd_gemm_f32_device(ddcsvd_handle_t handle, int mode, int M, int N, int K, const float *A, int lda,
+                           const float *B, int ldb, float *C, int ldc, float alpha, float beta);
+
 /* ---------------------------------------------------------------- diagnostics */
 
 const char *ddcsvd_status_string(int status);

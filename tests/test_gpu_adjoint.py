@@ -104,7 +104,7 @@ def test_autograd_function_end_to_end(lib, cuda):
     g = torch.tensor(rng.standard_normal(128), dtype=torch.float32, device="cuda")
 
     def f(U, S, V):  # sign-invariant: sum_j w_j s_j + (g^T u_j)^2
-        return (S * w).sum() + ((g @ U) ** 2).sum()
+        return (S * w.to(S.dtype)).sum() + ((g.to(U.dtype) @ U) ** 2).sum()
 
     A1 = A.clone().requires_grad_(True)
     U, S, V = ddc_svd(A1)

@@ -1,0 +1,38 @@
+"""GEMM back ends (CUDA-core FP32, tcgen05 split TF32) against FP64 products."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("K", [8, 64, 512, 4096])
+def test_gemm_backends_accuracy(lib, cuda, K):
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(K)
+    M, N = 256, 192
+    A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
+    B = torch.rand((N, K), device="cuda", generator=g) * 2 - 1
+    ref = A.double() @ B.double().T
+    errs = {}
+    for mode in ("blocked", "tf32x3", "tf32x6"):
+        C = lib.gemm_nt_device(A, B, mode=mode)
+        errs[mode] = float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref))
+    print(f"K={K} rel err", {k: f"{v:.2e}" for k, v in errs.items()})
+    # FP32-level: within a small factor of the CUDA-core FMA result
+    assert errs["blocked"] <= 2e-6
+    assert errs["tf32x6"] <= max(3 * errs["blocked"], 2e-7)
+    assert errs["tf32x3"] <= 5e-6
+
+
+def test_gemm_update_form(lib, cuda):
+    """C = beta C + alpha A B^T with a nonzero C, ragged sizes (TMA zero fill)."""
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(1)
+    M, N, K = 300, 130, 72  # K not a multiple of 32 (TMA zero fill); rows stay 16-byte aligned
+    A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
+    B = torch.rand((N, K), device="cuda", generator=g) * 2 - 1
+    C0 = torch.rand((M, N), device="cuda", generator=g) * 2 - 1
+    ref = 0.5 * C0.double() - 1.0 * (A.double() @ B.double().T)
+    for mode in ("blocked", "tf32x6"):
+        C = lib.gemm_nt_device(A, B, mode=mode, C=C0.clone(), alpha=-1.0, beta=0.5)
+        assert float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref)) <= 2e-5
