@@ -141,9 +141,103 @@ static int svd_backward(ddcsvd_context* h, int batch, int m, int n, const T* U, 
   return check_status(h, "svd_backward");
 }
 
+// ---------------------------------------------------------------- allocation-free variant
+// Some callers cannot allocate device memory at the moment they need the
+// adjoint: code running inside another framework's memory pool or a
+// pre-planned fixed memory budget, a real-time loop that must not reach the
+// driver's allocator (cudaMalloc can synchronise the device and fail under
+// fragmentation), or a context in which only caller-owned buffers may be
+// touched.  For them the FP64 adjoint has a variant whose intermediates live
+// in a fixed-size array compiled into this library instead of the handle's
+// workspace; it needs no handle either.
+constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB, held by every GPU that loads the library
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[128];  // device address of g_noalloc_scratch, per device
+
+// The array's host-side name is only a stand-in: its device address is looked
+// up once per device, with that device current.
+static int noalloc_scratch_address(int dev, char** out) {
+  if (dev < 0 || dev >= 128) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_last_error("cudaGetSymbolAddress of the adjoint scratch failed: %s", cudaGetErrorString(e));
+      return DDCSVD_ERR_CUDA;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = static_cast<char*>(g_noalloc_addr[dev]);
+  return DDCSVD_OK;
+}
+
+static int svd_backward_f64_noalloc(cudaStream_t stream, int batch, int m, int n, const double* U, const double* S,
+                                    const double* V, const double* gU, const double* gS, const double* gV,
+                                    double* gA) {
+  if (batch <= 0 || m <= 0 || n <= 0 || m < n || !U || !S || !V || !gA) return DDCSVD_ERR_ARG;
+  const int k = n;
+  // scratch layout: status word, J, K, M (k x k each), P (m x k), per problem
+  const size_t kk = (size_t)k * k * batch, mk = (size_t)m * k * batch;
+  Arena plan;
+  plan.take<DevStatus>(1);
+  plan.take<double>(kk);
+  plan.take<double>(kk);
+  plan.take<double>(kk);
+  plan.take<double>(mk);
+  if (plan.off > kNoAllocScratchBytes) {
+    set_last_error("allocation-free adjoint needs %zu bytes of scratch; its fixed limit is %zu bytes "
+                   "(batch * (3 n^2 + m n) * 8 plus 256): split the batch",
+                   plan.off, kNoAllocScratchBytes);
+    return DDCSVD_ERR_ARG;
+  }
+  int dev = 0;
+  DDC_CUDA_TRY(cudaGetDevice(&dev));
+  char* base = nullptr;
+  DDC_TRY(noalloc_scratch_address(dev, &base));
+  Arena a;
+  a.plan = false;
+  a.base = base;
+  DevStatus* st = a.take<DevStatus>(1);
+  double* J = a.take<double>(kk);
+  double* Kv = a.take<double>(kk);
+  double* Mm = a.take<double>(kk);
+  double* P = a.take<double>(mk);
+  ddcsvd_context ctx;  // stream only: nothing here allocates
+  ctx.device = dev;
+  ctx.stream = stream;
+  ctx.d_status = st;
+  // the array keeps the previous call's contents: the status word must start at zero
+  // (J, K, M and P are fully overwritten before they are read)
+  DDC_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevStatus), stream));
+  const long long sU = (long long)m * k, sV = (long long)n * k, sK = (long long)k * k;
+  if (gU) DDC_TRY(bgemm<double>(&ctx, batch, k, k, m, U, m, 1, sU, gU, 1, m, sU, J, k, sK, 1.0, 0.0));
+  if (gV) DDC_TRY(bgemm<double>(&ctx, batch, k, k, n, V, n, 1, sV, gV, 1, n, sV, Kv, k, sK, 1.0, 0.0));
+  dim3 g2(std::max(1, std::min(64, ceil_div(std::max(k * k, m * k), 256))), batch);
+  adjoint_core_kernel<double><<<g2, 256, 0, stream>>>(k, m, gU ? J : nullptr, gV ? Kv : nullptr, S, gS, gU, Mm, P);
+  count_launch();
+  DDC_TRY(bgemm<double>(&ctx, batch, m, k, k, U, 1, m, sU, Mm, 1, k, sK, P, m, sU, 1.0, 1.0));
+  DDC_TRY(bgemm<double>(&ctx, batch, m, n, k, P, 1, m, sU, V, n, 1, sV, gA, m, (long long)m * n, 1.0, 0.0));
+  DevStatus hs{0, 0};
+  DDC_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+  DDC_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (hs.code != 0) {
+    set_last_error("svd_backward_noalloc: device status %d", hs.code);
+    return hs.code;
+  }
+  return DDCSVD_OK;
+}
+
 }  // namespace ddcsvd
 
 using namespace ddcsvd;
+
+extern "C" int ddcsvd_svd_backward_f64_noalloc(void* stream, int batch, int m, int n, const double* dU,
+                                               const double* dS, const double* dV, const double* gU,
+                                               const double* gS, const double* gV, double* gA) {
+  return svd_backward_f64_noalloc(static_cast<cudaStream_t>(stream), batch, m, n, dU, dS, dV, gU, gS, gV, gA);
+}
 
 extern "C" int ddcsvd_svd_backward_f64_device(ddcsvd_handle_t h, int batch, int m, int n, const double* dU,
                                               const double* dS, const double* dV, const double* gU,

@@ -36,6 +36,7 @@ _SIGS = {
     "ddcsvd_svd_batched_f32_device": (c_int, [P, c_int, P, P, P, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f64_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f32_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
+    "ddcsvd_svd_backward_f64_noalloc": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
     "ddcsvd_gemm_f32_device": (c_int, [P, c_int, c_int, c_int, c_int, P, c_int, P, c_int, P, c_int, c_float,
                                        c_float]),
     "ddcsvd_status_string": (ctypes.c_char_p, [c_int]),

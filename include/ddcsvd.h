@@ -154,6 +154,26 @@ int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t handle, int batch, int m, int
                                    const float *dU, const float *dS, const float *dV,
                                    const float *gU, const float *gS, const float *gV, float *gA);
 
+/* No counterpart in the reference.  The FP64 adjoint above for callers that
+ * must not allocate device memory when they call it -- code working inside
+ * another framework's memory pool or a fixed, pre-planned memory budget, or a
+ * latency-critical loop that must stay away from the driver's allocator.  It
+ * takes no handle and calls no cudaMalloc / cudaFree / allocating library
+ * routine: its intermediates live in a 16 MiB array compiled into this
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Inputs and outputs are caller-owned device buffers (same layout as
+ * ddcsvd_svd_backward_f64_device); work goes to `stream` (a cudaStream_t,
+ * NULL = legacy default stream) and the call returns after a stream
+ * synchronisation.  Limit: batch * (3 n^2 + m n) * 8 + 256 bytes must not
+ * exceed 16 MiB, else DDCSVD_ERR_ARG (split the batch).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the one array:
+ * calls whose GPU work overlaps (concurrent streams or threads) race and must
+ * be serialised by the caller. */
+int ddcsvd_svd_backward_f64_noalloc(void *stream, int batch, int m, int n, const double *dU,
+                                    const double *dS, const double *dV, const double *gU,
+                                    const double *gS, const double *gV, double *gA);
+
 /* ---------------------------------------------------------------- GEMM back ends */
 
 /* The GEMM back ends of the pipeline, exposed for validation and reuse:
