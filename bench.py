@@ -224,6 +224,11 @@ def bench_batched(torch, lib, h, steps, flush):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     ms = float(np.mean(ts))
+    h.stage_timing(True)
+    plan.run()
+    torch.cuda.synchronize()
+    kms, kn = h.kernel_times(5)
+    h.stage_timing(False)
     # the single-matrix path looped over the first 128 problems (same inputs)
     sub = [torch.from_numpy(a).cuda() for a in mats[:128]]
     torch.cuda.synchronize()
@@ -239,7 +244,9 @@ def bench_batched(torch, lib, h, steps, flush):
     return {"svds_per_s": round(len(mats) / (ms * 1e-3), 1), "ms": round(ms, 3), "count": len(mats),
             "loop_single_svds_per_s": round(1e3 / loop_ms, 1), "compulsory_bytes": comp, "elements": mn,
             "hbm_frac": round(comp / (ms * 1e-3) / 1e9 / hbm, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
-            "worst_resid": float(f"{worst:.3e}")}
+            "worst_resid": float(f"{worst:.3e}"),
+            "kernel_ms": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform"],
+                                  [round(x, 3) for x in kms]))}
 
 
 def bench_adjoint(torch, lib, h, steps):

@@ -40,18 +40,23 @@ __global__ void pack_reflectors_kernel(int side, int rows, int bs, int j0, int s
 
 // T (bs x bs, col-major) from the Gram matrix G = U^T U:
 //   T[l,l] = tau_l,  T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l].
-__global__ void wy_tfactor_kernel(int bs, int j0, const float* __restrict__ tau, const float* G,
+__global__ void wy_tfactor_kernel(int bs, int j0, const float* __restrict__ tau, const float* __restrict__ G,
                                   float* T) {
   __shared__ float sT[kWY][kWY + 1];
+  __shared__ float sG[kWY][kWY + 1];
   __shared__ float col[kWY];
   const int t = threadIdx.x;
-  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) sT[idx % kWY][idx / kWY] = 0.f;
+  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) {
+    const int r = idx % kWY, c = idx / kWY;
+    sT[r][c] = 0.f;
+    sG[r][c] = (r < bs && c < bs) ? G[r + (size_t)c * bs] : 0.f;
+  }
   __syncthreads();
   for (int l = 0; l < bs; l++) {
     const float tl = tau[j0 + l];
     if (t < l) {
       float s = 0.f;
-      for (int k = t; k < l; k++) s += sT[t][k] * G[k + (size_t)l * bs];
+      for (int k = t; k < l; k++) s += sT[t][k] * sG[k][l];
       col[t] = -tl * s;
     }
     __syncthreads();

@@ -342,6 +342,7 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   memcpy(pin, tasks.data(), sizeof(BatchTask) * batch);
   memcpy(pin + sizeof(BatchTask) * batch, order.data(), sizeof(int) * batch);
   DDC_TRY(reset_status(h));
+  h->kused = 0;
   DDC_CUDA_TRY(cudaMemcpyAsync(dt, pin, sizeof(BatchTask) * batch, cudaMemcpyHostToDevice, h->stream));
   DDC_CUDA_TRY(cudaMemcpyAsync(dord, pin + sizeof(BatchTask) * batch, sizeof(int) * batch, cudaMemcpyHostToDevice,
                                h->stream));
@@ -398,5 +399,7 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   batch_sigma_out_kernel<<<std::min(batch, 1024), 128, 0, h->stream>>>(dt, batch, sig, dSigma);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
-  return check_status(h, "svd_batched");
+  const int rc = check_status(h, "svd_batched");
+  if (h->timing && rc == DDCSVD_OK) ktimer_collect(h);
+  return rc;
 }

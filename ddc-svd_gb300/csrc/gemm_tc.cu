@@ -346,14 +346,25 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int row = m0 + q * 32 + lane;
     if (ok && row < p.M) {
 #pragma unroll
-      for (int c = 0; c < BN; c++) {
-        const int col = n0 + c;
-        if (col < p.N) {
-          if (p.partial) {
-            p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = acc[c];
-          } else {
-            float* cp = p.C + row + (size_t)col * p.ldc;
-            *cp = (p.beta == 0.f ? 0.f : p.beta * *cp) + p.alpha * acc[c];
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        if (p.partial) {
+#pragma unroll
+          for (int jj = 0; jj < 16; jj++) {
+            const int col = n0 + c0 + jj;
+            if (col < p.N) p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = acc[c0 + jj];
+          }
+        } else {
+          // 16 independent loads of C in flight, then the 16 updates
+          float old[16];
+#pragma unroll
+          for (int jj = 0; jj < 16; jj++) {
+            const int col = n0 + c0 + jj;
+            old[jj] = (p.beta != 0.f && col < p.N) ? p.C[row + (size_t)col * p.ldc] : 0.f;
+          }
+#pragma unroll
+          for (int jj = 0; jj < 16; jj++) {
+            const int col = n0 + c0 + jj;
+            if (col < p.N) p.C[row + (size_t)col * p.ldc] = p.beta * old[jj] + p.alpha * acc[c0 + jj];
           }
         }
       }

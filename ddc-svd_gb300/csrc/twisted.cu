@@ -13,10 +13,11 @@
 // the reference.  Left vectors: y = B x normalised (the reference divides by
 // sigma, :548, which fails for sigma = 0).
 //
-// GB300 mapping: each thread owns one sigma_k; a CTA of two warps handles 32
-// vectors, warp 0 running the top-down (stationary) transform while warp 1
-// runs the bottom-up (progressive) transform of the same 32 shifts, so the
-// two sequential FP64 recurrences overlap.  Per-step arrays are stored
+// GB300 mapping: each lane owns one sigma_k; a CTA of four warps handles 32
+// vectors: warp 0 runs the top-down (stationary) transform while warp 1 runs
+// the bottom-up (progressive) transform of the same 32 shifts, then all four
+// warps split the twist search and the norm passes by index segment and two
+// of them solve the two halves of the twisted system concurrently.  Per-step arrays are stored
 // interleaved by vector (element i of vector k at [i * N + k]) so every
 // access of a warp is one contiguous 256-byte segment.
 #include <vector>
@@ -62,7 +63,18 @@ struct TwParams {
   const double *a, *b;
 };
 
-__global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
+constexpr int kTwWarps = 4;
+
+// 32 vectors per CTA, one per lane; kTwWarps warps share the work of each
+// vector: the stationary and progressive transforms run concurrently (warps
+// 0 and 1), the twist search and ||B z|| are split over index segments
+// (warp w takes segment w), and the two halves of the solve run concurrently
+// (warp 0 below the twist, warp 1 above).
+__global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
+  __shared__ double s_val[kTwWarps][32];
+  __shared__ int s_idx[kTwWarps][32];
+  __shared__ double s_nrm[2][32];
+  __shared__ int s_r[32];
   const int N = p.N;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
@@ -70,6 +82,7 @@ __global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
   const int lo = act ? p.L.blo[k] : 0, hi = act ? p.L.bhi[k] : 0;
   const int nb = hi - lo;
   const long long base = act ? p.L.base[k] + (k - lo) : 0;  // element i at base + (i - lo) * nb
+  auto at = [&](int i) { return base + (long long)(i - lo) * nb; };
   const double lam = act ? p.sigma[k] * p.sigma[k] : 0.0;
   const double tiny = DBL_MIN / DBL_EPSILON;
   if (w == 0) {
@@ -79,62 +92,91 @@ __global__ void __launch_bounds__(64) twisted_kernel(TwParams p) {
       double dp = p.dd[i] + s;
       if (fabs(dp) < tiny) dp = -tiny;
       const double L = p.dl[i] / dp;
-      const long long e = base + (long long)(i - lo) * nb;
-      p.Lp[e] = L;
-      p.S[e] = s;
+      p.Lp[at(i)] = L;
+      p.S[at(i)] = s;
       s = L * p.ll[i] * s - lam;
     }
-    if (hi > lo) p.S[base + (long long)(hi - 1 - lo) * nb] = s;
-  } else if (hi > lo) {
+    if (hi > lo) p.S[at(hi - 1)] = s;
+  } else if (w == 1 && hi > lo) {
     // progressive qd on the block: L D L^T - lam = U- D- U-^T, p_{hi-1} = d_{hi-1} - lam
     double pv = p.dd[hi - 1] - lam;
-    p.Pp[base + (long long)(hi - 1 - lo) * nb] = pv;
+    p.Pp[at(hi - 1)] = pv;
     for (int i = hi - 2; i >= lo; i--) {
       double dm = p.dll[i] + pv;
       if (fabs(dm) < tiny) dm = -tiny;
       const double tt = p.dd[i] / dm;
-      const long long e = base + (long long)(i - lo) * nb;
-      p.Um[e] = p.ll[i] * tt;
+      p.Um[at(i)] = p.ll[i] * tt;
       pv = pv * tt - lam;
-      p.Pp[e] = pv;
+      p.Pp[at(i)] = pv;
     }
   }
   __syncthreads();
-  if (w != 0 || !act) return;
-  auto at = [&](int i) { return base + (long long)(i - lo) * nb; };
-  // twist index r = argmin |gamma_i|, gamma_i = s_i + p_i + lam (ties: larger i)
-  int r = hi - 1;
-  double gbest = fabs(p.S[at(hi - 1)] + p.Pp[at(hi - 1)] + lam);
-  for (int i = hi - 2; i >= lo; i--) {
-    const double g = fabs(p.S[at(i)] + p.Pp[at(i)] + lam);
-    if (g < gbest) { gbest = g; r = i; }
+  // ---- twist index r = argmin |gamma_i|, gamma_i = s_i + p_i + lam; ties -> larger i
+  {
+    const int seg = (nb + kTwWarps - 1) / kTwWarps;
+    const int a = lo + w * seg, b = min(hi, a + seg);
+    double best = INFINITY;
+    int bi = -1;
+    for (int i = b - 1; i >= a; i--) {  // downward scan, strict <: keeps the larger index on ties
+      const double g = fabs(p.S[at(i)] + p.Pp[at(i)] + lam);
+      if (g < best) { best = g; bi = i; }
+    }
+    s_val[w][lane] = best;
+    s_idx[w][lane] = bi;
   }
-  // solve N_r z = gamma_r e_r with z_r = 1, outwards from r
-  double nrm = 1.0;
-  p.Z[at(r)] = 1.0;
-  double z = 1.0;
-  for (int i = r - 1; i >= lo; i--) {
-    z = -p.Lp[at(i)] * z;
-    p.Z[at(i)] = z;
-    nrm += z * z;
+  __syncthreads();
+  if (w == 0) {
+    double best = INFINITY;
+    int r = hi - 1;
+    for (int q = kTwWarps - 1; q >= 0; q--) {  // segments from the top: the same order as one downward scan
+      if (s_idx[q][lane] >= 0 && s_val[q][lane] < best) { best = s_val[q][lane]; r = s_idx[q][lane]; }
+    }
+    s_r[lane] = act ? r : 0;
   }
-  z = 1.0;
-  for (int i = r + 1; i < hi; i++) {
-    z = -p.Um[at(i - 1)] * z;
-    p.Z[at(i)] = z;
-    nrm += z * z;
+  __syncthreads();
+  const int r = s_r[lane];
+  // ---- solve N_r z = gamma_r e_r with z_r = 1, outwards from r (two directions in parallel)
+  if (act && w == 0) {
+    double z = 1.0, nrm = 1.0;
+    p.Z[at(r)] = 1.0;
+    for (int i = r - 1; i >= lo; i--) {
+      z = -p.Lp[at(i)] * z;
+      p.Z[at(i)] = z;
+      nrm += z * z;
+    }
+    s_nrm[0][lane] = nrm;
+  } else if (act && w == 1) {
+    double z = 1.0, nrm = 0.0;
+    for (int i = r + 1; i < hi; i++) {
+      z = -p.Um[at(i - 1)] * z;
+      p.Z[at(i)] = z;
+      nrm += z * z;
+    }
+    s_nrm[1][lane] = nrm;
   }
-  // ||B z||^2 for the left vector (b is zero at the block end)
-  double by = 0.0;
-  double zi = p.Z[at(lo)];
-  for (int i = lo; i < hi; i++) {
-    const double zn = (i + 1 < hi) ? p.Z[at(i + 1)] : 0.0;
-    const double y = p.a[i] * zi + ((i + 1 < hi) ? p.b[i] * zn : 0.0);
-    by += y * y;
-    zi = zn;
+  __syncthreads();
+  // ---- ||B z||^2 for the left vector, split by segment (b is zero at the block end)
+  {
+    double by = 0.0;
+    if (act) {
+      const int seg = (nb + kTwWarps - 1) / kTwWarps;
+      const int a = lo + w * seg, b = min(hi, a + seg);
+      for (int i = a; i < b; i++) {
+        const double zi = p.Z[at(i)];
+        const double zn = (i + 1 < hi) ? p.Z[at(i + 1)] : 0.0;
+        const double y = p.a[i] * zi + ((i + 1 < hi) ? p.b[i] * zn : 0.0);
+        by += y * y;
+      }
+    }
+    s_val[w][lane] = by;
   }
-  p.xinv[k] = 1.0 / sqrt(nrm);
-  p.yinv[k] = (by > 0.0) ? 1.0 / sqrt(by) : 0.0;
+  __syncthreads();
+  if (w == 0 && act) {
+    double by = 0.0;
+    for (int q = 0; q < kTwWarps; q++) by += s_val[q][lane];
+    p.xinv[k] = 1.0 / sqrt(s_nrm[0][lane] + s_nrm[1][lane]);
+    p.yinv[k] = (by > 0.0) ? 1.0 / sqrt(by) : 0.0;
+  }
 }
 
 // rank of sigma_k among the sigmas of its group (ascending, stable).
@@ -256,7 +298,7 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
   ktimer_begin(ctx, KC_VECTORS);
   tw_setup_kernel<<<1, 256, 0, ctx->stream>>>(N, a, b, dd, ll, dl, dll);
   count_launch();
-  twisted_kernel<<<ceil_div(N, 32), 64, 0, ctx->stream>>>(p);
+  twisted_kernel<<<ceil_div(N, 32), 32 * kTwWarps, 0, ctx->stream>>>(p);
   count_launch();
   tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, p.L, rank, sigma_sorted);
   count_launch();
