@@ -35,6 +35,12 @@ namespace ddcsvd {
 
 constexpr int kPS = 2 * kPanel + 4;  // floats per partial-sum record
 
+#ifdef DDCSVD_PHASE_TRACE
+__device__ unsigned long long g_phase_trace[128 * 16];
+#endif
+// phase marks of the panel kernel: CTA 7, column 5 of every panel, one row per panel
+#define PMARK(slot) DDC_MARK(blockIdx.x == 7 && j == 5, p.k0 / kPanel, slot)
+
 struct PanelParams {
   int m, n, k0, nb, ldw, ldn, P;
   int rc, cc;  // rows / columns per CTA
@@ -65,6 +71,28 @@ __device__ __forceinline__ void householder(float x0, double t2, float* alpha, f
   *alpha = (float)a;
   *tau = (float)((nrm + fabs((double)x0)) / nrm);
   *scale = (float)(1.0 / ((double)x0 - a));
+}
+
+// The same from a compensated (float-float) ||tail||^2, in FP32 only.  The
+// input matrix is scaled so that max|a| lies in [2^-40, 2^40] (or is left
+// alone when it already does), so x0^2 + t2 neither overflows nor loses
+// anything that matters against ||A||.  sqrt of the rounded pair and the two
+// quotients are correctly rounded FP32 operations: alpha is within one ulp
+// of the FP64 result.
+__device__ __forceinline__ void householder_ff(float x0, FF t2, float* alpha, float* tau, float* scale) {
+  const FF n2 = ff_add_sq(t2, x0);
+  const float nrm = sqrtf(__fadd_rn(n2.hi, n2.lo));
+  if (nrm == 0.f) {
+    *alpha = 0.f;
+    *tau = 0.f;
+    *scale = 0.f;
+    return;
+  }
+  const float ax = fabsf(x0);
+  const float sg = x0 < 0.f ? -1.f : 1.f;
+  *alpha = -sg * nrm;
+  *tau = (nrm + ax) / nrm;
+  *scale = sg / (ax + nrm);  // 1 / (x0 - alpha)
 }
 
 // sum_{r in [r0, r1)} col[r] * xs[r]; col in global (16B-aligned base), xs in
@@ -138,60 +166,85 @@ __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int
   }
   red[t] = acc;
   __syncthreads();
-  if (t < 4 * R4) {
-    const int qq = t >> 2, comp = t & 3;
-    float s = 0.f;
-    for (int gg = 0; gg < G; gg++) {
-      float4 v = red[gg * R4 + qq];
-      s += comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
+  // pairwise tree over the G column groups (log2 G steps; a serial sum over
+  // G = 512 groups of a 4-row block cost ~20 us per column)
+  int half = 1;
+  while (half < G) half <<= 1;
+  for (half >>= 1; half > 0; half >>= 1) {
+    if (g < half && g + half < G) {
+      const float4 o = red[t + half * R4];
+      float4 v = red[t];
+      v.x += o.x;
+      v.y += o.y;
+      v.z += o.z;
+      v.w += o.w;
+      red[t] = v;
     }
-    out[t] = s;
+    __syncthreads();
+  }
+  if (t < 4 * R4) {
+    const float4 v = red[t >> 2];
+    const int comp = t & 3;
+    out[t] = comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
   }
   __syncthreads();
 }
 
-// Ordered sum over the P per-CTA partial records of `cnt` floats (+ one FP64
-// norm): every thread of the CTA loads a share of the records into shared
-// memory, then thread q adds column q in CTA order (deterministic).
-__device__ __forceinline__ void reduce_partials(const float* __restrict__ part, const double* __restrict__ nrm,
-                                                int P, int cnt, float* stage, float* tot, double* dtot) {
-  const int t = threadIdx.x, nt = blockDim.x;
-  const int total = P * cnt;
-  // every thread issues up to 8 independent loads before storing any of them
-  for (int base = t; base < total; base += 8 * nt) {
-    float v[8];
+// Deterministic sum over the P per-CTA partial records of `cnt` floats plus
+// the compensated norm pair at [kPS - 2], [kPS - 1].  Warp w owns entries w,
+// w + nw, ... and lanes take records lane, lane + 32, ...: every load of a
+// warp is issued before the first add, so the reduction costs one L2 round
+// trip, and the fixed lane order and shuffle tree make the result independent
+// of timing.
+__device__ __forceinline__ void reduce_partials(const float* __restrict__ part, int P, int cnt, float* tot,
+                                                FF* ntot) {
+  constexpr int kE = 5, kB = 8;  // entries per warp and records per lane held in one pass
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float acc[kE];
+  FF nacc{0.f, 0.f};
 #pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int idx = base + u * nt;
-      v[u] = 0.f;
-      if (idx < total) {
-        const int b = idx / cnt;
-        v[u] = __ldcg(part + (size_t)b * kPS + (idx - b * cnt));
+  for (int e = 0; e < kE; e++) acc[e] = 0.f;
+  for (int b0 = 0; b0 < P; b0 += 32 * kB) {
+    float v[kE][kB];
+    float2 nv[kB];
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int b = b0 + lane + 32 * u;
+      nv[u] = (w == nw - 1 && b < P) ? __ldcg(reinterpret_cast<const float2*>(part + (size_t)b * kPS + kPS - 2))
+                                     : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int e = 0; e < kE; e++) {
+      const int q = w + e * nw;
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int b = b0 + lane + 32 * u;
+        v[e][u] = (q < cnt && b < P) ? __ldcg(part + (size_t)b * kPS + q) : 0.f;
       }
     }
 #pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int idx = base + u * nt;
-      if (idx < total) stage[idx] = v[u];
-    }
-  }
-  if (t >= 32 && t < 64) {  // one warp sums the FP64 norms
-    double v[8];
-    const int l = t - 32;
+    for (int u = 0; u < kB; u++) nacc = ff_add(nacc, FF{nv[u].x, nv[u].y});
 #pragma unroll
-    for (int u = 0; u < 8; u++) v[u] = (l + 32 * u < P) ? __ldcg(nrm + l + 32 * u) : 0.0;
-    double acc = 0.0;
+    for (int e = 0; e < kE; e++)
 #pragma unroll
-    for (int u = 0; u < 8; u++) acc += v[u];
-    for (int b = l + 256; b < P; b += 32) acc += __ldcg(nrm + b);
-    acc = warp_sum(acc);
-    if (t == 32) *dtot = acc;
+      for (int u = 0; u < kB; u++) acc[e] += v[e][u];
   }
-  __syncthreads();
-  if (t < cnt) {
-    float acc = 0.f;
-    for (int b = 0; b < P; b++) acc += stage[b * cnt + t];
-    tot[t] = acc;
+#pragma unroll
+  for (int e = 0; e < kE; e++) {
+    const int q = w + e * nw;
+    const float sum = warp_sum(acc[e]);
+    if (lane == 0 && q < cnt) tot[q] = sum;
+  }
+  // entries beyond kE * nw (only with fewer than 16 warps)
+  for (int q = w + kE * nw; q < cnt; q += nw) {
+    float a2 = 0.f;
+    for (int b = lane; b < P; b += 32) a2 += __ldcg(part + (size_t)b * kPS + q);
+    a2 = warp_sum(a2);
+    if (lane == 0) tot[q] = a2;
+  }
+  if (w == nw - 1) {
+    nacc = warp_sum_ff(nacc);
+    if (lane == 0) *ntot = nacc;
   }
   __syncthreads();
 }
@@ -219,11 +272,10 @@ struct PanelSmem {
   float* XS;      // rc x kLD: own rows of X
   float* YS;      // cc x kLD: own columns of Y
   float* VTS;     // cc x kLD: own columns of VT
-  float* stage;   // P * (2 kPanel + 2): partial records
   float* pre;     // max(rc, cc): prefetched original row/column entries
   float* misc;    // 8: prefetched scalars
   float *Yi, *VTi, *Wi, *Xi, *p1, *p2, *q1, *q2, *tot;
-  double* dred;   // 32
+  FF* nrm;        // reduced compensated norm
   float* scal;    // 8
 };
 
@@ -244,7 +296,6 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
   s.XS = p; p += rc * kLD;
   s.YS = p; p += cc * kLD;
   s.VTS = p; p += cc * kLD;
-  s.stage = p; p += P * (2 * kPanel + 2);
   s.pre = p; p += round_up(max(rc, cc) + 4, 4);
   s.misc = p; p += 8;
   s.Yi = p; p += kPanel + 4;
@@ -257,7 +308,7 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
   s.q2 = p; p += kPanel + 4;
   s.tot = p; p += kPS + 4;
   p = reinterpret_cast<float*>(round_up(reinterpret_cast<uintptr_t>(p), 16));
-  s.dred = reinterpret_cast<double*>(p);
+  s.nrm = reinterpret_cast<FF*>(p);
   p += 64;
   s.scal = p;
   return s;
@@ -266,7 +317,7 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
 size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P) {
   size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
              round_up(cc * 8 + 4, 4) + 2 * (size_t)rc * kLD + 2 * (size_t)cc * kLD +
-             (size_t)P * (2 * kPanel + 2) + round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
+             round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
              64 + 8;
   return f * sizeof(float) + 64;
 }
@@ -286,6 +337,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
 
   for (int j = 0; j < p.nb; j++) {
     const int i = k0 + j;
+    PMARK(0);
     // ---------------- S1: update column i on own rows, partial sums
     const int r_s = max(ra, i);
     const int nrow = max(0, rb - r_s);
@@ -311,16 +363,15 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     }
     __syncthreads();
     {
-      // partial sums over own rows r > i: [0] ||x||^2 (FP64), [1..j] Up^T x, [1+j..2j] X^T x
+      // partial sums over own rows r > i: [1..j] Up^T x, [1+j..2j] X^T x, and
+      // ||x||^2 as a compensated pair at [kPS-2, kPS-1]
       const int r1 = max(r_s, i + 1);
       if (wid == 0) {
-        double acc = 0.0;
-        for (int r = r1 + lane; r < rb; r += 32) {
-          double x = S.own[r - r_s];
-          acc += x * x;
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) p.colnrm[b] = acc;
+        FF acc{0.f, 0.f};
+        for (int r = r1 + lane; r < rb; r += 32) acc = ff_add_sq(acc, S.own[r - r_s]);
+        acc = warp_sum_ff(acc);
+        if (lane == 0)
+          *reinterpret_cast<float2*>(p.colpart + (size_t)b * kPS + kPS - 2) = make_float2(acc.hi, acc.lo);
       }
       if (t >= 32 && t < 32 + 2 * j) {
         const int q = t - 32;
@@ -330,7 +381,9 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         p.colpart[(size_t)b * kPS + 1 + q] = acc;
       }
     }
+    PMARK(1);
     if (!grid_sync(p.bar, p.P, p.st, 1)) return;
+    PMARK(2);
 
     // ---------------- S2: column reflector
     if (t < j) {
@@ -338,10 +391,10 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
     }
     if (t == 64) S.misc[0] = __ldcg(p.xcol + i);
-    reduce_partials(p.colpart, p.colnrm, p.P, 2 * j + 1, S.stage, S.tot, S.dred);
+    reduce_partials(p.colpart, p.P, 2 * j + 1, S.tot, S.nrm);
     if (t == 0) {
       float x0 = S.misc[0], alpha, tau, scale;
-      householder(x0, S.dred[0], &alpha, &tau, &scale);
+      householder_ff(x0, *S.nrm, &alpha, &tau, &scale);
       S.scal[0] = alpha;
       S.scal[1] = tau;
       S.scal[2] = scale;
@@ -363,6 +416,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       S.UpS[(r - ra) * kLD + j] = u;
     }
     if (i == n - 1) break;  // last column: no right reflector
+    PMARK(3);
     // ---------------- S3: y = A^T u on own columns, Y column j, row-i update
     {
       // stage the unscaled column and prefetch the original row i of own columns
@@ -371,6 +425,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       stage_vec(S.big, p.xcol, i + 1, m);
       for (int cl = t; cl < ncol; cl += blockDim.x) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
       __syncthreads();
+      PMARK(4);
       if (ncol > 0) {
         int segs = min(8, max(1, nw / ncol));
         const int len = m - (i + 1);
@@ -382,6 +437,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
           if (lane == 0) S.ypart[cl * 8 + sg] = v;
         }
         __syncthreads();
+        PMARK(5);
         for (int cl = wid; cl < ncol; cl += nw) {  // warp per column, lanes over l
           const int c = c_s + cl, lc = c - ca;
           float ydot = 0.f;
@@ -406,16 +462,15 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         }
       }
       __syncthreads();
-      // partials over own columns c > i+1: [0] ||w||^2, [1..j+1] Y^T w, [j+2..2j+1] VT^T w
+      // partials over own columns c > i+1: [1..j+1] Y^T w, [j+2..2j+1] VT^T w,
+      // and ||w||^2 as a compensated pair at [kPS-2, kPS-1]
       const int c1 = max(c_s, i + 2);
       if (wid == 0) {
-        double acc = 0.0;
-        for (int c = c1 + lane; c < cb; c += 32) {
-          double w = S.owncol[c - c_s];
-          acc += w * w;
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) p.rownrm[b] = acc;
+        FF acc{0.f, 0.f};
+        for (int c = c1 + lane; c < cb; c += 32) acc = ff_add_sq(acc, S.owncol[c - c_s]);
+        acc = warp_sum_ff(acc);
+        if (lane == 0)
+          *reinterpret_cast<float2*>(p.rowpart + (size_t)b * kPS + kPS - 2) = make_float2(acc.hi, acc.lo);
       }
       if (t >= 32 && t < 32 + 2 * j + 1) {
         const int q = t - 32;
@@ -425,17 +480,19 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         p.rowpart[(size_t)b * kPS + 1 + q] = acc;
       }
     }
+    PMARK(6);
     if (!grid_sync(p.bar, p.P, p.st, 2)) return;
+    PMARK(7);
 
     // ---------------- S5: row reflector
     if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
     if (t >= 96 && t < 96 + j + 1) S.q1[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
     if (t >= 160 && t < 160 + j) S.q2[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
-    reduce_partials(p.rowpart, p.rownrm, p.P, 2 * j + 2, S.stage, S.tot, S.dred);
+    reduce_partials(p.rowpart, p.P, 2 * j + 2, S.tot, S.nrm);
     if (t == 0) {
       float x0 = S.misc[1], beta, tau, scale;
       if (i < n - 2) {
-        householder(x0, S.dred[0], &beta, &tau, &scale);
+        householder_ff(x0, *S.nrm, &beta, &tau, &scale);
       } else {  // one element left: no reflection (bidiag.c:125-129)
         beta = x0;
         tau = 0.f;
@@ -465,6 +522,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         S.VTS[(c - ca) * kLD + j] = v;
       }
     }
+    PMARK(8);
     // stage the unscaled row for x = A v; prefetch the original column i+1 of own rows
     if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
     {
@@ -472,12 +530,14 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       for (int r = r_lo + t; r < rb; r += blockDim.x) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
     }
     __syncthreads();
+    PMARK(9);
     // ---------------- S6: x = A v on own rows, X column j
     {
       const int r_lo = max(ra, i + 1);
       if (rb > r_lo) {
         const int R4 = (rb - ra + 3) >> 2;
         if (tp != 0.f) block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
+        PMARK(10);
         for (int r = r_lo + wid; r < rb; r += nw) {  // warp per row, lanes over l
           const int lr = r - ra;
           float part = 0.f;
@@ -494,6 +554,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       }
     }
     __syncthreads();
+    PMARK(11);
   }
 }
 
@@ -668,6 +729,55 @@ __global__ void export_reflectors_kernel(int m, int n, const float* __restrict__
 }
 
 // ------------------------------------------------------------------------
+// Range scaling for the blocked path.  Its Householder norms are compensated
+// FP32 sums, so the matrix is brought into [2^-40, 2^40] by an exact power of
+// two when max|a| lies outside (LAPACK's xGESVD scales for the same reason);
+// inputs already in range are not touched.  d and e are scaled back after the
+// factorisation; the reflectors do not depend on the scale.
+// ------------------------------------------------------------------------
+__global__ void range_scan_kernel(int m, int n, const float* __restrict__ W, int ldw, unsigned* amax) {
+  float mx = 0.f;
+  const int m4 = m >> 2;
+  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    const float4* col = reinterpret_cast<const float4*>(W + (size_t)c * ldw);
+    for (int q = threadIdx.x; q < m4; q += blockDim.x) {
+      const float4 v = col[q];
+      mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+    }
+    for (int r = 4 * m4 + threadIdx.x; r < m; r += blockDim.x) mx = fmaxf(mx, fabsf(W[r + (size_t)c * ldw]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(amax, __float_as_uint(mx));
+}
+
+// 2^k with max|a| * 2^k in [0.5, 1) when max|a| is outside [2^-40, 2^40], else 1
+__device__ __forceinline__ float range_scale(unsigned bits) {
+  const float a = __uint_as_float(bits);
+  if (!(a > 0.f) || isinf(a) || (a >= 0x1p-40f && a <= 0x1p40f)) return 1.f;
+  int ex = 0;
+  frexpf(a, &ex);
+  return ldexpf(1.f, max(-126, min(126, -ex)));
+}
+
+__global__ void range_apply_kernel(int m, int n, float* W, int ldw, const unsigned* amax) {
+  const float s = range_scale(*amax);
+  if (s == 1.f) return;
+  for (int c = blockIdx.x; c < n; c += gridDim.x)
+    for (int r = threadIdx.x; r < m; r += blockDim.x) W[r + (size_t)c * ldw] *= s;
+}
+
+__global__ void range_unscale_kernel(int n, float* d, float* e, const unsigned* amax) {
+  const float s = range_scale(*amax);
+  if (s == 1.f) return;
+  const float inv = 1.f / s;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    d[i] *= inv;
+    if (i < n - 1) e[i] *= inv;
+  }
+}
+
+// ------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------
 int bidiag_coop_ctas(ddcsvd_context* ctx, int m, int n) {
@@ -687,6 +797,7 @@ void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWo
   w->colpart = a.take<float>((size_t)P * kPS + 2 * P);
   w->rowpart = a.take<float>((size_t)P * kPS + 2 * P);
   w->bar = a.take<GridBarrier>(4);
+  w->amax = a.take<unsigned>(4);
   w->gemm_scratch = a.take<char>(gemm_scratch_bytes(kind, m, n, 2 * kPanel));
   const bool tc = (kind != GEMM_SIMT);
   w->Apk = a.take<float>(tc ? (size_t)m * 2 * kPanel + 64 : 16);
@@ -706,6 +817,12 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
                    float* tauq, float* taup, BidiagWork& w, GemmKind kind, Arena* scratch) {
   if (m < n || n <= 0) return DDCSVD_ERR_ARG;
   const int P = w.P;
+  const int sg = std::min(n, 4 * ctx->num_sms);
+  DDC_CUDA_TRY(cudaMemsetAsync(w.amax, 0, sizeof(unsigned), ctx->stream));
+  range_scan_kernel<<<sg, 256, 0, ctx->stream>>>(m, n, W, ldw, w.amax);
+  range_apply_kernel<<<sg, 256, 0, ctx->stream>>>(m, n, W, ldw, w.amax);
+  count_launch(2);
+  DDC_CUDA_TRY(cudaGetLastError());
   for (int k0 = 0; k0 < n; k0 += kPanel) {
     const int nb = std::min(kPanel, n - k0);
     PanelParams pp;
@@ -750,6 +867,9 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
       ktimer_end(ctx);
     }
   }
+  range_unscale_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(n, d, e, w.amax);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
 }
 
@@ -784,3 +904,9 @@ int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw
 }
 
 }  // namespace ddcsvd
+
+#ifdef DDCSVD_PHASE_TRACE
+extern "C" int ddcsvd_trace_read(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, ddcsvd::g_phase_trace, sizeof(ddcsvd::g_phase_trace));
+}
+#endif

@@ -50,51 +50,78 @@ __device__ __forceinline__ void set_error(DevStatus* st, int code, int detail) {
   if (atomicCAS(&st->code, 0, code) == 0) st->detail = detail;
 }
 
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // Barrier state: one per cooperative launch, zeroed before the launch.
 struct GridBarrier {
-  unsigned count;
-  unsigned gen;
+  unsigned count;  // arrivals so far in this launch (only ever grows)
+  unsigned gen;    // unused, kept for layout
 };
 
 // Grid-wide barrier for a cooperative launch of `nblocks` CTAs.  Returns
 // false (in every thread of the CTA) if the status word holds an error or
 // the wait exceeded kWaitLimitNs; callers then leave their loops.
+//
+// The arrival counter is never reset inside a launch: barrier k of the launch
+// is complete once it reaches (k + 1) * nblocks, and because no CTA can arrive
+// at barrier k + 1 before barrier k is complete, the value returned by a CTA's
+// own arrival tells it which barrier it is in.  That costs one atomic round
+// trip per CTA plus the polls, with no second "release" write on the critical
+// path.  The status word is read alongside the arrival and then every 32 polls.
 __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, DevStatus* st,
                                           int where) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    int ok = ld_volatile_int(&st->code) == 0;
-    if (ok) {
-      unsigned g = ld_acquire(&bar->gen);
-      __threadfence();
-      unsigned arrived = atomicAdd(&bar->count, 1u);
-      if (arrived == nblocks - 1) {
-        bar->count = 0;
-        __threadfence();
-        atomicAdd(&bar->gen, 1u);
-      } else {
-        unsigned long long t0 = global_ns();
-        while (ld_acquire(&bar->gen) == g) {
+    const int code = ld_volatile_int(&st->code);
+    const unsigned old = atom_add_acq_rel(&bar->count, 1u);
+    const unsigned target = (old / nblocks + 1u) * nblocks;
+    int ok = code == 0;
+    if (ok && old + 1u != target) {
+      unsigned polls = 0;
+      unsigned long long t0 = 0;
+      while ((int)(ld_acquire(&bar->count) - target) < 0) {
+        if ((++polls & 31u) == 0) {
           if (ld_volatile_int(&st->code) != 0) {
             ok = 0;
             break;
           }
-          if (global_ns() - t0 > kWaitLimitNs) {
+          const unsigned long long now = global_ns();
+          if (t0 == 0) {
+            t0 = now;
+          } else if (now - t0 > kWaitLimitNs) {
             set_error(st, DDCSVD_ERR_TIMEOUT, where);
             ok = 0;
             break;
           }
-          __nanosleep(32);
         }
       }
-      __threadfence();
     }
     s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
 }
+
+// Optional phase trace for kernel tuning: a build with -DDDCSVD_PHASE_TRACE
+// records %globaltimer at DDC_MARK points of one CTA into a device array that
+// ddcsvd_trace_read() copies out.  Without the macro the marks compile to
+// nothing.
+#ifdef DDCSVD_PHASE_TRACE
+// the translation unit that uses the marks defines g_phase_trace[128 * 16]
+#define DDC_MARK(cond, row, slot)                                                        \
+  do {                                                                                   \
+    if ((cond) && threadIdx.x == 0 && (row) < 128) g_phase_trace[(row) * 16 + (slot)] = global_ns(); \
+  } while (0)
+#else
+#define DDC_MARK(cond, row, slot) \
+  do {                            \
+  } while (0)
+#endif
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -107,6 +134,43 @@ template <typename T>
 __device__ __forceinline__ T warp_prod(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v *= __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---- compensated (float-float) sums
+// A value hi + lo with |lo| <= ulp(hi)/2, built from error-free transforms
+// (Knuth's two-sum, the FMA product error).  Sums of squares carried this way
+// keep about 44 significant bits using only FP32 instructions: on GB300 the
+// FP64 pipe is narrow and its latency sits on the critical path of every
+// Householder step, so the panel kernels avoid it.  The _rn intrinsics keep
+// the compiler from contracting or reassociating the error terms.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  const float t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s, t);
+  return FF{hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+
+// a + x * x with the product's rounding error kept
+__device__ __forceinline__ FF ff_add_sq(FF a, float x) {
+  const float p = __fmul_rn(x, x);
+  const float pe = __fmaf_rn(x, x, -p);
+  return ff_add(a, FF{p, pe});
+}
+
+__device__ __forceinline__ FF warp_sum_ff(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    // order the operands by lane so that both partners compute the same sum
+    v = ((threadIdx.x & o) == 0) ? ff_add(v, w) : ff_add(w, v);
+  }
   return v;
 }
 

@@ -96,6 +96,7 @@ struct BidiagWork {
   float *xcol, *xrow;
   float *colpart, *rowpart;
   GridBarrier* bar;
+  unsigned* amax;  // max |a| of the input (bit pattern), for range scaling
   int P;  // CTAs of the cooperative launch
   char* gemm_scratch;
   float *Apk, *Bpk;  // K-major packed trailing-update operands (tensor-core modes)

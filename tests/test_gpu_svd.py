@@ -137,6 +137,22 @@ def test_deterministic(lib, cuda):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("mode", ["blocked", "tf32x6"])
+@pytest.mark.parametrize("scale", [2.0 ** 60, 2.0 ** -60, 1e30, 1e-30])
+def test_svd_extreme_magnitudes(lib, cuda, orc, mode, scale):
+    """Inputs far outside [2^-40, 2^40]: the blocked path scales by a power of
+    two before its FP32 compensated norms and scales d, e back; sigma must
+    follow the input scale and the vectors must be those of the unscaled input."""
+    if not _mode_available(lib, mode):
+        pytest.skip(f"{mode} unavailable")
+    rng = np.random.default_rng(11)
+    A = rng.uniform(-1, 1, (200, 120)).astype(np.float32)
+    As = (A.astype(np.float64) * scale).astype(np.float32)
+    s, U, V = run(lib, cuda, As, mode)
+    assert np.all(np.isfinite(s)) and np.all(np.isfinite(U)) and np.all(np.isfinite(V))
+    check_metrics(orc, As.astype(np.float64) / scale, s / scale, U, V)
+
+
 def test_nonfinite_input_fails_loudly(lib, cuda):
     A = np.ones((16, 8), dtype=np.float32)
     A[3, 2] = np.nan
