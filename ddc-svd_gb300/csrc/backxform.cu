@@ -67,10 +67,182 @@ __global__ void wy_tfactor_kernel(int bs, int j0, const float* __restrict__ tau,
   for (int idx = t; idx < bs * bs; idx += blockDim.x) T[idx] = sT[idx % bs][idx / bs];
 }
 
+// ---------------------------------------------------------------- tensor-core path
+// All reflectors of one side as an explicit column-major matrix Uc (column j
+// = reflector j over the rows of C: zero above its unit entry at row j + side,
+// the stored vector below, all zero when tau_j = 0).  Left reflectors are
+// columns of W, right reflectors rows of W (transposed here through a 32 x 32
+// shared-memory tile, so both reads and writes are coalesced).
+__global__ void build_reflectors_kernel(int side, int rows_total, int nref, const float* __restrict__ W, int ldw,
+                                        const float* __restrict__ tau, float* Uc, int ldu) {
+  __shared__ float tile[32][33];  // [row][reflector]
+  const int r0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    // side 0 reads W[r, j] along r; side 1 reads W[j, r] along j
+    const int r = side == 0 ? r0 + threadIdx.x : r0 + k;
+    const int j = side == 0 ? j0 + k : j0 + threadIdx.x;
+    float v = 0.f;
+    if (r < rows_total && j < nref && tau[j] != 0.f) {
+      if (r == j + side) v = 1.f;
+      else if (r > j + side) v = side == 0 ? W[r + (size_t)j * ldw] : W[j + (size_t)r * ldw];
+    }
+    if (side == 0) tile[threadIdx.x][k] = v;
+    else tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + threadIdx.x, j = j0 + k;
+    if (r < ldu && j < nref) Uc[r + (size_t)j * ldu] = tile[threadIdx.x][k];
+  }
+}
+
+// Offset (floats) of block b's U_b T_b in the packed UT array: block b covers
+// rows [b kWY, rows_total) and is stored row-major with kWY columns.
+__host__ __device__ inline long long ut_offset(int b, int rows_total) {
+  return (long long)kWY * ((long long)b * rows_total - (long long)kWY * b * (b - 1) / 2);
+}
+
+// One CTA per WY block b (reflectors j0 = b kWY ... j0 + bs - 1, rows
+// [j0, rows_total) of Uc):  G = U_b^T U_b,  the compact-WY factor T_b
+// (T[l,l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l]), and
+// UT_b = U_b T_b (row-major, ld kWY), so that applying the block is
+// C -= UT_b (U_b^T C): two tensor-core products and no per-block small kernels.
+constexpr int kPrepRows = 32;
+__global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nref, const float* __restrict__ Uc,
+                                                         int ldu, const float* __restrict__ tau, float* UT) {
+  __shared__ float sU[kPrepRows][kWY + 1];
+  __shared__ float sG[kWY][kWY + 1];
+  __shared__ float sT[kWY][kWY + 1];
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int j0 = b * kWY, bs = min(kWY, nref - j0);
+  const int rows = rows_total - j0;
+  if (bs <= 0 || rows <= 0) return;
+  const float* U = Uc + j0 + (size_t)j0 * ldu;  // U_b(r, c) = U[r + c * ldu]
+  float* out = UT + ut_offset(b, rows_total);
+  auto load_tile = [&](int r0) {
+    for (int idx = t; idx < kPrepRows * kWY; idx += 256) {
+      const int rr = idx & (kPrepRows - 1), c = idx / kPrepRows;
+      const int r = r0 + rr;
+      sU[rr][c] = (r < rows && c < bs) ? U[r + (size_t)c * ldu] : 0.f;
+    }
+  };
+  // ---- G = U^T U: thread owns the 4 x 4 block (4 ti .., 4 tj ..)
+  {
+    const int ti = t & 15, tj = t >> 4;
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[a][c] = 0.f;
+    for (int r0 = 0; r0 < rows; r0 += kPrepRows) {
+      __syncthreads();
+      load_tile(r0);
+      __syncthreads();
+#pragma unroll 8
+      for (int k = 0; k < kPrepRows; k++) {
+        float x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+          x[a] = sU[k][4 * ti + a];
+          y[a] = sU[k][4 * tj + a];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) acc[a][c] += x[a] * y[c];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) sG[4 * ti + a][4 * tj + c] = acc[a][c];
+    for (int idx = t; idx < kWY * kWY; idx += 256) sT[idx & (kWY - 1)][idx / kWY] = 0.f;
+  }
+  __syncthreads();
+  // ---- T: column l from the finished columns 0..l-1; four threads per row
+  {
+    const int row = t >> 2, part = t & 3;
+    for (int l = 0; l < bs; l++) {
+      float sum = 0.f;
+      if (row < l)
+        for (int k = row + part; k < l; k += 4) sum += sT[row][k] * sG[k][l];
+      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+      const float tl = tau[j0 + l];
+      if (part == 0 && row < l) sT[row][l] = -tl * sum;
+      if (t == 0) sT[l][l] = tl;
+      __syncthreads();
+    }
+  }
+  // ---- UT = U T: thread owns row t/8 of the tile and 8 consecutive columns
+  {
+    const int rr = t >> 3, c0 = (t & 7) * 8;
+    for (int r0 = 0; r0 < rows; r0 += kPrepRows) {
+      __syncthreads();
+      load_tile(r0);
+      __syncthreads();
+      float acc[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) acc[c] = 0.f;
+#pragma unroll 8
+      for (int k = 0; k < kWY; k++) {
+        const float x = sU[rr][k];
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[c] += x * sT[k][c0 + c];
+      }
+      const int r = r0 + rr;
+      if (r < rows) {
+        float4* o = reinterpret_cast<float4*>(out + (size_t)r * kWY + c0);
+        o[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        o[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      }
+    }
+  }
+}
+
+// C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
+// last first:  W1 = U_b^T C (stored K-major for the next product) and
+// C -= UT_b W1.
+static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw,
+                            const float* tau, float* C, int ldc, int ncols, GemmKind kind, Arena& a,
+                            bool plan_only) {
+  const int ldu = (int)round_up(rows_total, 32);
+  const int nblk = ceil_div(std::max(nref, 1), kWY);
+  float* Uc = a.take<float>((size_t)ldu * std::max(nref, 1));
+  float* UT = a.take<float>((size_t)ut_offset(nblk, rows_total) + 64);
+  float* W1s = a.take<float>((size_t)kWY * ncols + 64);
+  const size_t sbytes = gemm_scratch_bytes(kind, ncols, kWY, rows_total);
+  char* sc = a.take<char>(sbytes);
+  if (plan_only || nref <= 0) return DDCSVD_OK;
+  Arena scratch;
+  scratch.base = sc;
+  scratch.plan = false;
+  scratch.cap = sbytes;
+  build_reflectors_kernel<<<dim3(ceil_div(ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
+      side, rows_total, nref, W, ldw, tau, Uc, ldu);
+  wy_prepare_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, tau, UT);
+  count_launch(2);
+  DDC_CUDA_TRY(cudaGetLastError());
+  for (int bi = nblk - 1; bi >= 0; bi--) {
+    const int j0 = bi * kWY;
+    const int bs = std::min(kWY, nref - j0);
+    const int rows = rows_total - j0;
+    if (rows <= 0 || bs <= 0) continue;
+    // W1^T = C[j0:, :]^T U_b, stored as W1s[j + n * kWY]
+    DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, Uc + (size_t)j0 * ldu, ldu, j0, W1s, kWY, 1.f,
+                             0.f, &scratch));
+    // C[j0:, :] -= UT_b W1
+    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, UT + ut_offset(bi, rows_total), kWY, 0, W1s, kWY, 0,
+                           C + j0, ldc, -1.f, 1.f, &scratch));
+  }
+  return DDCSVD_OK;
+}
+
 static int apply_blocked(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W,
                          int ldw, const float* tau, float* C, int ldc, int ncols, GemmKind kind,
                          Arena& a, bool plan_only) {
   const bool tc = (kind != GEMM_SIMT);
+  if (tc) return apply_blocked_tc(ctx, side, rows_total, nref, W, ldw, tau, C, ldc, ncols, kind, a, plan_only);
   const int ldp = (int)round_up(rows_total + 4, 32);
   float* Pk = a.take<float>((size_t)ldp * kWY);
   float* PkT = a.take<float>(tc ? (size_t)ldp * kWY : 16);

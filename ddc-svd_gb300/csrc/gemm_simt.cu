@@ -125,8 +125,38 @@ __global__ void splitk_reduce_kernel(int M, int N, int ksplit, const float* part
 int gemm_tc(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Mat B1, int K2,
             Mat A2, Mat B2, float alpha, float beta, float* C, int ldc, Arena* scratch);
 
+// Transposed variant: element (r, c) of the sum goes to C[c + r * ldc].  A
+// 32 x 32 tile is summed with loads along r and stored along c.
+__global__ void splitk_reduce_t_kernel(int M, int N, int ksplit, const float* __restrict__ partial, float alpha,
+                                       float beta, float* C, int ldc) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const size_t tot = (size_t)M * N;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + threadIdx.x, c = c0 + k;
+    float s = 0.f;
+    if (r < M && c < N)
+      for (int z = 0; z < ksplit; z++) s += partial[(size_t)z * tot + r + (size_t)c * M];
+    tile[k][threadIdx.x] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < M && c < N) {
+      float* cp = C + c + (size_t)r * ldc;
+      *cp = (beta == 0.f ? 0.f : beta * *cp) + alpha * tile[threadIdx.x][k];
+    }
+  }
+}
+
 void splitk_reduce(ddcsvd_context* ctx, int M, int N, int ksplit, const float* partial, float alpha,
-                   float beta, float* C, int ldc) {
+                   float beta, float* C, int ldc, bool trans) {
+  if (trans) {
+    splitk_reduce_t_kernel<<<dim3(ceil_div(M, 32), ceil_div(N, 32)), dim3(32, 8), 0, ctx->stream>>>(
+        M, N, ksplit, partial, alpha, beta, C, ldc);
+    count_launch();
+    return;
+  }
   const int blocks = std::min(4 * ctx->num_sms, ceil_div(M * N, 256));
   splitk_reduce_kernel<<<blocks, 256, 0, ctx->stream>>>(M, N, ksplit, partial, alpha, beta, C, ldc);
   count_launch();
@@ -165,8 +195,12 @@ int pack_kmajor(ddcsvd_context* ctx, int rows, int K1, const float* P1, int ld1,
 }
 size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K);
 
+// Split-K partial buffers: K is split only when the output has fewer tiles
+// than SMs, into at most 16 and at most 2 * SMs / tiles pieces, so
+// ksplit * M * N <= 2 * SMs * 128 * 128 (bounded here for up to 256 SMs).
 size_t gemm_scratch_bytes(GemmKind kind, int M, int N, int K) {
-  size_t simt = (size_t)16 * M * N * sizeof(float) + 4096;
+  const size_t cap = (size_t)2 * 256 * 128 * 128;
+  size_t simt = std::min((size_t)16 * M * N, cap) * sizeof(float) + 4096;
   if (kind == GEMM_SIMT) return simt;
   return std::max(simt, gemm_tc_scratch_bytes(kind, M, N, K));
 }

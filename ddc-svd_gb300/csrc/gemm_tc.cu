@@ -41,7 +41,7 @@
 namespace ddcsvd {
 
 void splitk_reduce(ddcsvd_context* ctx, int M, int N, int ksplit, const float* partial, float alpha,
-                   float beta, float* C, int ldc);
+                   float beta, float* C, int ldc, bool trans);
 
 namespace tc {
 
@@ -179,6 +179,7 @@ struct TcParams {
   int ldc;
   float alpha, beta;
   float* partial;  // split-K partials (M x N per split, ld M) or null
+  int trans;       // store C transposed: element (r, c) at C[c + r * ldc]
   DevStatus* st;
 };
 
@@ -355,16 +356,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         } else {
           // 16 independent loads of C in flight, then the 16 updates
+          const size_t rs = p.trans ? (size_t)p.ldc : 1, cs = p.trans ? 1 : (size_t)p.ldc;
           float old[16];
 #pragma unroll
           for (int jj = 0; jj < 16; jj++) {
             const int col = n0 + c0 + jj;
-            old[jj] = (p.beta != 0.f && col < p.N) ? p.C[row + (size_t)col * p.ldc] : 0.f;
+            old[jj] = (p.beta != 0.f && col < p.N) ? p.C[row * rs + col * cs] : 0.f;
           }
 #pragma unroll
           for (int jj = 0; jj < 16; jj++) {
             const int col = n0 + c0 + jj;
-            if (col < p.N) p.C[row + (size_t)col * p.ldc] = p.beta * old[jj] + p.alpha * acc[c0 + jj];
+            if (col < p.N) p.C[row * rs + col * cs] = p.beta * old[jj] + p.alpha * acc[c0 + jj];
           }
         }
       }
@@ -428,7 +430,7 @@ static int make_map(CUtensorMap* map, const float* base, long long kext, long lo
 template <int BN, int NP>
 static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long long lda, int a_koff,
                   const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha, float beta,
-                  Arena* scratch) {
+                  Arena* scratch, bool trans) {
   using L = Layout<BN, NP>;
   CUtensorMap ma, mb;
   DDC_TRY(make_map(&ma, A, (long long)a_koff + K, M, lda, BM));
@@ -449,6 +451,7 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   p.ldc = ldc;
   p.alpha = alpha;
   p.beta = beta;
+  p.trans = trans ? 1 : 0;
   p.st = ctx->d_status;
   const int tiles = ceil_div(M, BM) * ceil_div(N, BN);
   int ksplit = 1;
@@ -464,7 +467,7 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   tc_gemm_split_tf32_kernel<BN, NP><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, p);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
-  if (ksplit > 1) splitk_reduce(ctx, M, N, ksplit, p.partial, alpha, beta, C, ldc);
+  if (ksplit > 1) splitk_reduce(ctx, M, N, ksplit, p.partial, alpha, beta, C, ldc, trans);
   return DDCSVD_OK;
 }
 
@@ -482,12 +485,12 @@ bool tc_available(ddcsvd_context* ctx) {
 size_t gemm_tc_scratch_bytes(GemmKind kind, int M, int N, int K) {
   (void)kind;
   (void)K;
-  return (size_t)16 * M * N * sizeof(float) + 4096;
+  return std::min((size_t)16 * M * N, (size_t)2 * 256 * 128 * 128) * sizeof(float) + 4096;
 }
 
-int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
-                   int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
-                   float beta, Arena* scratch) {
+static int tc_dispatch(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                       int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
+                       float beta, Arena* scratch, bool trans) {
   if (kind != GEMM_TF32X3 && kind != GEMM_TF32X6) {
     set_last_error("split-BF16 tensor-core GEMM is not implemented");
     return DDCSVD_ERR_UNSUPPORTED;
@@ -495,11 +498,25 @@ int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, cons
   if (M <= 0 || N <= 0) return DDCSVD_OK;
   if ((a_koff & 3) || (b_koff & 3)) return DDCSVD_ERR_ARG;
   if (kind == GEMM_TF32X6) {
-    if (N <= 64) return tc::launch<64, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
-    return tc::launch<128, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+    if (N <= 64)
+      return tc::launch<64, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
+    return tc::launch<128, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   }
-  if (N <= 64) return tc::launch<64, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
-  return tc::launch<128, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch);
+  if (N <= 64)
+    return tc::launch<64, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
+  return tc::launch<128, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
+}
+
+int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                   int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
+                   float beta, Arena* scratch) {
+  return tc_dispatch(ctx, kind, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, false);
+}
+
+int gemm_tc_kmajor_t(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                     int a_koff, const float* B, long long ldb, int b_koff, float* Ct, int ldct, float alpha,
+                     float beta, Arena* scratch) {
+  return tc_dispatch(ctx, kind, M, N, K, A, lda, a_koff, B, ldb, b_koff, Ct, ldct, alpha, beta, scratch, true);
 }
 
 // Strided-operand entry used by gemm(): only the K-major layouts map onto the

@@ -85,6 +85,11 @@ bool tc_available(ddcsvd_context* ctx);
 int gemm_tc_kmajor(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
                    int a_koff, const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha,
                    float beta, Arena* scratch);
+// The same with C stored transposed: element (r, c) of the M x N result at
+// Ct[c + r * ldct].
+int gemm_tc_kmajor_t(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, const float* A, long long lda,
+                     int a_koff, const float* B, long long ldb, int b_koff, float* Ct, int ldct, float alpha,
+                     float beta, Arena* scratch);
 // rows x (K1 + K2) K-major copy of two column-major blocks.
 int pack_kmajor(ddcsvd_context* ctx, int rows, int K1, const float* P1, int ld1, int K2, const float* P2, int ld2,
                 float* out, int ldo);
