@@ -38,8 +38,18 @@ constexpr int kPS = 2 * kPanel + 4;  // floats per partial-sum record
 #ifdef DDCSVD_PHASE_TRACE
 __device__ unsigned long long g_phase_trace[128 * 16];
 #endif
-// phase marks of the panel kernel: CTA 7, column 5 of every panel, one row per panel
+// phase marks of the panel kernel, CTA 7: column 5 of every panel (one row per
+// panel), or with DDCSVD_TRACE_ALLCOLS every column of the panels at k0 = 0,
+// 1024, 2048, 3072 (row = 32 * (k0 / 1024) + j)
+// (slots 12 / 13: kernel entry / exit)
+#ifdef DDCSVD_TRACE_ALLCOLS
+#define PMARK(slot) DDC_MARK(blockIdx.x == 7 && (p.k0 & 1023) == 0, 32 * (p.k0 >> 10) + j, slot)
+#define PMARK_K(slot) \
+  DDC_MARK(blockIdx.x == 7 && (p.k0 & 1023) == 0, 32 * (p.k0 >> 10) + ((slot) == 12 ? 0 : 31), slot)
+#else
 #define PMARK(slot) DDC_MARK(blockIdx.x == 7 && j == 5, p.k0 / kPanel, slot)
+#define PMARK_K(slot) DDC_MARK(blockIdx.x == 7, p.k0 / kPanel, slot)
+#endif
 
 struct PanelParams {
   int m, n, k0, nb, ldw, ldn, P;
@@ -191,60 +201,55 @@ __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int
 }
 
 // Deterministic sum over the P per-CTA partial records of `cnt` floats plus
-// the compensated norm pair at [kPS - 2], [kPS - 1].  Warp w owns entries w,
-// w + nw, ... and lanes take records lane, lane + 32, ...: every load of a
-// warp is issued before the first add, so the reduction costs one L2 round
-// trip, and the fixed lane order and shuffle tree make the result independent
-// of timing.
-__device__ __forceinline__ void reduce_partials(const float* __restrict__ part, int P, int cnt, float* tot,
-                                                FF* ntot) {
-  constexpr int kE = 5, kB = 8;  // entries per warp and records per lane held in one pass
+// the compensated norm pair at [kPS - 2], [kPS - 1].  Warp w takes records
+// w, w + nw, ...; its lanes read each record along q (coalesced 128-byte
+// lines: an earlier version read along b, one sector per lane, and its cost
+// grew with cnt to ~9 us).  All loads of a warp are issued before the first
+// add; the nw warp sums are then added in warp order, so the result does not
+// depend on timing.  `red` holds nw * (kPS + 4) floats.
+__device__ __forceinline__ void reduce_partials(const float* __restrict__ part, int P, int cnt, float* red,
+                                                float* tot, FF* ntot) {
+  constexpr int kR = 12;  // records per warp held in one pass (P <= kR * nw in one pass)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  float acc[kE];
+  float a0 = 0.f, a1 = 0.f;
   FF nacc{0.f, 0.f};
+  for (int b0 = w; b0 < P; b0 += kR * nw) {
+    float v0[kR], v1[kR];
+    float2 nv[kR];
 #pragma unroll
-  for (int e = 0; e < kE; e++) acc[e] = 0.f;
-  for (int b0 = 0; b0 < P; b0 += 32 * kB) {
-    float v[kE][kB];
-    float2 nv[kB];
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int b = b0 + lane + 32 * u;
-      nv[u] = (w == nw - 1 && b < P) ? __ldcg(reinterpret_cast<const float2*>(part + (size_t)b * kPS + kPS - 2))
-                                     : make_float2(0.f, 0.f);
+    for (int u = 0; u < kR; u++) {
+      const int b = b0 + u * nw;
+      const float* rec = part + (size_t)b * kPS;
+      const bool in = b < P;
+      v0[u] = (in && lane < cnt) ? __ldcg(rec + lane) : 0.f;
+      v1[u] = (in && lane + 32 < cnt) ? __ldcg(rec + 32 + lane) : 0.f;
+      nv[u] = (in && lane == 0) ? __ldcg(reinterpret_cast<const float2*>(rec + kPS - 2)) : make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int e = 0; e < kE; e++) {
-      const int q = w + e * nw;
-#pragma unroll
-      for (int u = 0; u < kB; u++) {
-        const int b = b0 + lane + 32 * u;
-        v[e][u] = (q < cnt && b < P) ? __ldcg(part + (size_t)b * kPS + q) : 0.f;
-      }
+    for (int u = 0; u < kR; u++) {
+      a0 += v0[u];
+      a1 += v1[u];
+      nacc = ff_add(nacc, FF{nv[u].x, nv[u].y});
     }
-#pragma unroll
-    for (int u = 0; u < kB; u++) nacc = ff_add(nacc, FF{nv[u].x, nv[u].y});
-#pragma unroll
-    for (int e = 0; e < kE; e++)
-#pragma unroll
-      for (int u = 0; u < kB; u++) acc[e] += v[e][u];
   }
-#pragma unroll
-  for (int e = 0; e < kE; e++) {
-    const int q = w + e * nw;
-    const float sum = warp_sum(acc[e]);
-    if (lane == 0 && q < cnt) tot[q] = sum;
+  static_assert(2 * kPanel <= 64, "record entries beyond 64 are not reduced");
+  float* rw = red + w * (kPS + 4);
+  rw[lane] = a0;
+  rw[32 + lane] = a1;
+  if (lane == 0) {
+    rw[kPS] = nacc.hi;
+    rw[kPS + 1] = nacc.lo;
   }
-  // entries beyond kE * nw (only with fewer than 16 warps)
-  for (int q = w + kE * nw; q < cnt; q += nw) {
-    float a2 = 0.f;
-    for (int b = lane; b < P; b += 32) a2 += __ldcg(part + (size_t)b * kPS + q);
-    a2 = warp_sum(a2);
-    if (lane == 0) tot[q] = a2;
-  }
-  if (w == nw - 1) {
-    nacc = warp_sum_ff(nacc);
-    if (lane == 0) *ntot = nacc;
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < cnt && t < 64) {
+    float sum = 0.f;
+    for (int k = 0; k < nw; k++) sum += red[k * (kPS + 4) + t];
+    tot[t] = sum;
+  } else if (t == 64) {
+    FF sum{0.f, 0.f};
+    for (int k = 0; k < nw; k++) sum = ff_add(sum, FF{red[k * (kPS + 4) + kPS], red[k * (kPS + 4) + kPS + 1]});
+    *ntot = sum;
   }
   __syncthreads();
 }
@@ -276,6 +281,7 @@ struct PanelSmem {
   float* misc;    // 8: prefetched scalars
   float *Yi, *VTi, *Wi, *Xi, *p1, *p2, *q1, *q2, *tot;
   FF* nrm;        // reduced compensated norm
+  float* redp;    // (threads / 32) * (kPS + 4): per-warp partial sums
   float* scal;    // 8
 };
 
@@ -311,6 +317,8 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
   s.nrm = reinterpret_cast<FF*>(p);
   p += 64;
   s.scal = p;
+  p += 8;
+  s.redp = p;
   return s;
 }
 
@@ -318,7 +326,7 @@ size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P) {
   size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
              round_up(cc * 8 + 4, 4) + 2 * (size_t)rc * kLD + 2 * (size_t)cc * kLD +
              round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
-             64 + 8;
+             64 + 8 + (size_t)(threads / 32) * (kPS + 4);
   return f * sizeof(float) + 64;
 }
 
@@ -334,6 +342,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
   const int ra = rbase + b * p.rc, rb = min(m, ra + p.rc);
   const int ca = k0 + 1 + b * p.cc, cb = min(n, ca + p.cc);
   float prev_taup = 0.f;  // tau of the previous step's right reflector
+  PMARK_K(12);
 
   for (int j = 0; j < p.nb; j++) {
     const int i = k0 + j;
@@ -391,7 +400,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
     }
     if (t == 64) S.misc[0] = __ldcg(p.xcol + i);
-    reduce_partials(p.colpart, p.P, 2 * j + 1, S.tot, S.nrm);
+    reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm);
     if (t == 0) {
       float x0 = S.misc[0], alpha, tau, scale;
       householder_ff(x0, *S.nrm, &alpha, &tau, &scale);
@@ -488,7 +497,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
     if (t >= 96 && t < 96 + j + 1) S.q1[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
     if (t >= 160 && t < 160 + j) S.q2[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
-    reduce_partials(p.rowpart, p.P, 2 * j + 2, S.tot, S.nrm);
+    reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm);
     if (t == 0) {
       float x0 = S.misc[1], beta, tau, scale;
       if (i < n - 2) {
@@ -556,6 +565,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     __syncthreads();
     PMARK(11);
   }
+  PMARK_K(13);
 }
 
 // ------------------------------------------------------------------------
