@@ -400,20 +400,25 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
     }
     if (t == 64) S.misc[0] = __ldcg(p.xcol + i);
+    // S3's inputs do not depend on the reflector: stage the unscaled column and
+    // row i of the own columns in the same round trip as the partial records
+    const int c_s = max(ca, i + 1);
+    const int ncol = max(0, cb - c_s);
+    if (i < n - 1) {
+      stage_vec(S.big, p.xcol, i + 1, m);
+      for (int cl = t; cl < ncol; cl += blockDim.x) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
+    }
     reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm);
-    if (t == 0) {
-      float x0 = S.misc[0], alpha, tau, scale;
-      householder_ff(x0, *S.nrm, &alpha, &tau, &scale);
-      S.scal[0] = alpha;
-      S.scal[1] = tau;
-      S.scal[2] = scale;
-      if (b == 0) {
+    // every thread forms the reflector from the same shared inputs (no broadcast round)
+    float tq, sq;
+    {
+      float alpha;
+      householder_ff(S.misc[0], *S.nrm, &alpha, &tq, &sq);
+      if (t == 0 && b == 0) {
         p.d[i] = alpha;
-        p.tauq[i] = tau;
+        p.tauq[i] = tq;
       }
     }
-    __syncthreads();
-    const float tq = S.scal[1], sq = S.scal[2];
     if (t < j) {
       S.p1[t] = S.Wi[t] + sq * S.tot[1 + t];
       S.p2[t] = S.Xi[t] + sq * S.tot[1 + j + t];
@@ -428,12 +433,6 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     PMARK(3);
     // ---------------- S3: y = A^T u on own columns, Y column j, row-i update
     {
-      // stage the unscaled column and prefetch the original row i of own columns
-      const int c_s = max(ca, i + 1);
-      const int ncol = max(0, cb - c_s);
-      stage_vec(S.big, p.xcol, i + 1, m);
-      for (int cl = t; cl < ncol; cl += blockDim.x) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
-      __syncthreads();
       PMARK(4);
       if (ncol > 0) {
         int segs = min(8, max(1, nw / ncol));
@@ -497,26 +496,29 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
     if (t >= 96 && t < 96 + j + 1) S.q1[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
     if (t >= 160 && t < 160 + j) S.q2[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
+    // S6's inputs do not depend on the reflector: stage the unscaled row and the
+    // original column i+1 of the own rows in the same round trip as the records
+    if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
+    {
+      const int r_lo = max(ra, i + 1);
+      for (int r = r_lo + t; r < rb; r += blockDim.x) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
+    }
     reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm);
-    if (t == 0) {
-      float x0 = S.misc[1], beta, tau, scale;
+    float tp, sp;
+    {
+      float beta;
       if (i < n - 2) {
-        householder_ff(x0, *S.nrm, &beta, &tau, &scale);
+        householder_ff(S.misc[1], *S.nrm, &beta, &tp, &sp);
       } else {  // one element left: no reflection (bidiag.c:125-129)
-        beta = x0;
-        tau = 0.f;
-        scale = 0.f;
+        beta = S.misc[1];
+        tp = 0.f;
+        sp = 0.f;
       }
-      S.scal[3] = beta;
-      S.scal[4] = tau;
-      S.scal[5] = scale;
-      if (b == 0) {
+      if (t == 0 && b == 0) {
         p.e[i] = beta;
-        p.taup[i] = tau;
+        p.taup[i] = tp;
       }
     }
-    __syncthreads();
-    const float tp = S.scal[4], sp = S.scal[5];
     prev_taup = tp;
     if (t <= j) S.q1[t] += sp * S.tot[1 + t];
     if (t < j) S.q2[t] += sp * S.tot[j + 2 + t];
@@ -532,12 +534,6 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       }
     }
     PMARK(8);
-    // stage the unscaled row for x = A v; prefetch the original column i+1 of own rows
-    if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
-    {
-      const int r_lo = max(ra, i + 1);
-      for (int r = r_lo + t; r < rb; r += blockDim.x) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
-    }
     __syncthreads();
     PMARK(9);
     // ---------------- S6: x = A v on own rows, X column j
