@@ -350,14 +350,15 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     // ---------------- S1: update column i on own rows, partial sums
     const int r_s = max(ra, i);
     const int nrow = max(0, rb - r_s);
-    // one round trip: row i of Y / VT and the own rows of column i
-    if (t < j) {
-      S.Yi[t] = __ldcg(Y + i + (size_t)t * ldn);
-      // VT[i, t]: row t of the panel's right reflectors at column i; the entry
-      // of the previous step (t = j-1) is its unit leading element.
-      S.VTi[t] = (t == j - 1) ? (prev_taup != 0.f ? 1.f : 0.f) : __ldcg(VT + i + (size_t)t * ldn);
+    // Row i of Y (S.Yi), of VT (S.VTi) and the own rows of column i (S.pre,
+    // indexed r - ra) were loaded by the previous step's S5; only the first
+    // column of a panel loads here.  VT[i, j-1] is the previous right
+    // reflector's unit leading element.
+    if (j == 0) {
+      for (int rr = t; rr < nrow; rr += blockDim.x) S.pre[r_s - ra + rr] = __ldcg(W + r_s + rr + (size_t)i * ldw);
+    } else if (t == 0) {
+      S.VTi[j - 1] = prev_taup != 0.f ? 1.f : 0.f;
     }
-    for (int rr = t; rr < nrow; rr += blockDim.x) S.pre[rr] = __ldcg(W + r_s + rr + (size_t)i * ldw);
     __syncthreads();
     for (int rr = wid; rr < nrow; rr += nw) {  // warp per row, lanes over l
       const int r = r_s + rr, lr = r - ra;
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       if (lane < j) part = S.UpS[lr * kLD + lane] * S.Yi[lane] + S.XS[lr * kLD + lane] * S.VTi[lane];
       part = warp_sum(part);
       if (lane == 0) {
-        const float x = S.pre[rr] - part;
+        const float x = S.pre[lr] - part;
         S.own[rr] = x;
         p.xcol[r] = x;
       }
@@ -494,8 +495,9 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
 
     // ---------------- S5: row reflector
     if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
-    if (t >= 96 && t < 96 + j + 1) S.q1[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
-    if (t >= 160 && t < 160 + j) S.q2[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
+    // row i+1 of Y and VT: needed below and, unscaled, by the next step's S1
+    if (t >= 96 && t < 96 + j + 1) S.Yi[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
+    if (t >= 160 && t < 160 + j) S.VTi[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
     // S6's inputs do not depend on the reflector: stage the unscaled row and the
     // original column i+1 of the own rows in the same round trip as the records
     if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
@@ -520,8 +522,8 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       }
     }
     prev_taup = tp;
-    if (t <= j) S.q1[t] += sp * S.tot[1 + t];
-    if (t < j) S.q2[t] += sp * S.tot[j + 2 + t];
+    if (t <= j) S.q1[t] = S.Yi[t] + sp * S.tot[1 + t];
+    if (t < j) S.q2[t] = S.VTi[t] + sp * S.tot[j + 2 + t];
     {
       const int c_s = max(ca, i + 1);
       for (int c = c_s + t; c < cb; c += blockDim.x) {
