@@ -1,6 +1,7 @@
 // internal.hpp -- declarations shared by the translation units of libddcsvd.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>

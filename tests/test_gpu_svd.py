@@ -153,6 +153,17 @@ def test_svd_extreme_magnitudes(lib, cuda, orc, mode, scale):
     check_metrics(orc, As.astype(np.float64) / scale, s / scale, U, V)
 
 
+@pytest.mark.parametrize("m,n", [(3000, 2500), (6000, 700)])
+def test_svd_large_shapes(lib, cuda, orc, m, n):
+    """Sizes beyond the other tests: several thousand rows, many panels, and a
+    tall shape whose row blocks per CTA exceed one warp's width."""
+    mode = "tf32x6" if _mode_available(lib, "tf32x6") else "blocked"
+    rng = np.random.default_rng(m + n)
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    s, U, V = run(lib, cuda, A, mode)
+    check_metrics(orc, A, s, U, V)
+
+
 def test_nonfinite_input_fails_loudly(lib, cuda):
     A = np.ones((16, 8), dtype=np.float32)
     A[3, 2] = np.nan
