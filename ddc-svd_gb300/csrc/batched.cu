@@ -187,7 +187,49 @@ __global__ void __launch_bounds__(kBatchThreads) batch_bidiag_kernel(const Batch
   }
 }
 
+// Applies reflectors j = jhi-1 ... 0 to kCW columns held in registers (lane
+// owns rows lane + 32 k).  Reflector j is the vector v(r) = vec(j, r) for
+// rows r >= j + shift (unit leading entry stored), zero above.
+constexpr int kRowsPerLane = 8;  // register-resident columns: rows <= 256
+constexpr int kCW = 4;           // columns per warp at a time
+template <typename VecFn>
+__device__ __forceinline__ void apply_reflectors_regs(float (&c)[kCW][kRowsPerLane], int rows, int jhi, int shift,
+                                                      const float* __restrict__ tau, VecFn vec, int lane) {
+  for (int j = jhi - 1; j >= 0; j--) {
+    const float t = tau[j];
+    if (t == 0.f) continue;
+    float u[kRowsPerLane];
+#pragma unroll
+    for (int k = 0; k < kRowsPerLane; k++) {
+      const int r = lane + 32 * k;
+      u[k] = (r >= j + shift && r < rows) ? vec(j, r) : 0.f;
+    }
+    float d[kCW];
+#pragma unroll
+    for (int q = 0; q < kCW; q++) {
+      float a = 0.f;
+#pragma unroll
+      for (int k = 0; k < kRowsPerLane; k++) a += u[k] * c[q][k];
+      d[q] = a;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < kCW; q++) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
+#pragma unroll
+    for (int q = 0; q < kCW; q++) {
+      const float f = t * d[q];
+#pragma unroll
+      for (int k = 0; k < kRowsPerLane; k++) c[q][k] -= f * u[k];
+    }
+  }
+}
+
 // U_core = Q [Y; 0], V_core = P X for one problem per CTA (multU / multV).
+// Problems up to 256 rows keep kCW columns per warp in registers and read the
+// reflectors from shared memory (or L1): one warp-wide reduction per
+// reflector for kCW columns at once.  Larger problems use the plain column
+// loop (one column per warp, in global memory).
 __global__ void __launch_bounds__(kBatchThreads) batch_backxform_kernel(const BatchTask* __restrict__ tasks,
                                                                         int ntask, const float* __restrict__ W,
                                                                         const float* __restrict__ tq,
@@ -206,35 +248,74 @@ __global__ void __launch_bounds__(kBatchThreads) batch_backxform_kernel(const Ba
     // core U / V of a transposed problem are the caller's V / U
     float* Uc = (T.trans ? V : U) + T.offU;
     float* Vc = (T.trans ? U : V) + T.offV;
-    // rows n..m-1 of [Y; 0]
-    for (int idx = threadIdx.x; idx < (m - n) * n; idx += blockDim.x) {
-      const int r = n + idx % (m - n), c = idx / (m - n);
-      Uc[r + (size_t)c * m] = 0.f;
-    }
     __syncthreads();
     const float* tauq = tq + T.offD;
     const float* taup = tp + T.offD;
-    for (int c = wid; c < n; c += nw) {
-      float* col = Uc + (size_t)c * m;
-      for (int j = n - 1; j >= 0; j--) {
-        const float t = tauq[j];
-        if (t == 0.f) continue;
-        const float* u = R + (size_t)j * m;  // unit stored at u[j]
-        float s = 0.f;
-        for (int r = j + lane; r < m; r += 32) s += u[r] * col[r];
-        s = warp_sum(s) * t;
-        for (int r = j + lane; r < m; r += 32) col[r] -= s * u[r];
-        __syncwarp();
+    if (m <= 32 * kRowsPerLane) {
+      for (int c0 = wid * kCW; c0 < n; c0 += nw * kCW) {
+        float c[kCW][kRowsPerLane];
+        // U: columns of [Y; 0] (rows >= n are zero), left reflectors n-1 .. 0
+#pragma unroll
+        for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+          for (int k = 0; k < kRowsPerLane; k++) {
+            const int r = lane + 32 * k, col = c0 + qq;
+            c[qq][k] = (col < n && r < n) ? Uc[r + (size_t)col * m] : 0.f;
+          }
+        apply_reflectors_regs(c, m, n, 0, tauq, [&](int j, int r) { return R[r + (size_t)j * m]; }, lane);
+#pragma unroll
+        for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+          for (int k = 0; k < kRowsPerLane; k++) {
+            const int r = lane + 32 * k, col = c0 + qq;
+            if (col < n && r < m) Uc[r + (size_t)col * m] = c[qq][k];
+          }
+        // V: columns of X, right reflectors n-3 .. 0 (row j of R from column j+1)
+#pragma unroll
+        for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+          for (int k = 0; k < kRowsPerLane; k++) {
+            const int r = lane + 32 * k, col = c0 + qq;
+            c[qq][k] = (col < n && r < n) ? Vc[r + (size_t)col * n] : 0.f;
+          }
+        apply_reflectors_regs(c, n, n - 2, 1, taup, [&](int j, int k) { return R[j + (size_t)k * m]; }, lane);
+#pragma unroll
+        for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+          for (int k = 0; k < kRowsPerLane; k++) {
+            const int r = lane + 32 * k, col = c0 + qq;
+            if (col < n && r < n) Vc[r + (size_t)col * n] = c[qq][k];
+          }
       }
-      float* vc = Vc + (size_t)c * n;
-      for (int j = n - 3; j >= 0; j--) {
-        const float t = taup[j];
-        if (t == 0.f) continue;
-        float s = 0.f;  // right reflector j: row j of R from column j+1 (unit stored)
-        for (int k = j + 1 + lane; k < n; k += 32) s += R[j + (size_t)k * m] * vc[k];
-        s = warp_sum(s) * t;
-        for (int k = j + 1 + lane; k < n; k += 32) vc[k] -= s * R[j + (size_t)k * m];
-        __syncwarp();
+    } else {
+      // rows n..m-1 of [Y; 0]
+      for (int idx = threadIdx.x; idx < (m - n) * n; idx += blockDim.x) {
+        const int r = n + idx % (m - n), c = idx / (m - n);
+        Uc[r + (size_t)c * m] = 0.f;
+      }
+      __syncthreads();
+      for (int c = wid; c < n; c += nw) {
+        float* col = Uc + (size_t)c * m;
+        for (int j = n - 1; j >= 0; j--) {
+          const float t = tauq[j];
+          if (t == 0.f) continue;
+          const float* u = R + (size_t)j * m;  // unit stored at u[j]
+          float s = 0.f;
+          for (int r = j + lane; r < m; r += 32) s += u[r] * col[r];
+          s = warp_sum(s) * t;
+          for (int r = j + lane; r < m; r += 32) col[r] -= s * u[r];
+          __syncwarp();
+        }
+        float* vc = Vc + (size_t)c * n;
+        for (int j = n - 3; j >= 0; j--) {
+          const float t = taup[j];
+          if (t == 0.f) continue;
+          float s = 0.f;  // right reflector j: row j of R from column j+1 (unit stored)
+          for (int k = j + 1 + lane; k < n; k += 32) s += R[j + (size_t)k * m] * vc[k];
+          s = warp_sum(s) * t;
+          for (int k = j + 1 + lane; k < n; k += 32) vc[k] -= s * R[j + (size_t)k * m];
+          __syncwarp();
+        }
       }
     }
     __syncthreads();

@@ -58,6 +58,7 @@ struct DcParams {
   double* L[2];
   double *ds, *zs, *hfs, *hls;
   double *dq, *zq, *fq, *lq;
+  float *dqf, *zqf;  // FP32 copies of dq, zq for the first phase of the root solver
   double *dd, *fd, *ld;  // deflated entries (ascending d)
   double *tau, *zh, *rS, *rF, *rL;
   int* org;
@@ -262,6 +263,7 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
   for (int k = lo; k < hi; k++) {
     if (!p.defl[slot + k]) {
       p.dq[slot + off] = ds[k]; p.zq[slot + off] = zs[k];
+      p.dqf[slot + off] = (float)ds[k]; p.zqf[slot + off] = (float)zs[k];
       p.fq[slot + off] = hfs[k]; p.lq[slot + off] = hls[k];
       zzl += zs[k] * zs[k];
       off++;
@@ -295,59 +297,103 @@ __device__ __forceinline__ void sec_eval(int q, const double* d, const double* z
   f = 1.0 + psi + phi;
 }
 
+// FP32 twin of sec_eval on the FP32 copies of d and z.
+__device__ __forceinline__ void sec_eval32(int q, const float* d, const float* z, float dorg, float tau, int split,
+                                           int lane, float& f, float& psi, float& dpsi, float& phi, float& dphi) {
+  float ps = 0.f, dps = 0.f, ph = 0.f, dph = 0.f;
+  for (int j = lane; j < q; j += 32) {
+    const float dj = d[j];
+    const float del = (dj - dorg) * (dj + dorg) - tau;
+    const float tt = z[j] / del;
+    if (j <= split) { ps += z[j] * tt; dps += tt * tt; }
+    else { ph += z[j] * tt; dph += tt * tt; }
+  }
+  psi = warp_sum(ps); dpsi = warp_sum(dps); phi = warp_sum(ph); dphi = warp_sum(dph);
+  f = 1.f + psi + phi;
+}
+
+// One safeguarded step of the root iteration (two-pole rational model for an
+// interior root, one pole for the last root), shared by the FP32 and FP64
+// phases.  Returns true when converged.
+template <typename T>
+__device__ __forceinline__ bool sec_step(bool last, T f, T psi, T dpsi, T phi, T dphi, T da0, T db0, T eps,
+                                         T& lo, T& hi, T& tau) {
+  const T err = last ? T(8) * (T(1) + fabs(psi)) + fabs(tau) * dpsi
+                     : T(8) * (T(1) + fabs(psi) + fabs(phi)) + fabs(tau) * (dpsi + dphi);
+  if (fabs(f) <= eps * err) return true;
+  if (f < T(0)) lo = tau; else hi = tau;
+  if (hi - lo <= T(4) * eps * fmax(fabs(lo), fabs(hi))) return true;
+  T tn;
+  if (last) {
+    const T da = -tau;
+    const T s1 = da * da * dpsi;
+    const T c = f - s1 / da;
+    tn = (c != T(0)) ? tau + da + s1 / c : T(0.5) * (lo + hi);
+  } else {
+    const T da = da0 - tau, db = db0 - tau;
+    const T s1 = da * da * dpsi, s2 = db * db * dphi;
+    const T c = f - s1 / da - s2 / db;
+    const T aq = c, bq = c * (da + db) + s1 + s2, cq = da * db * f;
+    const T disc = sqrt(fabs(bq * bq - T(4) * aq * cq));
+    T eta;
+    if (aq == T(0)) eta = cq / bq;
+    else if (bq <= T(0)) eta = (bq - disc) / (T(2) * aq);
+    else eta = T(2) * cq / (bq + disc);
+    tn = tau + eta;
+  }
+  if (!(tn > lo && tn < hi)) tn = T(0.5) * (lo + hi);
+  tau = tn;
+  return false;
+}
+
 // Root i of the node's secular equation; returns origin (local index) and tau.
-__device__ bool sec_root(int q, const double* d, const double* z, double zz, int i, int lane,
-                         int* origin, double* tau_out) {
+// Phase 1 iterates in FP32 (GB300's FP64 pipe is narrow and these sums are
+// the D&C's dominant cost) to about single precision; phase 2 continues in
+// FP64 from that point inside the FP64 bracket, typically for 1-3 steps, to
+// full accuracy.  A poor FP32 start (clustered poles, range trouble) only
+// costs more FP64 steps: the FP64 phase keeps its own bisection safeguard.
+__device__ bool sec_root(int q, const double* d, const double* z, const float* df, const float* zf, double zz,
+                         int i, int lane, int* origin, double* tau_out) {
   double f, psi, dpsi, phi, dphi;
-  bool conv = false;
-  if (i < q - 1) {
+  const bool last = (i == q - 1);
+  int o;
+  double lo, hi, tau, da0 = 0.0, db0 = 0.0;
+  if (!last) {
     const double dd = (d[i + 1] - d[i]) * (d[i + 1] + d[i]);
     sec_eval(q, d, z, d[i], 0.5 * dd, i, lane, f, psi, dpsi, phi, dphi);
-    const int o = (f >= 0.0) ? i : i + 1;
+    o = (f >= 0.0) ? i : i + 1;
     const double dorg = d[o];
-    double lo, hi, tau;
     if (o == i) { lo = 0.0; hi = 0.5 * dd; tau = 0.5 * dd; }
     else { lo = -0.5 * dd; hi = 0.0; tau = -0.5 * dd; }
-    const double da0 = (d[i] - dorg) * (d[i] + dorg);
-    const double db0 = (d[i + 1] - dorg) * (d[i + 1] + dorg);
-    for (int it = 0; it < kSecMaxIt; it++) {
-      sec_eval(q, d, z, dorg, tau, i, lane, f, psi, dpsi, phi, dphi);
-      const double err = 8.0 * (1.0 + fabs(psi) + fabs(phi)) + fabs(tau) * (dpsi + dphi);
-      if (fabs(f) <= DBL_EPSILON * err) { conv = true; break; }
-      if (f < 0.0) lo = tau; else hi = tau;
-      if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) { conv = true; break; }
-      const double da = da0 - tau, db = db0 - tau;
-      const double s1 = da * da * dpsi, s2 = db * db * dphi;
-      const double c = f - s1 / da - s2 / db;
-      const double aq = c, bq = c * (da + db) + s1 + s2, cq = da * db * f;
-      const double disc = sqrt(fabs(bq * bq - 4.0 * aq * cq));
-      double eta;
-      if (aq == 0.0) eta = cq / bq;
-      else if (bq <= 0.0) eta = (bq - disc) / (2.0 * aq);
-      else eta = 2.0 * cq / (bq + disc);
-      double tn = tau + eta;
-      if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
-      tau = tn;
-    }
-    *origin = o;
-    *tau_out = tau;
-    return conv;
+    da0 = (d[i] - dorg) * (d[i] + dorg);
+    db0 = (d[i + 1] - dorg) * (d[i + 1] + dorg);
+  } else {
+    o = q - 1;
+    lo = 0.0; hi = zz; tau = 0.5 * zz;
   }
-  const int o = q - 1;
   const double dorg = d[o];
-  double lo = 0.0, hi = zz, tau = 0.5 * zz;
+  const int split = last ? q - 1 : i;
+  // ---- phase 1: FP32
+  {
+    float lo32 = (float)lo, hi32 = (float)hi, t32 = (float)tau;
+    const float d32 = df[o], da32 = (float)da0, db32 = (float)db0;
+    for (int it = 0; it < 40; it++) {
+      float f3, ps3, dps3, ph3, dph3;
+      sec_eval32(q, df, zf, d32, t32, split, lane, f3, ps3, dps3, ph3, dph3);
+      if (!(fabsf(f3) < INFINITY) || !(dps3 < INFINITY) || !(dph3 < INFINITY)) break;
+      if (sec_step<float>(last, f3, ps3, dps3, ph3, dph3, da32, db32, 4.f * FLT_EPSILON, lo32, hi32, t32)) break;
+    }
+    const double t = (double)t32;
+    if (t > lo && t < hi) tau = t;
+  }
+  // ---- phase 2: FP64
+  bool conv = false;
   for (int it = 0; it < kSecMaxIt; it++) {
-    sec_eval(q, d, z, dorg, tau, q - 1, lane, f, psi, dpsi, phi, dphi);
-    const double err = 8.0 * (1.0 + fabs(psi)) + fabs(tau) * dpsi;
-    if (fabs(f) <= DBL_EPSILON * err) { conv = true; break; }
-    if (f < 0.0) lo = tau; else hi = tau;
-    if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) { conv = true; break; }
-    const double da = -tau;
-    const double s1 = da * da * dpsi;
-    const double c = f - s1 / da;
-    double tn = (c != 0.0) ? tau + da + s1 / c : 0.5 * (lo + hi);
-    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
-    tau = tn;
+    sec_eval(q, d, z, dorg, tau, split, lane, f, psi, dpsi, phi, dphi);
+    if (sec_step<double>(last, f, psi, dpsi, phi, dphi, da0, db0, DBL_EPSILON, lo, hi, tau)) {
+      conv = true;
+      break;
+    }
   }
   *origin = o;
   *tau_out = tau;
@@ -407,6 +453,23 @@ __device__ void dc_finish_node(const DcParams& p, int node, int par, bool rows, 
   }
 }
 
+#ifdef DDCSVD_PHASE_TRACE
+__device__ unsigned long long g_dc_trace[64 * 16];
+#endif
+// phase marks of CTA 0, one row per depth (slots: 0 start, 1 after P1, 2 after
+// its barrier, 3 after P2, 4 barrier, 5 P3, 6 barrier, 7 P4, 8 barrier, 9 P5,
+// 10 barrier)
+#ifdef DDCSVD_PHASE_TRACE
+#define DMARK(slot)                                                               \
+  do {                                                                            \
+    if (blockIdx.x == 0 && threadIdx.x == 0 && d < 64) g_dc_trace[d * 16 + (slot)] = global_ns(); \
+  } while (0)
+#else
+#define DMARK(slot) \
+  do {              \
+  } while (0)
+#endif
+
 __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
   __shared__ int shi[40];
   __shared__ double shd[40];
@@ -417,6 +480,7 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
   for (int d = p.maxdepth; d >= 0; d--) {
     const int par = d & 1;
     const bool rows = d > 0;
+    DMARK(0);
     // ---- P1a leaves of this depth (thread each)
     for (int k = p.depth_start[d] + gt; k < p.depth_start[d + 1]; k += nthreads) {
       if (p.nd_K[k] >= 0) continue;
@@ -433,7 +497,9 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       if (d > 0 && !grid_sync(p.bar, p.P, p.st, 600 + d)) return;
       continue;
     }
+    DMARK(1);
     if (!grid_sync(p.bar, p.P, p.st, 100 + d)) return;
+    DMARK(2);
     // ---- P2 secular roots (warp per root)
     for (int pos = gw; pos < p.N; pos += nwarps) {
       const int node = find_node(p, d, pos);
@@ -442,7 +508,7 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       if (i >= q) continue;
       int o;
       double tau;
-      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.zz[node], i, lane, &o, &tau);
+      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, lane, &o, &tau);
       if (lane == 0) {
         p.org[pos] = o;
         p.tau[pos] = tau;
@@ -451,8 +517,10 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
         if (!ok) set_error(p.st, DDCSVD_ERR_NOCONV, pos);
       }
     }
+    DMARK(3);
     if (rows) {
       if (!grid_sync(p.bar, p.P, p.st, 200 + d)) return;
+      DMARK(4);
       // ---- P3 z-hat (warp per component)
       for (int pos = gw; pos < p.N; pos += nwarps) {
         const int node = find_node(p, d, pos);
@@ -479,7 +547,9 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
           p.zh[pos] = (p.zq[pos] >= 0.0) ? a : -a;
         }
       }
+      DMARK(5);
       if (!grid_sync(p.bar, p.P, p.st, 300 + d)) return;
+      DMARK(6);
       // ---- P4 rows of the merged right vectors (warp per root)
       for (int pos = gw; pos < p.N; pos += nwarps) {
         const int node = find_node(p, d, pos);
@@ -505,11 +575,15 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
         }
       }
     }
+    DMARK(7);
     if (!grid_sync(p.bar, p.P, p.st, 400 + d)) return;
+    DMARK(8);
     // ---- P5 final merge + normalisation (CTA per node)
     for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
       dc_finish_node(p, p.depth_merge[mi], par, rows, shd);
+    DMARK(9);
     if (d > 0 && !grid_sync(p.bar, p.P, p.st, 500 + d)) return;
+    DMARK(10);
   }
 }
 
@@ -585,6 +659,7 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
   const int maxnodes = 2 * N + 8;
   int* scratch_ints = a.take<int>((size_t)N * 2 + maxnodes);
   double* dbl = a.take<double>((size_t)N * 25 + 3 * (size_t)maxnodes + 8);
+  float* flt = a.take<float>((size_t)N * 2 + 8);
   GridBarrier* bar = a.take<GridBarrier>(4);
   if (plan_only) return DDCSVD_OK;
   const int nnodes = H->nnodes, md = H->maxdepth;
@@ -611,6 +686,7 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
   p.dd = q; q += N; p.fd = q; q += N; p.ld = q; q += N;
   p.tau = q; q += N; p.zh = q; q += N; p.rS = q; q += N; p.rF = q; q += N; p.rL = q; q += N;
   p.zz = q; q += maxnodes; p.phi = q; q += maxnodes; p.psi = q; q += maxnodes;
+  p.dqf = flt; p.zqf = flt + N;
   p.out = sigma;
   p.bar = bar;
   p.st = ctx->d_status;
@@ -636,3 +712,9 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
 }
 
 }  // namespace ddcsvd
+
+#ifdef DDCSVD_PHASE_TRACE
+extern "C" int ddcsvd_dc_trace_read(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, ddcsvd::g_dc_trace, sizeof(ddcsvd::g_dc_trace));
+}
+#endif
