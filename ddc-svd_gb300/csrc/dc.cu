@@ -51,6 +51,7 @@ struct DcParams {
   const int* depth_start;  // [maxdepth + 2]
   const int* depth_merge;  // merge-node ids sorted by depth then slot
   const int* dm_start;     // [maxdepth + 2] ranges into depth_merge
+  const int* dgroup;       // [maxdepth + 2] lanes per root at each depth (1..32)
   const double* b1;
   const double* b2;
   double* sig[2];
@@ -158,6 +159,45 @@ __device__ double block_sumd(double v, double* sh) {
   return r;
 }
 
+// Cooperation policies for the per-node phases: a whole CTA for large nodes,
+// one warp for nodes of at most kWarpNode entries (a batch forest has
+// thousands of those per depth; a CTA each would mostly wait at barriers).
+constexpr int kWarpNode = 64;
+struct CtaGroup {
+  int* shi;
+  double* shd;
+  __device__ int rank() const { return threadIdx.x; }
+  __device__ int size() const { return blockDim.x; }
+  __device__ void sync() const { __syncthreads(); }
+  __device__ double max(double v) const { return block_max(v, shd); }
+  __device__ double sum(double v) const { return block_sumd(v, shd); }
+  __device__ int exscan(int v, int* tot) const { return block_exscan(v, shi, tot); }
+  __device__ int any(int v) const { return __syncthreads_or(v); }
+};
+struct WarpGroup {
+  __device__ int rank() const { return threadIdx.x & 31; }
+  __device__ int size() const { return 32; }
+  __device__ void sync() const { __syncwarp(); }
+  __device__ double max(double v) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+  }
+  __device__ double sum(double v) const { return warp_sum(v); }
+  __device__ int exscan(int v, int* tot) const {
+    const int lane = threadIdx.x & 31;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    *tot = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+  }
+  __device__ int any(int v) const { return __any_sync(0xffffffffu, v); }
+};
+
 // number of a[0..n) < v (strict) or <= v
 __device__ __forceinline__ int count_lt(const double* a, int n, double v) {
   int lo = 0, hi = n;
@@ -171,8 +211,9 @@ __device__ __forceinline__ int count_le(const double* a, int n, double v) {
 }
 
 // ---------------------------------------------------------------- P1 merge set-up
-__device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, double* shd) {
-  const int t = threadIdx.x;
+template <class Grp>
+__device__ void dc_setup_node(const DcParams& p, int node, int par, const Grp& grp) {
+  const int t = grp.rank(), nt = grp.size();
   const int nn = p.nd_nn[node], slot = p.nd_slot[node], K = p.nd_K[node], r0 = p.nd_r0[node];
   const int c1 = p.nd_c1[node], c2 = p.nd_c2[node];
   const int n1 = K, n2 = nn - K - 1;
@@ -198,26 +239,26 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
     ds[0] = 0.0; zs[0] = r; hfs[0] = c0 * phi1; hls[0] = s0 * psi2;
     zmax = fabs(r);
   }
-  for (int k = t; k < n1; k += blockDim.x) {
+  for (int k = t; k < n1; k += nt) {
     const double v = s1[k];
     const int pos = 1 + k + count_lt(s2, n2, v);
     const double z = bk1 * l1[k];
     ds[pos] = v; zs[pos] = z; hfs[pos] = f1[k]; hls[pos] = 0.0;
     dmax = fmax(dmax, fabs(v)); zmax = fmax(zmax, fabs(z));
   }
-  for (int k = t; k < n2; k += blockDim.x) {
+  for (int k = t; k < n2; k += nt) {
     const double v = s2[k];
     const int pos = 1 + k + count_le(s1, n1, v);
     const double z = bk2 * f2[k];
     ds[pos] = v; zs[pos] = z; hfs[pos] = 0.0; hls[pos] = l2[k];
     dmax = fmax(dmax, fabs(v)); zmax = fmax(zmax, fabs(z));
   }
-  dmax = block_max(dmax, shd);
-  zmax = block_max(zmax, shd);
+  dmax = grp.max(dmax);
+  zmax = grp.max(zmax);
   const double tol = 8.0 * DBL_EPSILON * fmax(dmax, zmax);
-  __syncthreads();
+  grp.sync();
   // deflation 1: negligible z
-  const int per = ceil_div(nn, blockDim.x);
+  const int per = ceil_div(nn, nt);
   const int lo = min(nn, t * per), hi = min(nn, lo + per);
   int cnt = 0;
   for (int k = lo; k < hi; k++) {
@@ -226,18 +267,16 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
     cnt += !dfl;
   }
   int tot;
-  int off = block_exscan(cnt, shi, &tot);
+  int off = grp.exscan(cnt, &tot);
   // positions of non-deflated entries -> compacted arrays (tentative)
   for (int k = lo; k < hi; k++)
     if (!p.defl[slot + k]) { p.dq[slot + off] = ds[k]; off++; }
-  __syncthreads();
+  grp.sync();
   // deflation 2 needed?  (adjacent non-deflated values within tol)
-  __shared__ int need2;
-  if (t == 0) need2 = 0;
-  __syncthreads();
-  for (int k = 1 + t; k < tot; k += blockDim.x)
-    if (p.dq[slot + k] - p.dq[slot + k - 1] <= tol) need2 = 1;
-  __syncthreads();
+  int close = 0;
+  for (int k = 1 + t; k < tot; k += nt)
+    if (p.dq[slot + k] - p.dq[slot + k - 1] <= tol) close = 1;
+  const int need2 = grp.any(close);
   if (need2 && t == 0) {
     int prev = -1;
     for (int k = 0; k < nn; k++) {
@@ -253,11 +292,11 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
       prev = k;
     }
   }
-  __syncthreads();
+  grp.sync();
   // final compaction: non-deflated -> dq/zq/fq/lq, deflated -> dd/fd/ld
   cnt = 0;
   for (int k = lo; k < hi; k++) cnt += !p.defl[slot + k];
-  off = block_exscan(cnt, shi, &tot);
+  off = grp.exscan(cnt, &tot);
   int doff = lo - off;  // deflated entries before this thread's range
   double zzl = 0.0;
   for (int k = lo; k < hi; k++) {
@@ -272,7 +311,7 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
       doff++;
     }
   }
-  double zz = block_sumd(zzl, shd);
+  double zz = grp.sum(zzl);
   if (t == 0) {
     p.nq[node] = tot;
     p.zz[node] = zz;
@@ -281,34 +320,62 @@ __device__ void dc_setup_node(const DcParams& p, int node, int par, int* shi, do
   }
 }
 
-// ---------------------------------------------------------------- secular roots (warp)
+// ---------------------------------------------------------------- lane groups
+// The per-root phases run one group of G lanes (G = 1, 2, ..., 32, chosen per
+// depth from its largest node) per root: small nodes of a batch forest would
+// otherwise leave most of a warp idle and pay five shuffle rounds per sum.
+struct LaneGroup {
+  int G;          // lanes per group
+  int lg;         // lane within the group
+  unsigned mask;  // lanes of this group within the warp
+};
+__device__ __forceinline__ LaneGroup make_group(int G, int lane) {
+  LaneGroup g;
+  g.G = G;
+  g.lg = lane & (G - 1);
+  g.mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  return g;
+}
+template <typename T>
+__device__ __forceinline__ T gsum(T v, const LaneGroup& g) {
+  for (int o = g.G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(g.mask, v, o);
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T gprod(T v, const LaneGroup& g) {
+  for (int o = g.G >> 1; o > 0; o >>= 1) v *= __shfl_xor_sync(g.mask, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------- secular roots
 __device__ __forceinline__ void sec_eval(int q, const double* d, const double* z, double dorg,
-                                         double tau, int split, int lane, double& f, double& psi,
+                                         double tau, int split, const LaneGroup& g, double& f, double& psi,
                                          double& dpsi, double& phi, double& dphi) {
   double ps = 0.0, dps = 0.0, ph = 0.0, dph = 0.0;
-  for (int j = lane; j < q; j += 32) {
+  for (int j = g.lg; j < q; j += g.G) {
     const double dj = d[j];
     const double del = (dj - dorg) * (dj + dorg) - tau;
     const double tt = z[j] / del;
     if (j <= split) { ps += z[j] * tt; dps += tt * tt; }
     else { ph += z[j] * tt; dph += tt * tt; }
   }
-  psi = warp_sum(ps); dpsi = warp_sum(dps); phi = warp_sum(ph); dphi = warp_sum(dph);
+  psi = gsum(ps, g); dpsi = gsum(dps, g); phi = gsum(ph, g); dphi = gsum(dph, g);
   f = 1.0 + psi + phi;
 }
 
 // FP32 twin of sec_eval on the FP32 copies of d and z.
 __device__ __forceinline__ void sec_eval32(int q, const float* d, const float* z, float dorg, float tau, int split,
-                                           int lane, float& f, float& psi, float& dpsi, float& phi, float& dphi) {
+                                           const LaneGroup& g, float& f, float& psi, float& dpsi, float& phi,
+                                           float& dphi) {
   float ps = 0.f, dps = 0.f, ph = 0.f, dph = 0.f;
-  for (int j = lane; j < q; j += 32) {
+  for (int j = g.lg; j < q; j += g.G) {
     const float dj = d[j];
     const float del = (dj - dorg) * (dj + dorg) - tau;
     const float tt = z[j] / del;
     if (j <= split) { ps += z[j] * tt; dps += tt * tt; }
     else { ph += z[j] * tt; dph += tt * tt; }
   }
-  psi = warp_sum(ps); dpsi = warp_sum(dps); phi = warp_sum(ph); dphi = warp_sum(dph);
+  psi = gsum(ps, g); dpsi = gsum(dps, g); phi = gsum(ph, g); dphi = gsum(dph, g);
   f = 1.f + psi + phi;
 }
 
@@ -353,14 +420,14 @@ __device__ __forceinline__ bool sec_step(bool last, T f, T psi, T dpsi, T phi, T
 // full accuracy.  A poor FP32 start (clustered poles, range trouble) only
 // costs more FP64 steps: the FP64 phase keeps its own bisection safeguard.
 __device__ bool sec_root(int q, const double* d, const double* z, const float* df, const float* zf, double zz,
-                         int i, int lane, int* origin, double* tau_out) {
+                         int i, const LaneGroup& g, int* origin, double* tau_out) {
   double f, psi, dpsi, phi, dphi;
   const bool last = (i == q - 1);
   int o;
   double lo, hi, tau, da0 = 0.0, db0 = 0.0;
   if (!last) {
     const double dd = (d[i + 1] - d[i]) * (d[i + 1] + d[i]);
-    sec_eval(q, d, z, d[i], 0.5 * dd, i, lane, f, psi, dpsi, phi, dphi);
+    sec_eval(q, d, z, d[i], 0.5 * dd, i, g, f, psi, dpsi, phi, dphi);
     o = (f >= 0.0) ? i : i + 1;
     const double dorg = d[o];
     if (o == i) { lo = 0.0; hi = 0.5 * dd; tau = 0.5 * dd; }
@@ -379,7 +446,7 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
     const float d32 = df[o], da32 = (float)da0, db32 = (float)db0;
     for (int it = 0; it < 40; it++) {
       float f3, ps3, dps3, ph3, dph3;
-      sec_eval32(q, df, zf, d32, t32, split, lane, f3, ps3, dps3, ph3, dph3);
+      sec_eval32(q, df, zf, d32, t32, split, g, f3, ps3, dps3, ph3, dph3);
       if (!(fabsf(f3) < INFINITY) || !(dps3 < INFINITY) || !(dph3 < INFINITY)) break;
       if (sec_step<float>(last, f3, ps3, dps3, ph3, dph3, da32, db32, 4.f * FLT_EPSILON, lo32, hi32, t32)) break;
     }
@@ -389,7 +456,7 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
   // ---- phase 2: FP64
   bool conv = false;
   for (int it = 0; it < kSecMaxIt; it++) {
-    sec_eval(q, d, z, dorg, tau, split, lane, f, psi, dpsi, phi, dphi);
+    sec_eval(q, d, z, dorg, tau, split, g, f, psi, dpsi, phi, dphi);
     if (sec_step<double>(last, f, psi, dpsi, phi, dphi, da0, db0, DBL_EPSILON, lo, hi, tau)) {
       conv = true;
       break;
@@ -415,8 +482,9 @@ __device__ __forceinline__ int find_node(const DcParams& p, int d, int pos) {
 }
 
 // ---------------------------------------------------------------- P5 final merge
-__device__ void dc_finish_node(const DcParams& p, int node, int par, bool rows, double* shd) {
-  const int t = threadIdx.x;
+template <class Grp>
+__device__ void dc_finish_node(const DcParams& p, int node, int par, bool rows, const Grp& grp) {
+  const int t = grp.rank(), nt = grp.size();
   const int nn = p.nd_nn[node], slot = p.nd_slot[node];
   const int q = p.nq[node], nd = nn - q;
   const double* rs = p.rS + slot;
@@ -424,29 +492,29 @@ __device__ void dc_finish_node(const DcParams& p, int node, int par, bool rows, 
   double* sig = p.sig[par] + slot;
   double* F = p.F[par] + slot;
   double* L = p.L[par] + slot;
-  for (int k = t; k < q; k += blockDim.x) {
+  for (int k = t; k < q; k += nt) {
     const int pos = k + count_lt(dd, nd, rs[k]);
     sig[pos] = rs[k];
     if (rows) { F[pos] = p.rF[slot + k]; L[pos] = p.rL[slot + k]; }
   }
-  for (int k = t; k < nd; k += blockDim.x) {
+  for (int k = t; k < nd; k += nt) {
     const int pos = k + count_le(rs, q, dd[k]);
     sig[pos] = dd[k];
     if (rows) { F[pos] = p.fd[slot + k]; L[pos] = p.ld[slot + k]; }
   }
   if (!rows) return;
-  __syncthreads();
+  grp.sync();
   double sf = 0.0, sl = 0.0;
-  for (int k = t; k < nn; k += blockDim.x) { sf += F[k] * F[k]; sl += L[k] * L[k]; }
-  sf = block_sumd(sf, shd);
-  sl = block_sumd(sl, shd);
+  for (int k = t; k < nn; k += nt) { sf += F[k] * F[k]; sl += L[k] * L[k]; }
+  sf = grp.sum(sf);
+  sl = grp.sum(sl);
   const double ph = p.phi[node], ps = p.psi[node];
   const double nf = sqrt(sf + ph * ph), nl = sqrt(sl + ps * ps);
-  for (int k = t; k < nn; k += blockDim.x) {
+  for (int k = t; k < nn; k += nt) {
     if (nf > 0.0) F[k] /= nf;
     if (nl > 0.0) L[k] /= nl;
   }
-  __syncthreads();
+  grp.sync();
   if (t == 0) {
     if (nf > 0.0) p.phi[node] = ph / nf;
     if (nl > 0.0) p.psi[node] = ps / nl;
@@ -490,9 +558,15 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       p.phi[k] = phi;
       p.psi[k] = psi;
     }
-    // ---- P1b merge set-up (CTA per node)
-    for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
-      dc_setup_node(p, p.depth_merge[mi], par, shi, shd);
+    // ---- P1b merge set-up: CTA per large node, warp per small node
+    {
+      const CtaGroup cg{shi, shd};
+      for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
+        if (p.nd_nn[p.depth_merge[mi]] > kWarpNode) dc_setup_node(p, p.depth_merge[mi], par, cg);
+      const WarpGroup wg;
+      for (int mi = p.dm_start[d] + gw; mi < p.dm_start[d + 1]; mi += nwarps)
+        if (p.nd_nn[p.depth_merge[mi]] <= kWarpNode) dc_setup_node(p, p.depth_merge[mi], par, wg);
+    }
     if (p.dm_start[d + 1] == p.dm_start[d]) {  // only leaves at this depth
       if (d > 0 && !grid_sync(p.bar, p.P, p.st, 600 + d)) return;
       continue;
@@ -500,16 +574,18 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
     DMARK(1);
     if (!grid_sync(p.bar, p.P, p.st, 100 + d)) return;
     DMARK(2);
-    // ---- P2 secular roots (warp per root)
-    for (int pos = gw; pos < p.N; pos += nwarps) {
+    // ---- P2 secular roots (lane group per root)
+    const LaneGroup g = make_group(p.dgroup[d], lane);
+    const int gid = gt / g.G, ngroups = nthreads / g.G;
+    for (int pos = gid; pos < p.N; pos += ngroups) {
       const int node = find_node(p, d, pos);
       if (node < 0) continue;
       const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
       if (i >= q) continue;
       int o;
       double tau;
-      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, lane, &o, &tau);
-      if (lane == 0) {
+      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau);
+      if (g.lg == 0) {
         p.org[pos] = o;
         p.tau[pos] = tau;
         const double dorg = p.dq[slot + o];
@@ -521,8 +597,8 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
     if (rows) {
       if (!grid_sync(p.bar, p.P, p.st, 200 + d)) return;
       DMARK(4);
-      // ---- P3 z-hat (warp per component)
-      for (int pos = gw; pos < p.N; pos += nwarps) {
+      // ---- P3 z-hat (lane group per component)
+      for (int pos = gid; pos < p.N; pos += ngroups) {
         const int node = find_node(p, d, pos);
         if (node < 0) continue;
         const int slot = p.nd_slot[node], j = pos - slot, q = p.nq[node];
@@ -532,15 +608,15 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
         const int* org = p.org + slot;
         const double dj = dq[j];
         double prod = 1.0;
-        for (int k = lane; k < q - 1; k += 32) {
+        for (int k = g.lg; k < q - 1; k += g.G) {
           const int ok = org[k];
           const double num = tau[k] - (dj - dq[ok]) * (dj + dq[ok]);
           const int kk = (k < j) ? k : k + 1;
           const double den = (dq[kk] - dj) * (dq[kk] + dj);
           prod *= num / den;
         }
-        prod = warp_prod(prod);
-        if (lane == 0) {
+        prod = gprod(prod, g);
+        if (g.lg == 0) {
           const int ol = org[q - 1];
           prod *= tau[q - 1] - (dj - dq[ol]) * (dj + dq[ol]);
           const double a = sqrt(fabs(prod));
@@ -550,8 +626,8 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       DMARK(5);
       if (!grid_sync(p.bar, p.P, p.st, 300 + d)) return;
       DMARK(6);
-      // ---- P4 rows of the merged right vectors (warp per root)
-      for (int pos = gw; pos < p.N; pos += nwarps) {
+      // ---- P4 rows of the merged right vectors (lane group per root)
+      for (int pos = gid; pos < p.N; pos += ngroups) {
         const int node = find_node(p, d, pos);
         if (node < 0) continue;
         const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
@@ -559,7 +635,7 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
         const double* dq = p.dq + slot;
         const double dorg = dq[p.org[pos]], ti = p.tau[pos];
         double nv = 0.0, sf = 0.0, sl = 0.0;
-        for (int j = lane; j < q; j += 32) {
+        for (int j = g.lg; j < q; j += g.G) {
           const double dj = dq[j];
           const double del = (dj - dorg) * (dj + dorg) - ti;
           const double v = p.zh[slot + j] / del;
@@ -567,8 +643,8 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
           sf += v * p.fq[slot + j];
           sl += v * p.lq[slot + j];
         }
-        nv = warp_sum(nv); sf = warp_sum(sf); sl = warp_sum(sl);
-        if (lane == 0) {
+        nv = gsum(nv, g); sf = gsum(sf, g); sl = gsum(sl, g);
+        if (g.lg == 0) {
           nv = sqrt(nv);
           p.rF[pos] = sf / nv;
           p.rL[pos] = sl / nv;
@@ -579,8 +655,14 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
     if (!grid_sync(p.bar, p.P, p.st, 400 + d)) return;
     DMARK(8);
     // ---- P5 final merge + normalisation (CTA per node)
-    for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
-      dc_finish_node(p, p.depth_merge[mi], par, rows, shd);
+    {
+      const CtaGroup cg{shi, shd};
+      for (int mi = p.dm_start[d] + blockIdx.x; mi < p.dm_start[d + 1]; mi += gridDim.x)
+        if (p.nd_nn[p.depth_merge[mi]] > kWarpNode) dc_finish_node(p, p.depth_merge[mi], par, rows, cg);
+      const WarpGroup wg;
+      for (int mi = p.dm_start[d] + gw; mi < p.dm_start[d + 1]; mi += nwarps)
+        if (p.nd_nn[p.depth_merge[mi]] <= kWarpNode) dc_finish_node(p, p.depth_merge[mi], par, rows, wg);
+    }
     DMARK(9);
     if (d > 0 && !grid_sync(p.bar, p.P, p.st, 500 + d)) return;
     DMARK(10);
@@ -643,12 +725,21 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
     for (int i = ds[d]; i < ds[d + 1]; i++) if (K[i] >= 0) dmerge.push_back(i);
   }
   dms[md + 1] = (int)dmerge.size();
+  // lanes per root at each depth: about 8 terms of the largest node per lane
+  std::vector<int> dgroup(md + 2, 1);
+  for (int d = 0; d <= md; d++) {
+    int mx = 0;
+    for (int k = dms[d]; k < dms[d + 1]; k++) mx = std::max(mx, nn[dmerge[k]]);
+    int G = 1;
+    while (G < 32 && G * 8 < mx) G <<= 1;
+    dgroup[d] = G;
+  }
   H.nnodes = nnodes;
   H.maxdepth = md;
   H.ndm = (int)dmerge.size();
   H.ints.clear();
   auto app = [&](const std::vector<int>& v) { H.ints.insert(H.ints.end(), v.begin(), v.end()); };
-  app(r0); app(nn); app(slot); app(K); app(c1); app(c2); app(ds); app(dms); app(dmerge);
+  app(r0); app(nn); app(slot); app(K); app(c1); app(c2); app(ds); app(dms); app(dmerge); app(dgroup);
 }
 
 size_t dc_max_ints(int N) { return 9 * (size_t)(2 * N + 8) + 2 * 64 + 16; }
@@ -675,6 +766,7 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
   p.depth_start = dints + o; o += md + 2;
   p.dm_start = dints + o; o += md + 2;
   p.depth_merge = dints + o; o += H->ndm;
+  p.dgroup = dints + o; o += md + 2;
   p.org = scratch_ints;
   p.defl = scratch_ints + N;
   p.nq = scratch_ints + 2 * (size_t)N;
