@@ -427,6 +427,9 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
   double lo, hi, tau, da0 = 0.0, db0 = 0.0;
   if (!last) {
     const double dd = (d[i + 1] - d[i]) * (d[i + 1] + d[i]);
+    // origin = nearer pole, from the sign of f at the midpoint (FP64: an FP32
+    // sign taken at an FP32-rounded midpoint picked the wrong half on close
+    // poles of a batch forest)
     sec_eval(q, d, z, d[i], 0.5 * dd, i, g, f, psi, dpsi, phi, dphi);
     o = (f >= 0.0) ? i : i + 1;
     const double dorg = d[o];
@@ -453,11 +456,18 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
     const double t = (double)t32;
     if (t > lo && t < hi) tau = t;
   }
-  // ---- phase 2: FP64
+  // ---- phase 2: FP64.  A step below 1e-10 |tau| is accepted without another
+  // evaluation: the rational model converges at least quadratically, so the
+  // remaining error is far below FP64 resolution.
   bool conv = false;
   for (int it = 0; it < kSecMaxIt; it++) {
     sec_eval(q, d, z, dorg, tau, split, g, f, psi, dpsi, phi, dphi);
+    const double prev = tau;
     if (sec_step<double>(last, f, psi, dpsi, phi, dphi, da0, db0, DBL_EPSILON, lo, hi, tau)) {
+      conv = true;
+      break;
+    }
+    if (fabs(tau - prev) <= 1e-10 * fabs(tau)) {
       conv = true;
       break;
     }

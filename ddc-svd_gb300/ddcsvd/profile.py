@@ -1,6 +1,10 @@
 """Runs SVDs of one seeded matrix through the device API, for profilers.
 
     python -m ddcsvd.profile --size 4096 --mode tf32x6 --reps 2 [--kind graded|uniform]
+    python -m ddcsvd.profile --batched 2048 --reps 2
+
+--batched runs the seeded uneven batch instead (rng(3): m ~ U{16..256},
+n ~ U{8..m}, entries U[-1, 1]) through ddcsvd_svd_batched_f32_device.
 
 The first repetition warms up (workspace allocation, module load); each
 repetition is one complete SVD.  Prints the per-SVD device time of the last
@@ -26,7 +30,30 @@ def main() -> None:
     ap.add_argument("--mode", default="tf32x6")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--kind", default="graded", choices=["graded", "uniform"])
+    ap.add_argument("--batched", type=int, default=0, help="number of problems of the uneven batch")
     args = ap.parse_args()
+    if args.batched:
+        import numpy as np
+
+        torch.cuda.set_device(0)
+        rng = np.random.default_rng(3)
+        mats = []
+        for _ in range(args.batched):
+            m = int(rng.integers(16, 257))
+            n = int(rng.integers(8, m + 1))
+            mats.append(rng.uniform(-1, 1, (m, n)).astype(np.float32))
+        plan = ddcsvd.BatchPlan([a.shape for a in mats])
+        plan.load([torch.from_numpy(a).cuda() for a in mats])
+        ms = 0.0
+        for _ in range(args.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            plan.run()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        print(f"batched {args.batched}: {ms:.3f} ms")
+        return
     m = args.size
     n = args.cols or m
     import numpy as np
