@@ -38,97 +38,120 @@ constexpr int kBatchThreads = 256;
 
 __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 
-// Reflector parameters from x0 and the squared norm of the rest (FP64).
-__device__ __forceinline__ void bhouse(float x0, double t2, float* alpha, float* tau, float* scale) {
-  const double nrm = sqrt((double)x0 * (double)x0 + t2);
-  if (nrm == 0.0) {
-    *alpha = 0.f;
-    *tau = 0.f;
-    *scale = 0.f;
-    return;
-  }
-  const double a = -(x0 < 0.f ? -1.0 : 1.0) * nrm;
-  *alpha = (float)a;
-  *tau = (float)((nrm + fabs((double)x0)) / nrm);
-  *scale = (float)(1.0 / ((double)x0 - a));
-}
-
-__device__ __forceinline__ double cta_sum(double v, double* red) {
+// Compensated CTA-wide sum; every thread gets the same value (warps are
+// added in warp order).  `red` holds 2 * (blockDim.x / 32) floats.
+__device__ __forceinline__ FF cta_sum_ff(FF v, float* red) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = warp_sum(v);
+  v = warp_sum_ff(v);
   __syncthreads();
-  if (lane == 0) red[wid] = v;
+  if (lane == 0) {
+    red[2 * wid] = v.hi;
+    red[2 * wid + 1] = v.lo;
+  }
   __syncthreads();
-  double r = 0.0;
-  for (int k = 0; k < nw; k++) r += red[k];
-  __syncthreads();
+  FF r{0.f, 0.f};
+  for (int k = 0; k < nw; k++) r = ff_add(r, FF{red[2 * k], red[2 * k + 1]});
   return r;
 }
 
-// Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA.
-// Reflectors stay in M in LAPACK form (unit leading entry stored).
+constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m - i <= 256)
+
+// Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA
+// (the reference's bidiag_seq order, bidiag.c:33-186: left reflector and
+// rank-1 update, then right reflector and rank-1 update, per column).
+// Reflectors stay in M in LAPACK form (unit leading entry stored).  Norms are
+// compensated FP32 sums and the reflector scalars FP32 (the caller keeps
+// max|M| in [2^-40, 2^40]); every thread forms them from the same reduced
+// value, so no broadcast round is needed.
 __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, float* tq, float* tp,
-                           float* vrow, double* red, float* scal) {
+                           float* vrow, float* red) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
   for (int i = 0; i < n; i++) {
     // ---- left reflector from column i
-    double s2 = 0.0;
-    for (int r = i + 1 + t; r < m; r += blockDim.x) {
-      const double x = M[r + (size_t)i * ld];
-      s2 += x * x;
-    }
-    s2 = cta_sum(s2, red);
+    const float x0 = M[i + (size_t)i * ld];
+    FF s2{0.f, 0.f};
+    for (int r = i + 1 + t; r < m; r += blockDim.x) s2 = ff_add_sq(s2, M[r + (size_t)i * ld]);
+    s2 = cta_sum_ff(s2, red);
+    float alpha, tauq, sq;
+    householder_ff(x0, s2, &alpha, &tauq, &sq);
     if (t == 0) {
-      float a, ta, sc;
-      bhouse(M[i + (size_t)i * ld], s2, &a, &ta, &sc);
-      scal[0] = ta;
-      scal[1] = sc;
-      d[i] = a;
-      tq[i] = ta;
+      d[i] = alpha;
+      tq[i] = tauq;
+      M[i + (size_t)i * ld] = 1.f;
     }
-    __syncthreads();
-    const float tauq = scal[0], sq = scal[1];
     for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
     __syncthreads();
-    if (t == 0) M[i + (size_t)i * ld] = 1.f;
-    __syncthreads();
     if (i == n - 1) break;
-    // ---- left update of columns > i (left_dotprods + left_update_mat)
+    // ---- left update of columns > i (left_dotprods + left_update_mat):
+    // four columns per warp at a time against the reflector held in registers
     if (tauq != 0.f) {
-      const float* u = M + (size_t)i * ld;
-      for (int c = i + 1 + wid; c < n; c += nw) {
-        float* col = M + (size_t)c * ld;
-        float w = 0.f;
-        for (int r = i + lane; r < m; r += 32) w += u[r] * col[r];
-        w = warp_sum(w) * tauq;
-        for (int r = i + lane; r < m; r += 32) col[r] -= w * u[r];
+      const float* uc = M + (size_t)i * ld;
+      if (m - i <= 32 * kColRegs) {
+        float u[kColRegs];
+#pragma unroll
+        for (int k = 0; k < kColRegs; k++) {
+          const int r = i + lane + 32 * k;
+          u[k] = (r < m) ? uc[r] : 0.f;
+        }
+        for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
+          float w[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            float a = 0.f;
+            if (c0 + q < n) {
+              const float* col = M + (size_t)(c0 + q) * ld;
+#pragma unroll
+              for (int k = 0; k < kColRegs; k++) {
+                const int r = i + lane + 32 * k;
+                if (r < m) a += u[k] * col[r];
+              }
+            }
+            w[q] = a;
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int q = 0; q < 4; q++) w[q] += __shfl_xor_sync(0xffffffffu, w[q], o);
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            if (c0 + q >= n) continue;
+            float* col = M + (size_t)(c0 + q) * ld;
+            const float f = w[q] * tauq;
+#pragma unroll
+            for (int k = 0; k < kColRegs; k++) {
+              const int r = i + lane + 32 * k;
+              if (r < m) col[r] -= f * u[k];
+            }
+          }
+        }
+      } else {
+        for (int c = i + 1 + wid; c < n; c += nw) {
+          float* col = M + (size_t)c * ld;
+          float w = 0.f;
+          for (int r = i + lane; r < m; r += 32) w += uc[r] * col[r];
+          w = warp_sum(w) * tauq;
+          for (int r = i + lane; r < m; r += 32) col[r] -= w * uc[r];
+        }
       }
     }
     __syncthreads();
     // ---- right reflector from row i
-    double r2 = 0.0;
-    for (int c = i + 2 + t; c < n; c += blockDim.x) {
-      const double x = M[i + (size_t)c * ld];
-      r2 += x * x;
+    const float y0 = M[i + (size_t)(i + 1) * ld];
+    FF r2{0.f, 0.f};
+    for (int c = i + 2 + t; c < n; c += blockDim.x) r2 = ff_add_sq(r2, M[i + (size_t)c * ld]);
+    r2 = cta_sum_ff(r2, red);
+    float beta, taup, sp;
+    if (i < n - 2) {
+      householder_ff(y0, r2, &beta, &taup, &sp);
+    } else {  // one element left: no reflection (bidiag.c:125-129)
+      beta = y0;
+      taup = 0.f;
+      sp = 0.f;
     }
-    r2 = cta_sum(r2, red);
     if (t == 0) {
-      float b, ta, sc;
-      const float x0 = M[i + (size_t)(i + 1) * ld];
-      if (i < n - 2) {
-        bhouse(x0, r2, &b, &ta, &sc);
-      } else {  // one element left: no reflection (bidiag.c:125-129)
-        b = x0;
-        ta = 0.f;
-        sc = 0.f;
-      }
-      scal[2] = ta;
-      scal[3] = sc;
-      e[i] = b;
-      tp[i] = ta;
+      e[i] = beta;
+      tp[i] = taup;
     }
-    __syncthreads();
-    const float taup = scal[2], sp = scal[3];
     for (int c = i + 1 + t; c < n; c += blockDim.x) {
       float v;
       if (c == i + 1) v = (taup != 0.f) ? 1.f : 0.f;
@@ -157,8 +180,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_bidiag_kernel(const Batch
                                                                      float* tp, int smem_floats, int maxn) {
   extern __shared__ __align__(16) float sm[];
   __shared__ int s_task;
-  __shared__ double red[32];
-  __shared__ float scal[8];
+  __shared__ float red[64];
+  __shared__ unsigned s_amax;
   float* vrow = sm;                 // maxn
   float* Ms = sm + ((maxn + 3) & ~3);  // problem copy when it fits
   while (true) {
@@ -172,15 +195,34 @@ __global__ void __launch_bounds__(kBatchThreads) batch_bidiag_kernel(const Batch
     const bool fits = (long long)m * n <= smem_floats;
     float* Wg = W + T.offW;
     float* M = fits ? Ms : Wg;
-    // load the (oriented) problem
+    // load the (oriented) problem; max|a| for the range scaling of the norms
     const float* src = A + T.offA;
+    if (threadIdx.x == 0) s_amax = 0u;
+    float amax = 0.f;
     for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
       const int r = idx % m, c = idx / m;
-      M[r + (size_t)c * ld] = T.trans ? src[c + (size_t)r * n] : src[idx];
+      const float v = T.trans ? src[c + (size_t)r * n] : src[idx];
+      M[r + (size_t)c * ld] = v;
+      amax = fmaxf(amax, fabsf(v));
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     __syncthreads();
-    cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, scal);
+    if ((threadIdx.x & 31) == 0 && amax > 0.f) atomicMax(&s_amax, __float_as_uint(amax));
     __syncthreads();
+    const float sc = range_scale(s_amax);
+    if (sc != 1.f)
+      for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) M[(idx % m) + (size_t)(idx / m) * ld] *= sc;
+    __syncthreads();
+    cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red);
+    __syncthreads();
+    if (sc != 1.f) {
+      const float inv = 1.f / sc;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        d[T.offD + k] *= inv;
+        if (k < n - 1) e[T.offD + k] *= inv;
+      }
+    }
     if (fits)
       for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) Wg[idx] = M[idx];
     __syncthreads();

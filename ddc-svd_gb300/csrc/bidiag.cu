@@ -83,28 +83,6 @@ __device__ __forceinline__ void householder(float x0, double t2, float* alpha, f
   *scale = (float)(1.0 / ((double)x0 - a));
 }
 
-// The same from a compensated (float-float) ||tail||^2, in FP32 only.  The
-// input matrix is scaled so that max|a| lies in [2^-40, 2^40] (or is left
-// alone when it already does), so x0^2 + t2 neither overflows nor loses
-// anything that matters against ||A||.  sqrt of the rounded pair and the two
-// quotients are correctly rounded FP32 operations: alpha is within one ulp
-// of the FP64 result.
-__device__ __forceinline__ void householder_ff(float x0, FF t2, float* alpha, float* tau, float* scale) {
-  const FF n2 = ff_add_sq(t2, x0);
-  const float nrm = sqrtf(__fadd_rn(n2.hi, n2.lo));
-  if (nrm == 0.f) {
-    *alpha = 0.f;
-    *tau = 0.f;
-    *scale = 0.f;
-    return;
-  }
-  const float ax = fabsf(x0);
-  const float sg = x0 < 0.f ? -1.f : 1.f;
-  *alpha = -sg * nrm;
-  *tau = (nrm + ax) / nrm;
-  *scale = sg / (ax + nrm);  // 1 / (x0 - alpha)
-}
-
 // sum_{r in [r0, r1)} col[r] * xs[r]; col in global (16B-aligned base), xs in
 // shared memory indexed absolutely.  Warp-cooperative, result in all lanes.
 // Eight 16-byte loads per lane are kept in flight.
@@ -757,15 +735,6 @@ __global__ void range_scan_kernel(int m, int n, const float* __restrict__ W, int
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(amax, __float_as_uint(mx));
-}
-
-// 2^k with max|a| * 2^k in [0.5, 1) when max|a| is outside [2^-40, 2^40], else 1
-__device__ __forceinline__ float range_scale(unsigned bits) {
-  const float a = __uint_as_float(bits);
-  if (!(a > 0.f) || isinf(a) || (a >= 0x1p-40f && a <= 0x1p40f)) return 1.f;
-  int ex = 0;
-  frexpf(a, &ex);
-  return ldexpf(1.f, max(-126, min(126, -ex)));
 }
 
 __global__ void range_apply_kernel(int m, int n, float* W, int ldw, const unsigned* amax) {

@@ -174,6 +174,38 @@ __device__ __forceinline__ FF warp_sum_ff(FF v) {
   return v;
 }
 
+// Householder parameters (reference convention alpha = -sign(x0) ||x||,
+// sign(0) = +1) from x0 and a compensated (float-float) ||tail||^2, in FP32
+// only.  The input matrix is scaled so that max|a| lies in [2^-40, 2^40] (or is left
+// alone when it already does), so x0^2 + t2 neither overflows nor loses
+// anything that matters against ||A||.  sqrt of the rounded pair and the two
+// quotients are correctly rounded FP32 operations: alpha is within one ulp
+// of the FP64 result.
+__device__ __forceinline__ void householder_ff(float x0, FF t2, float* alpha, float* tau, float* scale) {
+  const FF n2 = ff_add_sq(t2, x0);
+  const float nrm = sqrtf(__fadd_rn(n2.hi, n2.lo));
+  if (nrm == 0.f) {
+    *alpha = 0.f;
+    *tau = 0.f;
+    *scale = 0.f;
+    return;
+  }
+  const float ax = fabsf(x0);
+  const float sg = x0 < 0.f ? -1.f : 1.f;
+  *alpha = -sg * nrm;
+  *tau = (nrm + ax) / nrm;
+  *scale = sg / (ax + nrm);  // 1 / (x0 - alpha)
+}
+
+// 2^k with max|a| * 2^k in [0.5, 1) when max|a| is outside [2^-40, 2^40], else 1
+__device__ __forceinline__ float range_scale(unsigned bits) {
+  const float a = __uint_as_float(bits);
+  if (!(a > 0.f) || isinf(a) || (a >= 0x1p-40f && a <= 0x1p40f)) return 1.f;
+  int ex = 0;
+  frexpf(a, &ex);
+  return ldexpf(1.f, max(-126, min(126, -ex)));
+}
+
 // Block-wide sum; `red` must hold blockDim.x/32 elements.  All threads get
 // the result.
 template <typename T>

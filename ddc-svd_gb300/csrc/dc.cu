@@ -685,51 +685,62 @@ __global__ void dc_copy_out(int N, const double* s, double* out) {
 
 // ---------------------------------------------------------------- host: forest
 // One tree per unreduced block [lo, hi) of the (split) bidiagonal; a block's
-// singular values occupy slots [lo, hi).
-static int build_tree(DcHost& T, int r0, int nn, int slot, int depth) {
-  int id = (int)T.r0.size();
-  T.r0.push_back(r0); T.nn.push_back(nn); T.slot.push_back(slot);
-  T.K.push_back(-1); T.c1.push_back(-1); T.c2.push_back(-1); T.depth.push_back(depth);
-  T.maxdepth = std::max(T.maxdepth, depth);
-  if (nn > 2) {
-    int K = nn / 2;
-    T.K[id] = K;
-    int a = build_tree(T, r0, K, slot + 1, depth + 1);
-    int b = build_tree(T, r0 + K + 1, nn - K - 1, slot + K + 1, depth + 1);
-    T.c1[id] = a;
-    T.c2[id] = b;
+// singular values occupy slots [lo, hi).  Nodes are created depth-first; a
+// stable counting sort by depth then gives the order the kernel walks (by
+// depth, slots ascending within a depth) without a comparison sort: a batch
+// forest has ~10^5 nodes and this runs on the host between two kernels.
+namespace {
+struct Forest {
+  std::vector<int> r0, nn, slot, K, c1, c2, depth;
+  int maxdepth = 0;
+  int add(int r, int n, int sl, int d) {
+    const int id = (int)r0.size();
+    r0.push_back(r); nn.push_back(n); slot.push_back(sl);
+    K.push_back(-1); c1.push_back(-1); c2.push_back(-1); depth.push_back(d);
+    if (d > maxdepth) maxdepth = d;
+    return id;
   }
-  return id;
-}
+  int build(int r, int n, int sl, int d) {
+    const int id = add(r, n, sl, d);
+    if (n > 2) {
+      const int k = n / 2;
+      K[id] = k;
+      const int a = build(r, k, sl + 1, d + 1);
+      const int b = build(r + k + 1, n - k - 1, sl + k + 1, d + 1);
+      c1[id] = a;
+      c2[id] = b;
+    }
+    return id;
+  }
+};
+}  // namespace
 
 void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
-  DcHost T0;
+  Forest T;
+  const size_t cap = 2 * (size_t)N + 8;
+  T.r0.reserve(cap); T.nn.reserve(cap); T.slot.reserve(cap); T.K.reserve(cap);
+  T.c1.reserve(cap); T.c2.reserve(cap); T.depth.reserve(cap);
   for (size_t b = 0; b + 1 < starts.size(); b++) {
     const int lo = starts[b], hi = starts[b + 1];
-    if (hi > lo) build_tree(T0, lo, hi - lo, lo, 0);
+    if (hi > lo) T.build(lo, hi - lo, lo, 0);
   }
-  const int nnodes = (int)T0.r0.size();
-  std::vector<int> order(nnodes);
-  for (int i = 0; i < nnodes; i++) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](int x, int y) {
-    return T0.depth[x] != T0.depth[y] ? T0.depth[x] < T0.depth[y] : T0.slot[x] < T0.slot[y];
-  });
-  std::vector<int> newid(nnodes);
-  for (int i = 0; i < nnodes; i++) newid[order[i]] = i;
-  const int md = T0.maxdepth;
-  std::vector<int> r0(nnodes), nn(nnodes), slot(nnodes), K(nnodes), c1(nnodes), c2(nnodes), dep(nnodes);
-  for (int i = 0; i < nnodes; i++) {
-    int o = order[i];
-    r0[i] = T0.r0[o]; nn[i] = T0.nn[o]; slot[i] = T0.slot[o]; K[i] = T0.K[o]; dep[i] = T0.depth[o];
-    c1[i] = T0.c1[o] >= 0 ? newid[T0.c1[o]] : -1;
-    c2[i] = T0.c2[o] >= 0 ? newid[T0.c2[o]] : -1;
+  const int nnodes = (int)T.r0.size();
+  const int md = T.maxdepth;
+  // stable counting sort by depth (depth-first creation keeps slots ascending within a depth)
+  std::vector<int> ds(md + 2, 0);
+  for (int i = 0; i < nnodes; i++) ds[T.depth[i] + 1]++;
+  for (int d = 0; d <= md; d++) ds[d + 1] += ds[d];
+  std::vector<int> newid(nnodes), fill(ds.begin(), ds.end() - 1);
+  for (int i = 0; i < nnodes; i++) newid[i] = fill[T.depth[i]]++;
+  std::vector<int> r0(nnodes), nn(nnodes), slot(nnodes), K(nnodes), c1(nnodes), c2(nnodes);
+  for (int o = 0; o < nnodes; o++) {
+    const int i = newid[o];
+    r0[i] = T.r0[o]; nn[i] = T.nn[o]; slot[i] = T.slot[o]; K[i] = T.K[o];
+    c1[i] = T.c1[o] >= 0 ? newid[T.c1[o]] : -1;
+    c2[i] = T.c2[o] >= 0 ? newid[T.c2[o]] : -1;
   }
-  std::vector<int> ds(md + 2, nnodes), dms(md + 2, 0), dmerge;
-  for (int d = md; d >= 0; d--) {
-    int first = nnodes;
-    for (int i = nnodes - 1; i >= 0; i--) if (dep[i] >= d) first = i;
-    ds[d] = first;
-  }
+  std::vector<int> dms(md + 2, 0), dmerge;
+  dmerge.reserve(nnodes);
   for (int d = 0; d <= md; d++) {
     dms[d] = (int)dmerge.size();
     for (int i = ds[d]; i < ds[d + 1]; i++) if (K[i] >= 0) dmerge.push_back(i);
@@ -748,6 +759,7 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
   H.maxdepth = md;
   H.ndm = (int)dmerge.size();
   H.ints.clear();
+  H.ints.reserve(6 * (size_t)nnodes + 3 * (md + 2) + dmerge.size());
   auto app = [&](const std::vector<int>& v) { H.ints.insert(H.ints.end(), v.begin(), v.end()); };
   app(r0); app(nn); app(slot); app(K); app(c1); app(c2); app(ds); app(dms); app(dmerge); app(dgroup);
 }

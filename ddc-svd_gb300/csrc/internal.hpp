@@ -122,7 +122,6 @@ int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw
 // ---------------------------------------------------------------- stage 2
 // Host description of the D&C forest (one tree per unreduced block).
 struct DcHost {
-  std::vector<int> r0, nn, slot, K, c1, c2, depth;  // construction scratch
   int maxdepth = 0;
   int nnodes = 0, ndm = 0;
   std::vector<int> ints;  // packed node table uploaded to the device

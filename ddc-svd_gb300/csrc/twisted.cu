@@ -27,19 +27,26 @@
 
 namespace ddcsvd {
 
-__global__ void tw_setup_kernel(int N, const double* __restrict__ a, const double* __restrict__ b,
-                                double* dd, double* ll, double* dl, double* dll) {
-  // floor for zero diagonal entries (rank-deficient B): keeps l_i finite
-  __shared__ double smax;
-  if (threadIdx.x == 0) {
-    double m = 0.0;
-    for (int i = 0; i < N; i++) m = fmax(m, fabs(a[i]));
-    for (int i = 0; i + 1 < N; i++) m = fmax(m, fabs(b[i]));
-    smax = (m > 0.0 ? m : 1.0) * DBL_EPSILON * DBL_EPSILON;
+// max |a_i|, |b_i| as the bit pattern of a non-negative double (ordered like
+// the value), for the floor below
+__global__ void tw_absmax_kernel(int N, const double* __restrict__ a, const double* __restrict__ b,
+                                 unsigned long long* amax) {
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    m = fmax(m, fabs(a[i]));
+    if (i + 1 < N) m = fmax(m, fabs(b[i]));
   }
-  __syncthreads();
-  const double fl = smax;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(amax, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void tw_setup_kernel(int N, const double* __restrict__ a, const double* __restrict__ b,
+                                const unsigned long long* amax, double* dd, double* ll, double* dl, double* dll) {
+  // floor for zero diagonal entries (rank-deficient B): keeps l_i finite
+  const double m = __longlong_as_double((long long)*amax);
+  const double fl = (m > 0.0 ? m : 1.0) * DBL_EPSILON * DBL_EPSILON;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     double ai = a[i];
     if (fabs(ai) < fl) ai = (ai < 0.0) ? -fl : fl;
     const double di = ai * ai;
@@ -225,19 +232,19 @@ __global__ void tw_finalize_kernel(TwParams p) {
 
 // zero the rows of each output column that lie outside the vector's block
 __global__ void tw_zero_outside_kernel(int N, TwParams p) {
-  const int k = blockIdx.x;
-  if (k >= N) return;
-  const int g = p.L.grp[k], g0 = p.L.g_lo[g], gn = p.L.g_n[g];
-  const int lo = p.L.blo[k], hi = p.L.bhi[k];
-  if (hi - lo == gn) return;
-  const int col = p.rank[k];
-  float* X = p.L.g_X[g] + (size_t)col * p.L.g_ldx[g];
-  float* Y = p.L.g_Y[g] + (size_t)col * p.L.g_ldy[g];
-  for (int i = threadIdx.x; i < gn; i += blockDim.x) {
-    const int gi = g0 + i;
-    if (gi < lo || gi >= hi) {
-      X[i] = 0.f;
-      Y[i] = 0.f;
+  for (int k = blockIdx.x; k < N; k += gridDim.x) {
+    const int g = p.L.grp[k], g0 = p.L.g_lo[g], gn = p.L.g_n[g];
+    const int lo = p.L.blo[k], hi = p.L.bhi[k];
+    if (hi - lo == gn) continue;
+    const int col = p.rank[k];
+    float* X = p.L.g_X[g] + (size_t)col * p.L.g_ldx[g];
+    float* Y = p.L.g_Y[g] + (size_t)col * p.L.g_ldy[g];
+    for (int i = threadIdx.x; i < gn; i += blockDim.x) {
+      const int gi = g0 + i;
+      if (gi < lo || gi >= hi) {
+        X[i] = 0.f;
+        Y[i] = 0.f;
+      }
     }
   }
 }
@@ -277,6 +284,7 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
                const double* sigma, const VecLayout* L, double* sigma_sorted, Arena& arena, bool plan_only) {
   if (N <= 0) return DDCSVD_ERR_ARG;
   double* small = arena.take<double>(6 * (size_t)N + 8);
+  unsigned long long* amax = arena.take<unsigned long long>(4);
   int* rank = arena.take<int>(N + 8);
   double* big = arena.take<double>(5 * (size_t)store);
   if (plan_only) return DDCSVD_OK;
@@ -296,15 +304,18 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
   p.b = b;
   p.Lp = big; p.Um = big + store; p.S = big + 2 * store; p.Pp = big + 3 * store; p.Z = big + 4 * store;
   ktimer_begin(ctx, KC_VECTORS);
-  tw_setup_kernel<<<1, 256, 0, ctx->stream>>>(N, a, b, dd, ll, dl, dll);
-  count_launch();
+  const int sg = std::min(ceil_div(N, 256), 4 * ctx->num_sms);
+  DDC_CUDA_TRY(cudaMemsetAsync(amax, 0, sizeof(unsigned long long), ctx->stream));
+  tw_absmax_kernel<<<sg, 256, 0, ctx->stream>>>(N, a, b, amax);
+  tw_setup_kernel<<<sg, 256, 0, ctx->stream>>>(N, a, b, amax, dd, ll, dl, dll);
+  count_launch(2);
   twisted_kernel<<<ceil_div(N, 32), 32 * kTwWarps, 0, ctx->stream>>>(p);
   count_launch();
   tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, p.L, rank, sigma_sorted);
   count_launch();
   tw_finalize_kernel<<<L->ntiles, dim3(32, 8), 0, ctx->stream>>>(p);
   count_launch();
-  tw_zero_outside_kernel<<<N, 128, 0, ctx->stream>>>(N, p);
+  tw_zero_outside_kernel<<<std::min(N, 16 * ctx->num_sms), 128, 0, ctx->stream>>>(N, p);
   count_launch();
   ktimer_end(ctx);
   DDC_CUDA_TRY(cudaGetLastError());
