@@ -34,7 +34,8 @@ struct BatchTask {
   long long offS;  // caller's sigma
 };
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 256;        // back-transformation CTAs
+constexpr int kBatchBidiagThreads = 512;  // bidiagonalisation CTAs (one per SM, whole problem in shared memory)
 
 __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 
@@ -173,7 +174,7 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads) batch_bidiag_kernel(const BatchTask* __restrict__ tasks,
+__global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const BatchTask* __restrict__ tasks,
                                                                      const int* __restrict__ order, int ntask,
                                                                      int* counter, const float* __restrict__ A,
                                                                      float* W, float* d, float* e, float* tq,
@@ -471,15 +472,22 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
                                h->stream));
   DDC_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), h->stream));
   // ---- stage 1: persistent CTAs over the size-sorted work list
-  const int smem_floats = 24 * 1024;  // problems up to 24K entries live in shared memory
-  const size_t smem = sizeof(float) * ((size_t)((maxn + 3) & ~3) + smem_floats);
+  // stage 1 keeps a problem in shared memory when it fits the SM's opt-in
+  // maximum (up to ~56K entries: all but the largest 256 x 2xx problems);
+  // stage 5 reads its reflectors from up to 24K entries of shared memory
+  const int smem_floats = 24 * 1024;
+  int max_optin = 0;
+  DDC_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+  const int vrow_floats = (int)((maxn + 3) & ~3);
+  const int bidiag_floats = std::max(1024, (max_optin - 2048) / (int)sizeof(float) - vrow_floats);
+  const size_t smem = sizeof(float) * ((size_t)vrow_floats + bidiag_floats);
   DDC_CUDA_TRY(cudaFuncSetAttribute(batch_bidiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
-  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_bidiag_kernel, kBatchThreads, smem));
+  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_bidiag_kernel, kBatchBidiagThreads, smem));
   const int grid1 = std::max(1, std::min(batch, h->num_sms * std::max(occ, 1)));
   ktimer_begin(h, KC_BIDIAG);
-  batch_bidiag_kernel<<<grid1, kBatchThreads, smem, h->stream>>>(dt, dord, batch, counter, dA, W, d, e, tq, tp,
-                                                                 smem_floats, maxn);
+  batch_bidiag_kernel<<<grid1, kBatchBidiagThreads, smem, h->stream>>>(dt, dord, batch, counter, dA, W, d, e, tq,
+                                                                       tp, bidiag_floats, maxn);
   ktimer_end(h);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
