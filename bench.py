@@ -191,6 +191,59 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
                        f"stages on its leading 1024^2 block ({max(tfull - tbb, 0):.2f} s, scaled by (4096/1024)^3)")}
 
 
+# DRAM bytes (read + write) of one panel-kernel launch, mean over the 4096^2
+# factorisation, from an ncu capture of `python -m ddcsvd.profile --size 4096
+# --mode tf32x6 --reps 1 --kind uniform` (metrics dram__bytes_read.sum and
+# dram__bytes_write.sum, all 128 launches).  Far below the algorithmic GEMV
+# bytes: the trailing block is re-read from L2, not HBM.
+PANEL_DRAM_BYTES_PER_LAUNCH = 23177000
+
+
+def bench_tall(torch, lib, h, steps):
+    """Thin SVD of the tall configuration: 16384 x 8192 FP32, entries N(0, 1)
+    from a seeded generator (rng(2)); residual and orthogonality in FP32 on
+    the GPU (no FP64 reference of this size is formed)."""
+    m, n = 16384, 8192
+    rng = np.random.default_rng(2)
+    A = torch.from_numpy(rng.standard_normal((n, m), dtype=np.float32)).cuda()  # column-major m x n
+    bufs = (torch.empty(n, device="cuda"), torch.empty((n, m), device="cuda"), torch.empty((n, n), device="cuda"))
+    lib.svd_device_colmajor(h, m, n, A, *bufs, mode="tf32x6")
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.svd_device_colmajor(h, m, n, A, *bufs, mode="tf32x6")
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    h.stage_timing(True)
+    lib.svd_device_colmajor(h, m, n, A, *bufs, mode="tf32x6")
+    torch.cuda.synchronize()
+    kms, kn = h.kernel_times(5)
+    h.stage_timing(False)
+    s, Ut, Vt = bufs
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    Am = A.t()
+    resid = float(torch.linalg.norm(Am - (Ut.t() * s) @ Vt) / torch.linalg.norm(Am))
+    ou = float(torch.linalg.norm(Ut @ Ut.t() - torch.eye(n, device="cuda")) / n ** 0.5)
+    ov = float(torch.linalg.norm(Vt @ Vt.t() - torch.eye(n, device="cuda")) / n ** 0.5)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    ms = float(np.mean(ts))
+    del A, bufs
+    torch.cuda.empty_cache()
+    return {"m": m, "n": n, "mode": "tf32x6", "ms": round(ms, 2),
+            "gflops": round(svd_flops(m, n) / (ms * 1e-3) / 1e9, 1),
+            "kernel_ms": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform"],
+                                  [round(x, 3) for x in kms])),
+            "gemv_roofline": {"bytes": gemv_bytes(m, n), "unit": "GB/s",
+                              "achieved": round(gemv_bytes(m, n) / (kms[0] * 1e-3) / 1e9, 1) if kms[0] > 0 else None,
+                              "peak": measured_peaks()[0]},
+            "accuracy_fp32_check": {"resid": float(f"{resid:.3e}"), "orth_u": float(f"{ou:.3e}"),
+                                    "orth_v": float(f"{ov:.3e}")}}
+
+
 def batched_workload(seed=3, count=2048):
     """2048 FP32 problems, m ~ U{16..256}, n ~ U{8..m}, entries U[-1, 1] (seeded)."""
     rng = np.random.default_rng(seed)
@@ -421,6 +474,7 @@ def main():
 
     batched = bench_batched(torch, lib, h, max(3, args.steps), flush) if not args.quick else None
     adjoint = bench_adjoint(torch, lib, h, max(3, args.steps)) if not args.quick else None
+    tall = bench_tall(torch, lib, h, 2) if not args.quick else None
 
     # roofline of the dominant kernel class (bidiagonalisation GEMV kernels)
     hbm, peak_kind = measured_peaks()
@@ -431,7 +485,9 @@ def main():
     achieved = bytes_total / (bid_ms * 1e-3) / 1e9 if bid_ms > 0 else None
     roof = {"bound": "hbm", "kernel": "bidiag_panel_kernel", "achieved": round(achieved, 1) if achieved else None,
             "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / hbm, 3) if achieved else None, "traffic": None,
+            "frac": round(achieved / hbm, 3) if achieved else None, "traffic": PANEL_DRAM_BYTES_PER_LAUNCH,
+            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per panel launch, mean over the 128 "
+                            "launches of a 4096^2 factorisation (L2 flushed before each launch by ncu)",
             "bytes_per_launch": round(bytes_total / nl), "launches": nl,
             "avg_launch_ms": round(bid_ms / nl, 4)}
 
@@ -453,7 +509,7 @@ def main():
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": M * N * 4,
                 "d2h_bytes_per_step": (N + M * N + N * N) * 4, "api": "ddcsvd_svd_f32 (pinned host buffers)"},
         "roofline": roof, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cb,
-        "batched": batched, "adjoint": adjoint,
+        "batched": batched, "adjoint": adjoint, "tall": tall,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
