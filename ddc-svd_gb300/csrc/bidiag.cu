@@ -62,6 +62,9 @@ struct PanelParams {
   double *colnrm, *rownrm;   // [P]
   GridBarrier* bar;
   DevStatus* st;
+  // tensor-core trailing update: the panel's [Up X] rows (>= k0 + nb) and
+  // [Y VT] rows written K-major (2 * kPanel floats per row) at the end, or null
+  float *Apk, *Bpk;
 };
 
 __device__ __forceinline__ float sgn_ref(float x) { return x < 0.f ? -1.f : 1.f; }
@@ -541,6 +544,22 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     __syncthreads();
     PMARK(11);
   }
+  // K-major operands of the trailing update straight from the shared-memory
+  // copies of the own rows / columns (replaces two pack kernels per panel)
+  if (p.Apk) {
+    const int kn = k0 + p.nb;
+    constexpr int K2 = 2 * kPanel;
+    const int r0 = max(ra, kn);
+    for (int idx = t; idx < max(0, rb - r0) * K2; idx += blockDim.x) {
+      const int r = r0 + idx / K2, jj = idx % K2, lr = r - ra;
+      p.Apk[(size_t)(r - kn) * K2 + jj] = (jj < kPanel) ? S.UpS[lr * kLD + jj] : S.XS[lr * kLD + jj - kPanel];
+    }
+    const int c0 = max(ca, kn);
+    for (int idx = t; idx < max(0, cb - c0) * K2; idx += blockDim.x) {
+      const int c = c0 + idx / K2, jj = idx % K2, lc = c - ca;
+      p.Bpk[(size_t)(c - kn) * K2 + jj] = (jj < kPanel) ? S.YS[lc * kLD + jj] : S.VTS[lc * kLD + jj - kPanel];
+    }
+  }
   PMARK_K(13);
 }
 
@@ -817,6 +836,9 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
     pp.rownrm = reinterpret_cast<double*>(round_up(reinterpret_cast<uintptr_t>(pp.rownrm), 8));
     pp.bar = w.bar;
     pp.st = ctx->d_status;
+    const bool fused_pack = (kind != GEMM_SIMT) && nb == kPanel && k0 + nb < n;
+    pp.Apk = fused_pack ? w.Apk : nullptr;
+    pp.Bpk = fused_pack ? w.Bpk : nullptr;
     DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
     const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads, P);
     ktimer_begin(ctx, KC_BIDIAG);
@@ -836,8 +858,11 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
                      ldw, scratch));
       } else {
         // tensor cores read K-major operands: [U_p X] and [Y VT] as rows of 2*nb
-        DDC_TRY(pack_kmajor(ctx, M, nb, W + kn + (size_t)k0 * ldw, ldw, nb, w.X + kn, ldw, w.Apk, 2 * kPanel));
-        DDC_TRY(pack_kmajor(ctx, N, nb, w.Y + kn, w.ldn, nb, w.VT + kn, w.ldn, w.Bpk, 2 * kPanel));
+        // (written by the panel kernel itself for full panels)
+        if (!fused_pack) {
+          DDC_TRY(pack_kmajor(ctx, M, nb, W + kn + (size_t)k0 * ldw, ldw, nb, w.X + kn, ldw, w.Apk, 2 * kPanel));
+          DDC_TRY(pack_kmajor(ctx, N, nb, w.Y + kn, w.ldn, nb, w.VT + kn, w.ldn, w.Bpk, 2 * kPanel));
+        }
         DDC_TRY(gemm_tc_kmajor(ctx, kind, M, N, 2 * nb, w.Apk, 2 * kPanel, 0, w.Bpk, 2 * kPanel, 0,
                                W + kn + (size_t)kn * ldw, ldw, -1.f, 1.f, scratch));
       }

@@ -35,6 +35,7 @@
 // TMA copies in flight and frees its TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <string.h>
 
 #include "async.cuh"
 #include "internal.hpp"
@@ -49,6 +50,12 @@ namespace tc {
 constexpr int BM = 128;
 constexpr int BK = 32;  // FP32 elements per slab row: 128 bytes = one swizzle span
 constexpr int THREADS = 192;
+// K slabs accumulated in one TMEM buffer before the epilogue warps drain it
+// into FP32 registers: the tensor core's own accumulation error grows with
+// the number of MMAs it chains (measured: ~linear in K; draining every 4
+// slabs raised the 4096^2 SVD residual from 1.3e-6 to 3.7e-6), so each
+// 32-wide slab is drained and added in FP32 round-to-nearest.
+constexpr int kGroup = 1;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 // Bounded wait for the phase of the given parity.  Returns false when the CTA
@@ -145,6 +152,7 @@ struct TcParams {
   float alpha, beta;
   float* partial;  // split-K partials (M x N per split, ld M) or null
   int trans;       // store C transposed: element (r, c) at C[c + r * ldc]
+  int tma_epi;     // 0: per-thread C update; 1: TMA store (beta 0); 2: TMA reduce-add (beta 1)
   DevStatus* st;
 };
 
@@ -161,7 +169,7 @@ struct Layout {
 template <int BN, int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     tc_gemm_split_tf32_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                              TcParams p) {
+                              const __grid_constant__ CUtensorMap tmC, TcParams p) {
   using L = Layout<BN, NP>;
   constexpr int STAGES = L::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -232,9 +240,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BM, BN);
       for (int i = 0; i < nsl; i++) {
-        const int s = i % STAGES, b = i & 1;
+        const int s = i % STAGES, g = i / kGroup, b = g & 1;
+        const bool gfirst = (i % kGroup) == 0;
+        const bool glast = (i % kGroup) == kGroup - 1 || i == nsl - 1;
         if (!mbar_wait(&conv[s], (i / STAGES) & 1, abort_flag, p.st, 902)) break;
-        if (i >= 2 && !mbar_wait(&acce[b], ((i >> 1) - 1) & 1, abort_flag, p.st, 905)) break;
+        if (gfirst && g >= 2 && !mbar_wait(&acce[b], ((g >> 1) - 1) & 1, abort_flag, p.st, 905)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + (uint32_t)(b * BN);
 #pragma unroll
@@ -246,7 +256,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             da[k] = smem_desc_sw128(smem_u32(a_part(s, k)) + off);
             db[k] = smem_desc_sw128(smem_u32(b_part(s, k)) + off);
           }
-          const uint32_t first = (kk > 0) ? 1u : 0u;  // each slab starts a fresh partial sum
+          const uint32_t first = (kk > 0 || !gfirst) ? 1u : 0u;  // each slab group starts a fresh partial sum
           if (NP == 3) {  // l*h, h*l, m*m, m*h, h*m, h*h
             mma_tf32(d, da[2], db[0], idesc, first);
             mma_tf32(d, da[0], db[2], idesc, 1u);
@@ -261,7 +271,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
         mma_commit(&empty[s]);
-        mma_commit(&accf[b]);
+        if (glast) mma_commit(&accf[b]);
       }
     }
   } else {
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
     for (int c = 0; c < BN; c++) acc[c] = 0.f;
     bool ok = true;
-    auto drain = [&](int j) {
+    auto drain = [&](int j) {  // slab group j
       const int b = j & 1;
       if (!mbar_wait(&accf[b], (j >> 1) & 1, abort_flag, p.st, 904)) {
         ok = false;
@@ -304,13 +314,28 @@ __global__ void __launch_bounds__(THREADS, 1)
                      reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, 128);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&conv[s]);
-      if (i >= 1) drain(i - 1);
+      if (i >= kGroup && (i % kGroup) == 0) drain(i / kGroup - 1);
     }
-    if (ok && nsl >= 1) drain(nsl - 1);
+    if (ok && nsl >= 1) drain((nsl - 1) / kGroup);
     // ---------------- epilogue: registers -> C
     ok = ok && !*abort_flag && nsl > 0;
     const int row = m0 + q * 32 + lane;
-    if (ok && row < p.M) {
+    if (p.tma_epi && !p.partial) {
+      // alpha * acc -> shared tile [BN cols][BM rows] (the stage buffers are
+      // free: every MMA has completed and every TMA load has landed), then one
+      // thread stores or reduce-adds the tile into C with a single TMA op
+      float* tile = reinterpret_cast<float*>(smem);
+      const int rl = q * 32 + lane;
+#pragma unroll
+      for (int c = 0; c < BN; c++) tile[c * BM + rl] = p.alpha * acc[c];
+      fence_proxy_async_smem();
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (ct == 0 && ok) {
+        if (p.tma_epi == 2) tma_reduce_add_2d(&tmC, tile, m0, n0);
+        else tma_store_2d(&tmC, tile, m0, n0);
+        bulk_commit_and_wait();
+      }
+    } else if (ok && row < p.M) {
 #pragma unroll
       for (int c0 = 0; c0 < BN; c0 += 16) {
         if (p.partial) {
@@ -392,6 +417,21 @@ static int make_map(CUtensorMap* map, const float* base, long long kext, long lo
   return DDCSVD_OK;
 }
 
+// 2-D map over the column-major output C (rows innermost), box BM x BN, no
+// swizzle: target of the TMA store / reduce-add epilogue.
+static int make_map_c(CUtensorMap* map, const float* C, long long M, long long N, long long ldc, int bn) {
+  EncodeFn enc = encode_fn();
+  if (!enc) return DDCSVD_ERR_UNSUPPORTED;
+  cuuint64_t dims[2] = {(cuuint64_t)M, (cuuint64_t)N};
+  cuuint64_t strides[1] = {(cuuint64_t)(ldc * 4)};
+  cuuint32_t box[2] = {(cuuint32_t)BM, (cuuint32_t)bn};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(C), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? DDCSVD_OK : DDCSVD_ERR_CUDA;
+}
+
 template <int BN, int NP>
 static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long long lda, int a_koff,
                   const float* B, long long ldb, int b_koff, float* C, int ldc, float alpha, float beta,
@@ -428,8 +468,15 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   p.per_split = ceil_div(p.nslab, ksplit);
   ksplit = ceil_div(p.nslab, p.per_split);
   p.partial = (ksplit > 1) ? reinterpret_cast<float*>(scratch->base) : nullptr;
+  // C update through one TMA store (beta 0) or reduce-add (beta 1) per tile
+  CUtensorMap mc;
+  memset(&mc, 0, sizeof(mc));
+  p.tma_epi = 0;
+  if (!trans && ksplit == 1 && (beta == 0.f || beta == 1.f) && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
+      (ldc % 4) == 0 && make_map_c(&mc, C, M, N, ldc, BN) == DDCSVD_OK)
+    p.tma_epi = (beta == 0.f) ? 1 : 2;
   dim3 grid(ceil_div(M, BM), ceil_div(N, BN), ksplit);
-  tc_gemm_split_tf32_kernel<BN, NP><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, p);
+  tc_gemm_split_tf32_kernel<BN, NP><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, mc, p);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
   if (ksplit > 1) splitk_reduce(ctx, M, N, ksplit, p.partial, alpha, beta, C, ldc, trans);
