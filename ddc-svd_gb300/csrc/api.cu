@@ -775,4 +775,58 @@ void bidiag_par(int m, int n, double* A, double* alpha, double* beta) {
   }
 }
 
+// form_u_par / form_v_par: the explicit factors from bidiag_par's reflectors
+// (host FP64 buffers in and out, computed on the GPU in FP64).
+static int form_factor_host(int m, int n, const double* A_mod, double* Q, bool left) {
+  if (m <= 0 || n <= 0 || !A_mod || !Q) return DDCSVD_ERR_ARG;
+  ddcsvd_context* h = nullptr;
+  DDC_TRY(default_ctx(&h));
+  std::lock_guard<std::mutex> g(h->mu);
+  const int rows = left ? m : n;
+  const size_t na = (size_t)m * n, nq = (size_t)rows * rows, ns = left ? 0 : (size_t)n * n;
+  double* buf = nullptr;
+  int rc = DDCSVD_OK;
+  if (cudaMallocAsync((void**)&buf, sizeof(double) * (na + nq + ns + 16), h->stream) != cudaSuccess) {
+    set_last_error("cudaMallocAsync of %zu bytes failed", sizeof(double) * (na + nq + ns + 16));
+    return DDCSVD_ERR_ALLOC;
+  }
+  double* dA = buf;
+  double* dQ = buf + na;
+  double* dS = dQ + nq;
+  do {
+    if (cudaMemcpyAsync(dA, A_mod, sizeof(double) * na, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+      rc = DDCSVD_ERR_CUDA;
+      break;
+    }
+    rc = form_factor_f64(h, m, n, dA, left, dQ, dS);
+    if (rc) break;
+    if (cudaMemcpyAsync(Q, dQ, sizeof(double) * nq, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) {
+      rc = DDCSVD_ERR_CUDA;
+      break;
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = DDCSVD_ERR_CUDA;
+  } while (0);
+  cudaFreeAsync(buf, h->stream);
+  cudaStreamSynchronize(h->stream);
+  return rc;
+}
+
+void form_u_par(int m, int n, const double* A_mod, double* U) {
+  t_last_error.clear();
+  const int rc = form_factor_host(m, n, A_mod, U, true);
+  if (rc != DDCSVD_OK) {
+    fprintf(stderr, "form_u_par: %s (%s)\n", ddcsvd_status_string(rc), ddcsvd_last_error());
+    if (U && m > 0) U[0] = __builtin_nan("");
+  }
+}
+
+void form_v_par(int m, int n, const double* A_mod, double* V) {
+  t_last_error.clear();
+  const int rc = form_factor_host(m, n, A_mod, V, false);
+  if (rc != DDCSVD_OK) {
+    fprintf(stderr, "form_v_par: %s (%s)\n", ddcsvd_status_string(rc), ddcsvd_last_error());
+    if (V && n > 0) V[0] = __builtin_nan("");
+  }
+}
+
 }  // extern "C"

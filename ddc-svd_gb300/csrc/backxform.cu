@@ -338,6 +338,68 @@ __global__ void __launch_bounds__(256) apply_plain_kernel(int rows_total, int nr
   }
 }
 
+// ---------------------------------------------------------------- explicit factors (FP64)
+// Columns of the orthogonal factors of A = U B V^T from the reference's
+// normalised reflectors (H = I - 2 v v^T, ||v|| = 1, as bidiag_par leaves
+// them in A_mod), one warp per column in FP64, in the reference's order:
+//   U[:, i] = H_0 ... H_{js(i)} e_i,  js(i) = min(i, mn - 1)        (form_u_par, bidiag_par.c:877-929)
+//   V[:, i] = G_0 ... G_{js(i)} e_i,  js(i) = min(i - 1, nref - 1)  (form_v_par, bidiag_par.c:932-988)
+// Reflectors beyond js(i) act on rows where e_i is zero and are skipped, as
+// in the reference.  Right reflector j is row j of A_mod from column j + 1,
+// read from a transposed copy (RT[k + j * n] = A_mod[j + k * m]).
+__global__ void form_factor_kernel(int rows, int nref, int shift, const double* __restrict__ R, int ldr,
+                                   double* Q) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < rows; i += nwarps) {
+    double* col = Q + (size_t)i * rows;
+    for (int k = lane; k < rows; k += 32) col[k] = (k == i) ? 1.0 : 0.0;
+    __syncwarp();
+    const int js = min(i - shift, nref - 1);
+    for (int j = js; j >= 0; j--) {
+      const double* v = R + (size_t)j * ldr;  // v(k) = v[k], k >= j + shift
+      double sdot = 0.0;
+      for (int k = j + shift + lane; k < rows; k += 32) sdot += col[k] * v[k];
+      sdot = warp_sum(sdot);
+      for (int k = j + shift + lane; k < rows; k += 32) col[k] -= 2.0 * v[k] * sdot;
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void transpose_f64_kernel(int rows, int cols, const double* __restrict__ A, int lda, double* AT,
+                                     int ldat) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int r = r0 + threadIdx.x, c = c0 + k;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? A[r + (size_t)c * lda] : 0.0;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int c = c0 + threadIdx.x, r = r0 + k;
+    if (r < rows && c < cols) AT[c + (size_t)r * ldat] = tile[threadIdx.x][k];
+  }
+}
+
+int form_factor_f64(ddcsvd_context* ctx, int m, int n, const double* dA, bool left, double* dQ, double* scratch) {
+  const int mn = std::min(m, n);
+  if (left) {
+    form_factor_kernel<<<std::min(ceil_div(m, 8), 8 * ctx->num_sms), 256, 0, ctx->stream>>>(m, mn, 0, dA, m, dQ);
+    count_launch();
+  } else {
+    const int nref = (m < n) ? mn : mn - 1;
+    // RT (n x n): RT[k + j * n] = A_mod[j + k * m] for the first min(m, n) rows j
+    transpose_f64_kernel<<<dim3(ceil_div(mn, 32), ceil_div(n, 32)), dim3(32, 8), 0, ctx->stream>>>(mn, n, dA, m,
+                                                                                                  scratch, n);
+    form_factor_kernel<<<std::min(ceil_div(n, 8), 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, nref, 1, scratch, n,
+                                                                                         dQ);
+    count_launch(2);
+  }
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
 int apply_left_reflectors(ddcsvd_context* ctx, int m, int nref, const float* W, int ldw,
                           const float* tauq, float* C, int ldc, int ncols, GemmKind kind,
                           bool plain, Arena& a, bool plan_only) {

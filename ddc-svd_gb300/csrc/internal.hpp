@@ -158,4 +158,8 @@ int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W,
                            const float* taup, float* C, int ldc, int ncols, GemmKind kind,
                            bool plain, Arena& a, bool plan_only);
 
+// Explicit U (m x m) or V (n x n) from the reference's FP64 reflector storage
+// (device buffers; scratch: n * n doubles for V).
+int form_factor_f64(ddcsvd_context* ctx, int m, int n, const double* dA, bool left, double* dQ, double* scratch);
+
 }  // namespace ddcsvd

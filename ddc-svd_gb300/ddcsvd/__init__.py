@@ -75,6 +75,30 @@ def bidiag_par(A: np.ndarray):
     return A, al, be[: n - 1]
 
 
+def form_u_par(A_mod: np.ndarray):
+    """form_u_par (bidiag_par.c:877) on bidiag_par's reflectors: the full m x m left factor."""
+    lib = load()
+    A = np.asarray(A_mod, dtype=np.float64, order="F")
+    m, n = A.shape
+    U = np.zeros((m, m), order="F")
+    lib.form_u_par(m, n, _addr(A), _addr(U))
+    if np.isnan(U.flat[0]):
+        raise DdcsvdError(2, "form_u_par")
+    return U
+
+
+def form_v_par(A_mod: np.ndarray):
+    """form_v_par (bidiag_par.c:932) on bidiag_par's reflectors: the full n x n right factor."""
+    lib = load()
+    A = np.asarray(A_mod, dtype=np.float64, order="F")
+    m, n = A.shape
+    V = np.zeros((n, n), order="F")
+    lib.form_v_par(m, n, _addr(A), _addr(V))
+    if np.isnan(V.flat[0]):
+        raise DdcsvdError(2, "form_v_par")
+    return V
+
+
 def svd(A: np.ndarray, mode="auto"):
     """FP32 host SVD (A not modified); returns (sigma asc, U (m,k), V (n,k)) as float32."""
     lib = load()

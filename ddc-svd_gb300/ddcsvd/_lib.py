@@ -23,6 +23,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed
 _SIGS = {
     "svd_gpu": (None, [c_int, c_int, P, P, P, P]),
     "bidiag_par": (None, [c_int, c_int, P, P, P]),
+    "form_u_par": (None, [c_int, c_int, P, P]),
+    "form_v_par": (None, [c_int, c_int, P, P]),
     "svd_gpu_ex": (c_int, [c_int, c_int, P, P, P, P, c_int]),
     "ddcsvd_svd_f32": (c_int, [c_int, c_int, P, c_int, P, P, c_int, P, c_int, c_int]),
     "ddcsvd_create": (c_int, [P, c_int]),

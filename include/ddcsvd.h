@@ -5,6 +5,7 @@
  * Drop-in entry points keep the reference's signatures and argument layout:
  *   svd_gpu     replaces svd_gpu.h:5   (svd_gpu.c:53-131)
  *   bidiag_par  replaces bidiag_par.h:30 (bidiag_par.c:34-450)
+ *   form_u_par, form_v_par  replace bidiag_par.h:33-34 (bidiag_par.c:877-988)
  * Everything else extends that interface (status codes, FP32 buffers, device
  * pointers, batching, the adjoint).  All matrices are column-major.  The
  * singular values come out ascending, as the reference returns them
@@ -78,6 +79,15 @@ void svd_gpu(int m, int n, double *A, double *sigma, double *U, double *V);
  * reflector v in the partial column from A[i,i], the i-th right reflector in
  * the partial row from A[i,i+1], each with H = I - 2 v v^T and ||v|| = 1. */
 void bidiag_par(int m, int n, double *A, double *alpha, double *beta);
+
+/* Replace bidiag_par.h:33-34 (bidiag_par.c:877-988).  Host FP64 buffers.
+ * From the reflectors that bidiag_par leaves in A_mod (m x n), form the full
+ * left factor U (m x m, column i at U + i*m) or the right factor V (n x n),
+ * so that A = U [B; 0] V^T; computed on the GPU in FP64 in the reference's
+ * order.  On failure the first entry of the output is NaN and one line goes
+ * to stderr (the reference has no error path). */
+void form_u_par(int m, int n, const double *A_mod, double *U);
+void form_v_par(int m, int n, const double *A_mod, double *V);
 
 /* ---------------------------------------------------------------- status-returning host API */
 

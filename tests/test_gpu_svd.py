@@ -164,6 +164,49 @@ def test_svd_large_shapes(lib, cuda, orc, m, n):
     check_metrics(orc, A, s, U, V)
 
 
+def _form_factors_numpy(A_mod, left):
+    """The reference's form_u_par / form_v_par loops (bidiag_par.c:877-988), restated in numpy."""
+    m, n = A_mod.shape
+    mn = min(m, n)
+    if left:
+        Q = np.eye(m)
+        for i in range(m):
+            for j in range(min(i, mn - 1), -1, -1):
+                v = A_mod[j:, j]
+                Q[j:, i] -= 2.0 * v * (v @ Q[j:, i])
+        return Q
+    nref = mn if m < n else mn - 1
+    Q = np.eye(n)
+    for i in range(n):
+        for j in range(min(i - 1, nref - 1), -1, -1):
+            v = A_mod[j, j + 1:]
+            Q[j + 1:, i] -= 2.0 * v * (v @ Q[j + 1:, i])
+    return Q
+
+
+@pytest.mark.parametrize("m,n", [(40, 40), (90, 57), (257, 130)])
+def test_form_factors_dropin(lib, cuda, m, n):
+    """form_u_par / form_v_par on bidiag_par's reflectors: the reference's loops
+    (numpy restatement) to FP64 accuracy; orthogonality and A = U [B; 0] V^T
+    to the FP32 level of the bidiagonalisation."""
+    rng = np.random.default_rng(m * 31 + n)
+    A = rng.uniform(-1, 1, (m, n))
+    A_mod, al, be = lib.bidiag_par(A)
+    U = lib.form_u_par(A_mod)
+    V = lib.form_v_par(A_mod)
+    assert np.abs(U - _form_factors_numpy(A_mod, True)).max() <= 1e-12
+    assert np.abs(V - _form_factors_numpy(A_mod, False)).max() <= 1e-12
+    # the reflectors come from the FP32 bidiagonalisation (||v|| = 1 to FP32):
+    # orthogonal to the FP32 level
+    assert np.linalg.norm(U.T @ U - np.eye(m)) / m ** 0.5 <= TOL
+    assert np.linalg.norm(V.T @ V - np.eye(n)) / n ** 0.5 <= TOL
+    B = np.zeros((m, n))
+    B[np.arange(n), np.arange(n)] = al
+    B[np.arange(n - 1), np.arange(1, n)] = be
+    A32 = A.astype(np.float32).astype(np.float64)
+    assert np.linalg.norm(U @ B @ V.T - A32) / np.linalg.norm(A32) <= 1e-5
+
+
 def test_nonfinite_input_fails_loudly(lib, cuda):
     A = np.ones((16, 8), dtype=np.float32)
     A[3, 2] = np.nan
