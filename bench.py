@@ -255,8 +255,21 @@ def batched_workload(seed=3, count=2048):
     return mats
 
 
+def lib_mode_ok(lib, h):
+    """True when the tensor-core mode runs on this device."""
+    import torch
+    try:
+        lib.svd_device(torch.ones((4, 4), device="cuda"), mode="tf32x6", handle=h)
+        return True
+    except lib.DdcsvdError as e:
+        if e.status == 8:
+            return False
+        raise
+
+
 def bench_batched(torch, lib, h, steps, flush):
     mats = batched_workload()
+    tuning = h.autotune_batched([a.shape for a in mats], reps=2)
     plan = lib.BatchPlan([a.shape for a in mats], handle=h)
     plan.load([torch.from_numpy(a).cuda() for a in mats])
     plan.run()
@@ -297,7 +310,7 @@ def bench_batched(torch, lib, h, steps, flush):
     return {"svds_per_s": round(len(mats) / (ms * 1e-3), 1), "ms": round(ms, 3), "count": len(mats),
             "loop_single_svds_per_s": round(1e3 / loop_ms, 1), "compulsory_bytes": comp, "elements": mn,
             "hbm_frac": round(comp / (ms * 1e-3) / 1e9 / hbm, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
-            "worst_resid": float(f"{worst:.3e}"),
+            "worst_resid": float(f"{worst:.3e}"), "tuning": tuning,
             "kernel_ms": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform"],
                                   [round(x, 3) for x in kms]))}
 
@@ -391,6 +404,8 @@ def main():
     A64r = A32.double()
     Ac = A32.t().contiguous()  # column-major buffer
     h = lib.Handle(local)
+    # launch knobs from the library's autotuner for this shape (untimed)
+    tuning = h.autotune_svd(M, N, mode="tf32x6", reps=2) if lib_mode_ok(lib, h) else h.tuning
     bufs = (torch.empty(N, device=dev), torch.empty((N, M), device=dev), torch.empty((N, N), device=dev))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -503,7 +518,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP64 sigma/vector stages)", "data": "synthetic",
         "config": {"workload": workload, "m": M, "n": N, "cond": 1e6, "mode": head,
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}"},
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}",
+                   "tuning": tuning},
         "modes_ms": mode_ms, "modes": info,
         "gflops": round(svd_flops(M, N) / (ms * 1e-3) / 1e9, 1),
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": M * N * 4,

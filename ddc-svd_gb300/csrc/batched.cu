@@ -479,14 +479,17 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   int max_optin = 0;
   DDC_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
   const int vrow_floats = (int)((maxn + 3) & ~3);
-  const int bidiag_floats = std::max(1024, (max_optin - 2048) / (int)sizeof(float) - vrow_floats);
+  const int bidiag_floats = h->tune[TK_BATCH_SMEM_FULL]
+                                ? std::max(1024, (max_optin - 2048) / (int)sizeof(float) - vrow_floats)
+                                : smem_floats;
+  const int bthreads = (h->tune[TK_BATCH_THREADS] == 256) ? 256 : kBatchBidiagThreads;
   const size_t smem = sizeof(float) * ((size_t)vrow_floats + bidiag_floats);
   DDC_CUDA_TRY(cudaFuncSetAttribute(batch_bidiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
-  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_bidiag_kernel, kBatchBidiagThreads, smem));
+  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_bidiag_kernel, bthreads, smem));
   const int grid1 = std::max(1, std::min(batch, h->num_sms * std::max(occ, 1)));
   ktimer_begin(h, KC_BIDIAG);
-  batch_bidiag_kernel<<<grid1, kBatchBidiagThreads, smem, h->stream>>>(dt, dord, batch, counter, dA, W, d, e, tq,
+  batch_bidiag_kernel<<<grid1, bthreads, smem, h->stream>>>(dt, dord, batch, counter, dA, W, d, e, tq,
                                                                        tp, bidiag_floats, maxn);
   ktimer_end(h);
   count_launch();

@@ -715,7 +715,7 @@ struct Forest {
 };
 }  // namespace
 
-void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
+void dc_build_host(int N, const std::vector<int>& starts, DcHost& H, int terms_per_lane) {
   Forest T;
   const size_t cap = 2 * (size_t)N + 8;
   T.r0.reserve(cap); T.nn.reserve(cap); T.slot.reserve(cap); T.K.reserve(cap);
@@ -746,13 +746,14 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H) {
     for (int i = ds[d]; i < ds[d + 1]; i++) if (K[i] >= 0) dmerge.push_back(i);
   }
   dms[md + 1] = (int)dmerge.size();
-  // lanes per root at each depth: about 8 terms of the largest node per lane
+  // lanes per root at each depth: about terms_per_lane terms of the largest node per lane
+  const int tpl = std::max(1, terms_per_lane);
   std::vector<int> dgroup(md + 2, 1);
   for (int d = 0; d <= md; d++) {
     int mx = 0;
     for (int k = dms[d]; k < dms[d + 1]; k++) mx = std::max(mx, nn[dmerge[k]]);
     int G = 1;
-    while (G < 32 && G * 8 < mx) G <<= 1;
+    while (G < 32 && G * tpl < mx) G <<= 1;
     dgroup[d] = G;
   }
   H.nnodes = nnodes;

@@ -214,7 +214,7 @@ int gemm_simt(ddcsvd_context* ctx, int M, int N, int K1, Mat A1, Mat B1, int K2,
   const int Ktot = T1.K + T2.K;
   int ksplit = 1;
   if (scratch && !scratch->plan && tiles < ctx->num_sms && Ktot >= 4 * BK * 8) {
-    ksplit = std::min(16, std::max(1, (2 * ctx->num_sms) / tiles));
+    ksplit = std::min(std::max(1, ctx->tune[TK_SPLITK_MAX]), std::max(1, (2 * ctx->num_sms) / tiles));
     ksplit = std::min(ksplit, std::max(1, Ktot / (8 * BK)));
     while (ksplit > 1 && (size_t)ksplit * M * N * sizeof(float) > scratch->cap) ksplit--;
   }

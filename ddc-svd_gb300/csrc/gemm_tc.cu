@@ -461,7 +461,7 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   const int tiles = ceil_div(M, BM) * ceil_div(N, BN);
   int ksplit = 1;
   if (scratch && !scratch->plan && tiles < ctx->num_sms && p.nslab >= 8) {
-    ksplit = std::min(16, std::max(1, (2 * ctx->num_sms) / tiles));
+    ksplit = std::min(std::max(1, ctx->tune[TK_SPLITK_MAX]), std::max(1, (2 * ctx->num_sms) / tiles));
     ksplit = std::min(ksplit, p.nslab / 4);
     while (ksplit > 1 && (size_t)ksplit * M * N * sizeof(float) > scratch->cap) ksplit--;
   }
@@ -509,12 +509,13 @@ static int tc_dispatch(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, 
   }
   if (M <= 0 || N <= 0) return DDCSVD_OK;
   if ((a_koff & 3) || (b_koff & 3)) return DDCSVD_ERR_ARG;
+  const bool bn64 = (N <= 64) || ctx->tune[TK_TC_BN] == 64;
   if (kind == GEMM_TF32X6) {
-    if (N <= 64)
+    if (bn64)
       return tc::launch<64, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
     return tc::launch<128, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   }
-  if (N <= 64)
+  if (bn64)
     return tc::launch<64, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   return tc::launch<128, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
 }

@@ -33,8 +33,23 @@ struct ddcsvd_context {
   int kused = 0;
   float kern_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int kern_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // launch-configuration knobs (ddcsvd_set_tuning / ddcsvd_autotune_*); none
+  // of them changes the arithmetic beyond the summation order of split-K and
+  // of the D&C lane groups
+  int tune[8] = {16, 0, 512, 1, 8, 0, 0, 0};
   std::mutex mu;
 };
+
+namespace ddcsvd {
+enum TuneKnob {
+  TK_SPLITK_MAX = 0,     // cap on split-K pieces of the GEMMs (1 = no split)
+  TK_TC_BN = 1,          // tensor-core tile width: 0 = by N (64 if N <= 64 else 128), 64 = always 64
+  TK_BATCH_THREADS = 2,  // batched stage-1 CTA size (256 or 512)
+  TK_BATCH_SMEM_FULL = 3,// 1: batched stage-1 problems resident up to the opt-in limit, 0: up to 24K entries
+  TK_DC_TERMS = 4,       // D&C: secular-sum terms per lane that size the lane groups (2..32)
+  TK_COUNT = 5
+};
+}  // namespace ddcsvd
 
 namespace ddcsvd {
 
@@ -126,7 +141,7 @@ struct DcHost {
   int nnodes = 0, ndm = 0;
   std::vector<int> ints;  // packed node table uploaded to the device
 };
-void dc_build_host(int N, const std::vector<int>& block_starts, DcHost& H);
+void dc_build_host(int N, const std::vector<int>& block_starts, DcHost& H, int terms_per_lane = 8);
 size_t dc_max_ints(int N);
 int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, double* sigma,
              const DcHost* H, const int* dints, Arena& a, bool plan_only);

@@ -70,7 +70,7 @@ int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vecto
   }
   starts.push_back(N);
   // ---- D&C forest over all blocks
-  dc_build_host(N, starts, P->H);
+  dc_build_host(N, starts, P->H, ctx->tune[TK_DC_TERMS]);
   // ---- compact block storage and finalize tiles
   std::vector<long long> base(N);
   std::vector<int4> tiles;

@@ -153,6 +153,32 @@ class Handle:
               "get_kernel_times")
         return [float(x) for x in ms], [int(x) for x in nl]
 
+    TUNING_KNOBS = ("splitk_max", "tc_bn", "batch_threads", "batch_smem_full", "dc_terms")
+
+    @property
+    def tuning(self) -> dict:
+        """Launch knobs of this handle (see ddcsvd_get_tuning)."""
+        buf = (ctypes.c_int * len(self.TUNING_KNOBS))()
+        check(load().ddcsvd_get_tuning(self._h, ctypes.addressof(buf), len(buf)), "get_tuning")
+        return dict(zip(self.TUNING_KNOBS, (int(x) for x in buf)))
+
+    @tuning.setter
+    def tuning(self, values: dict) -> None:
+        cur = self.tuning
+        cur.update(values)
+        buf = (ctypes.c_int * len(self.TUNING_KNOBS))(*[cur[k] for k in self.TUNING_KNOBS])
+        check(load().ddcsvd_set_tuning(self._h, ctypes.addressof(buf), len(buf)), "set_tuning")
+
+    def autotune_svd(self, m: int, n: int, mode="auto", reps: int = 2) -> dict:
+        check(load().ddcsvd_autotune_svd(self._h, m, n, _mode(mode), reps), "autotune_svd")
+        return self.tuning
+
+    def autotune_batched(self, shapes, reps: int = 2) -> dict:
+        ms = np.ascontiguousarray([s[0] for s in shapes], dtype=np.int32)
+        ns = np.ascontiguousarray([s[1] for s in shapes], dtype=np.int32)
+        check(load().ddcsvd_autotune_batched(self._h, len(ms), _addr(ms), _addr(ns), reps), "autotune_batched")
+        return self.tuning
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             load().ddcsvd_destroy(self._h)

@@ -45,6 +45,10 @@ _SIGS = {
     "ddcsvd_last_error": (ctypes.c_char_p, []),
     "ddcsvd_kernel_launch_count": (c_ll, []),
     "ddcsvd_set_stage_timing": (c_int, [P, c_int]),
+    "ddcsvd_get_tuning": (c_int, [P, P, c_int]),
+    "ddcsvd_set_tuning": (c_int, [P, P, c_int]),
+    "ddcsvd_autotune_svd": (c_int, [P, c_int, c_int, c_int, c_int]),
+    "ddcsvd_autotune_batched": (c_int, [P, c_int, P, P, c_int]),
     "ddcsvd_get_stage_times": (c_int, [P, P]),
     "ddcsvd_get_kernel_times": (c_int, [P, P, P, c_int]),
 }

@@ -184,6 +184,30 @@ int ddcsvd_svd_backward_f64_noalloc(void *stream, int batch, int m, int n, const
                                     const double *dS, const double *dV, const double *gU,
                                     const double *gS, const double *gV, double *gA);
 
+/* ---------------------------------------------------------------- autotuning */
+
+/* No counterpart in the reference (the reference has no launch parameters).
+ * Launch knobs of a handle, in this order:
+ *   [0] split-K cap of the GEMMs (1 = never split, default 16)
+ *   [1] tensor-core tile width (0 = by the output width, 64 = always 64)
+ *   [2] batched stage-1 CTA size (256 or 512, default 512)
+ *   [3] batched stage-1 residency (1 = whole problem in shared memory up to
+ *       the SM's opt-in limit, default; 0 = up to 24K entries, two CTAs/SM)
+ *   [4] D&C secular-sum terms per lane (2..32, default 8)
+ * None changes the results beyond the summation order of split-K and of the
+ * D&C sums.  get/set copy up to `count` knobs. */
+int ddcsvd_get_tuning(ddcsvd_handle_t handle, int *values, int count);
+int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);
+
+/* Coordinate search over the knobs on seeded synthetic data of the given
+ * single-matrix shape / batch of shapes (host arrays m, n), timed with CUDA
+ * events on the handle's stream, `reps` timed runs per candidate; the
+ * fastest values stay in the handle.  Allocates its own device buffers.
+ * The single-matrix tuner covers knobs [0] and [1], the batched tuner
+ * [2], [3] and [4]. */
+int ddcsvd_autotune_svd(ddcsvd_handle_t handle, int m, int n, int mode, int reps);
+int ddcsvd_autotune_batched(ddcsvd_handle_t handle, int batch, const int *m, const int *n, int reps);
+
 /* ---------------------------------------------------------------- GEMM back ends */
 
 /* The GEMM back ends of the pipeline, exposed for validation and reuse:
