@@ -154,6 +154,13 @@ __global__ void zero_rows_kernel(int r0, int r1, int ncols, float* C, int ldc) {
     C[r + (size_t)c * ldc] = 0.f;
 }
 
+// R (n x n) = upper triangle of the first n rows of W
+__global__ void triu_kernel(int n, const float* __restrict__ W, int ldw, float* R, int ldr) {
+  const int c = blockIdx.y;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ldr; r += gridDim.x * blockDim.x)
+    R[r + (size_t)c * ldr] = (r <= c && r < n) ? W[r + (size_t)c * ldw] : 0.f;
+}
+
 __global__ void finite_check_kernel(int m, int n, const float* A, int lda, DevStatus* st) {
   const size_t tot = (size_t)m * n;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
@@ -183,6 +190,9 @@ static int stage_event(ddcsvd_context* ctx, int k) {
 // reused by each stage in turn.
 static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                          int ldu, float* dV, int ldv, int mode, bool check_finite);
+static bool use_tall_qr(int m, int n, int mode);
+static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU, int ldu,
+                       float* dV, int ldv, int mode, bool check_finite);
 
 __global__ void copy2d_kernel(int rows, int cols, const float* __restrict__ src, int lds, float* dst, int ldd) {
   const int c = blockIdx.y;
@@ -197,14 +207,17 @@ static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda,
                     int ldu, float* dV, int ldv, int mode, bool check_finite) {
   const bool tcmode = (mode >= DDCSVD_MODE_BLOCKED_TF32X3);
   auto ok = [](const float* p, int ld) { return ((reinterpret_cast<uintptr_t>(p) & 15) == 0) && (ld % 4 == 0); };
+  const bool tall = use_tall_qr(m, n, mode);
   if (!tcmode || (ok(dU, ldu) && ok(dV, ldv)))
-    return svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
+    return tall ? svd_tall_qr(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite)
+                : svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
   const int lu = (int)round_up(m, 4), lv = (int)round_up(n, 4);
   float* buf = nullptr;
   DDC_CUDA_TRY(cudaMallocAsync((void**)&buf, sizeof(float) * ((size_t)lu * n + (size_t)lv * n + 64), ctx->stream));
   float* Ui = buf;
   float* Vi = buf + (size_t)lu * n + 32;
-  int rc = svd_core_impl(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite);
+  int rc = tall ? svd_tall_qr(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite)
+                : svd_core_impl(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite);
   if (rc == DDCSVD_OK) {
     copy2d_kernel<<<dim3(ceil_div(m, 256), n), 256, 0, ctx->stream>>>(m, n, Ui, lu, dU, ldu);
     copy2d_kernel<<<dim3(ceil_div(n, 256), n), 256, 0, ctx->stream>>>(n, n, Vi, lv, dV, ldv);
@@ -257,8 +270,10 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   a.base = (char*)ctx->ws;
   region_a(a, pl);
   // ---- stage 1
-  DDC_TRY(reset_status(ctx));
-  ctx->kused = 0;
+  if (!ctx->nested) {
+    DDC_TRY(reset_status(ctx));
+    ctx->kused = 0;
+  }
   DDC_TRY(stage_event(ctx, 0));
   if (check_finite) {
     finite_check_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(m, n, dA, lda, ctx->d_status);
@@ -331,8 +346,80 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   int rc = check_status(ctx, "svd");
   if (ctx->timing && rc == DDCSVD_OK) {
     for (int k = 0; k < 4; k++) cudaEventElapsedTime(&ctx->stage_ms[k], ctx->ev[k], ctx->ev[k + 1]);
-    ktimer_collect(ctx);
+    if (!ctx->nested) ktimer_collect(ctx);
   }
+  return rc;
+}
+
+// Tall matrices (m >= 2n): Householder QR first (one-barrier-per-column panel
+// kernel, tensor-core trailing updates), the SVD of the n x n factor R, then
+// U = Q [U_R; 0] with the QR reflectors (the back-transformation machinery).
+// The bidiagonalisation then runs on n x n instead of m x n: the GEMV half
+// moves 2 * 4 * n^3 / 3 bytes instead of 2 * 4 * (m - n/3) n^2 / 2.
+static bool use_tall_qr(int m, int n, int mode) {
+  return mode >= DDCSVD_MODE_BLOCKED_TF32X3 && m >= 2 * n && n >= 128 && getenv("DDCSVD_NO_QR") == nullptr;
+}
+
+static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU, int ldu,
+                       float* dV, int ldv, int mode, bool check_finite) {
+  const GemmKind kind = kind_of(mode);
+  const int ldq = (int)round_up(m, 32), ldr = (int)round_up(n, 32);
+  const int P = ctx->num_sms;
+  Arena plan;
+  plan.take<float>((size_t)ldq * n);      // Wq
+  plan.take<float>(n + 4);                // tau
+  plan.take<unsigned>(4);                 // amax
+  plan.take<float>((size_t)ldr * n);      // R
+  QrWork qw;
+  plan_qr(plan, m, n, P, kind, &qw);
+  char* buf = nullptr;
+  if (cudaMallocAsync((void**)&buf, plan.off + 4096, ctx->stream) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("cudaMallocAsync of %zu bytes for the QR path failed", plan.off + 4096);
+    return DDCSVD_ERR_ALLOC;
+  }
+  Arena a;
+  a.plan = false;
+  a.base = buf;
+  float* Wq = a.take<float>((size_t)ldq * n);
+  float* tau = a.take<float>(n + 4);
+  unsigned* amax = a.take<unsigned>(4);
+  float* R = a.take<float>((size_t)ldr * n);
+  plan_qr(a, m, n, P, kind, &qw);
+  int rc = DDCSVD_OK;
+  do {
+    if ((rc = reset_status(ctx))) break;
+    ctx->kused = 0;
+    if (check_finite) {
+      finite_check_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(m, n, dA, lda, ctx->d_status);
+      count_launch();
+    }
+    copy_pad_kernel<<<dim3(ceil_div(ldq, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, Wq, ldq);
+    count_launch();
+    if ((rc = range_scale_matrix(ctx, m, n, Wq, ldq, amax))) break;
+    if ((rc = qr_blocked(ctx, m, n, Wq, ldq, tau, qw, kind))) break;
+    triu_kernel<<<dim3(ceil_div(ldr, 256), n), 256, 0, ctx->stream>>>(n, Wq, ldq, R, ldr);
+    count_launch();
+    ctx->nested = true;
+    rc = svd_core_impl(ctx, n, n, R, ldr, dS, dU, ldu, dV, ldv, mode, false);
+    ctx->nested = false;
+    if (rc) break;
+    // U = Q [U_R; 0]
+    zero_rows_kernel<<<dim3(std::min(ceil_div(m - n, 256), 64), n), 256, 0, ctx->stream>>>(n, m, n, dU, ldu);
+    count_launch();
+    Arena p2;
+    DDC_TRY(apply_left_reflectors(ctx, m, n, nullptr, ldq, nullptr, dU, ldu, n, kind, false, p2, true));
+    if ((rc = ensure_workspace(ctx, p2.off + 4096))) break;
+    Arena w2;
+    w2.plan = false;
+    w2.base = (char*)ctx->ws;
+    if ((rc = apply_left_reflectors(ctx, m, n, Wq, ldq, tau, dU, ldu, n, kind, false, w2, false))) break;
+    if ((rc = range_unscale_vector(ctx, n, dS, amax))) break;
+    rc = check_status(ctx, "svd (QR path)");
+  } while (0);
+  ctx->nested = false;
+  cudaFreeAsync(buf, ctx->stream);
+  if (rc == DDCSVD_OK && ctx->timing) ktimer_collect(ctx);
   return rc;
 }
 

@@ -109,7 +109,8 @@ __host__ __device__ inline long long ut_offset(int b, int rows_total) {
 // C -= UT_b (U_b^T C): two tensor-core products and no per-block small kernels.
 constexpr int kPrepRows = 32;
 __global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nref, const float* __restrict__ Uc,
-                                                         int ldu, const float* __restrict__ tau, float* UT) {
+                                                         int ldu, const float* __restrict__ tau, float* UT,
+                                                         int transT) {
   __shared__ float sU[kPrepRows][kWY + 1];
   __shared__ float sG[kWY][kWY + 1];
   __shared__ float sT[kWY][kWY + 1];
@@ -174,6 +175,19 @@ __global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nre
       __syncthreads();
     }
   }
+  // Q^T = I - U T^T U^T (applying the block from the left as a transpose, as
+  // a QR factorisation does): use T^T
+  if (transT) {
+    for (int idx = t; idx < kWY * kWY; idx += 256) {
+      const int r = idx % kWY, c = idx / kWY;
+      if (r < c) {
+        const float x = sT[r][c];
+        sT[r][c] = sT[c][r];
+        sT[c][r] = x;
+      }
+    }
+    __syncthreads();
+  }
   // ---- UT = U T: thread owns row t/8 of the tile and 8 consecutive columns
   {
     const int rr = t >> 3, c0 = (t & 7) * 8;
@@ -200,6 +214,17 @@ __global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nre
   }
 }
 
+// One block of at most kWY reflectors (columns of Vp, unit lower
+// trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kWY columns.
+int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
+                     bool transT) {
+  if (nb > kWY || rows <= 0) return DDCSVD_ERR_ARG;
+  wy_prepare_kernel<<<1, 256, 0, ctx->stream>>>(rows, nb, Vp, ldv, tau, UT, transT ? 1 : 0);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
 // last first:  W1 = U_b^T C (stored K-major for the next product) and
 // C -= UT_b W1.
@@ -220,7 +245,7 @@ static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int n
   scratch.cap = sbytes;
   build_reflectors_kernel<<<dim3(ceil_div(ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
       side, rows_total, nref, W, ldw, tau, Uc, ldu);
-  wy_prepare_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, tau, UT);
+  wy_prepare_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, tau, UT, 0);
   count_launch(2);
   DDC_CUDA_TRY(cudaGetLastError());
   for (int bi = nblk - 1; bi >= 0; bi--) {

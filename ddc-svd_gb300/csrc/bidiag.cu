@@ -774,6 +774,106 @@ __global__ void range_unscale_kernel(int n, float* d, float* e, const unsigned* 
 }
 
 // ------------------------------------------------------------------------
+// QR preprocessing of tall matrices (m >= 2n): Householder QR, panels of
+// kPanel columns.  One persistent cooperative kernel per panel; CTAs own rows
+// and keep their rows of the panel in shared memory for the whole panel.  Per
+// column a single grid barrier: the reflector's dot products with the panel's
+// remaining columns are formed from the unscaled column,
+//   w_c = scale * sum_{r > i} x_r a_rc + a_ic,
+// so the norm and the dots share one reduction; records and the published row
+// i are double-buffered by column parity (a CTA can be at most one column
+// ahead of any other).  Same reflector convention as the bidiagonalisation.
+// ------------------------------------------------------------------------
+struct QrParams {
+  int m, k0, nb, ldw, P, rc;
+  float* W;
+  float* tau;
+  float* Vp;  // masked unit-lower reflectors of the panel, rows k0.. (ld ldv)
+  int ldv;
+  float* part;  // [2][P][kPS]
+  float* rowi;  // [2][kPanel + 4]: row i of the panel, published by its owner
+  GridBarrier* bar;
+  DevStatus* st;
+};
+
+size_t qr_smem_bytes(int rc, int threads) {
+  return sizeof(float) * ((size_t)rc * kLD + (size_t)(threads / 32) * (kPS + 4) + kPS + 4 + kPanel + 4 + 16) + 64;
+}
+
+__global__ void __launch_bounds__(kBidiagThreads, 1) qr_panel_kernel(QrParams p) {
+  extern __shared__ __align__(16) float smem[];
+  const int t = threadIdx.x, wid = t >> 5, lane = t & 31, nw = blockDim.x >> 5, b = blockIdx.x;
+  const int m = p.m, k0 = p.k0, nb = p.nb, ldw = p.ldw;
+  const int ra = (k0 & ~3) + b * p.rc, rb = min(m, ra + p.rc);
+  const int nrow = max(0, rb - ra);
+  float* As = smem;  // own rows of the panel, [row][kLD]
+  float* redp = As + (size_t)p.rc * kLD;
+  float* tot = redp + nw * (kPS + 4);
+  float* Ri = tot + kPS + 4;
+  FF* nrm = reinterpret_cast<FF*>(reinterpret_cast<uintptr_t>(Ri + kPanel + 4 + 1) & ~(uintptr_t)7);
+  float* W = p.W;
+  for (int idx = t; idx < nrow * nb; idx += blockDim.x) {
+    const int lr = idx % nrow, c = idx / nrow;
+    As[lr * kLD + c] = W[ra + lr + (size_t)(k0 + c) * ldw];
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; j++) {
+    const int i = k0 + j;
+    float* part = p.part + (size_t)(j & 1) * p.P * kPS;
+    float* rowi = p.rowi + (j & 1) * (kPanel + 4);
+    const int r1 = max(ra, i + 1);
+    if (i >= ra && i < rb)  // the owner of row i publishes a_ic, c >= j
+      for (int c = j + t; c < nb; c += blockDim.x) rowi[c] = As[(i - ra) * kLD + c];
+    if (wid == 0) {
+      FF acc{0.f, 0.f};
+      for (int r = r1 + lane; r < rb; r += 32) acc = ff_add_sq(acc, As[(r - ra) * kLD + j]);
+      acc = warp_sum_ff(acc);
+      if (lane == 0) *reinterpret_cast<float2*>(part + (size_t)b * kPS + kPS - 2) = make_float2(acc.hi, acc.lo);
+    } else if (t >= 32 && t < 32 + (nb - j - 1)) {
+      const int c = j + 1 + (t - 32);
+      float acc = 0.f;
+      for (int r = r1; r < rb; r++) acc += As[(r - ra) * kLD + j] * As[(r - ra) * kLD + c];
+      part[(size_t)b * kPS + (c - j - 1)] = acc;
+    }
+    if (!grid_sync(p.bar, p.P, p.st, 40)) return;
+    if (t >= 64 && t < 64 + (nb - j)) Ri[t - 64] = __ldcg(rowi + j + (t - 64));  // Ri[0] = x0
+    reduce_partials(part, p.P, nb - j - 1, redp, tot, nrm);
+    float alpha, tq, sq;
+    householder_ff(Ri[0], *nrm, &alpha, &tq, &sq);
+    if (t == 0 && b == 0) p.tau[i] = tq;
+    // columns c > j of the own rows r >= i (v_i = 1, v_r = scale x_r)
+    for (int idx = t; idx < nrow * (nb - j - 1); idx += blockDim.x) {
+      const int lr = idx % nrow, c = j + 1 + idx / nrow, r = ra + lr;
+      if (r < i) continue;
+      const float w = sq * tot[c - j - 1] + Ri[c - j];
+      const float v = (r == i) ? 1.f : sq * As[lr * kLD + j];
+      As[lr * kLD + c] -= tq * v * w;
+    }
+    __syncthreads();
+    for (int lr = t; lr < nrow; lr += blockDim.x) {
+      const int r = ra + lr;
+      if (r == i) As[lr * kLD + j] = alpha;
+      else if (r > i) As[lr * kLD + j] *= sq;
+    }
+    __syncthreads();
+  }
+  // write back; the masked reflectors go to Vp for the trailing update
+  for (int idx = t; idx < nrow * nb; idx += blockDim.x) {
+    const int lr = idx % nrow, c = idx / nrow, r = ra + lr;
+    const float a = As[lr * kLD + c];
+    W[r + (size_t)(k0 + c) * ldw] = a;
+    if (r >= k0) p.Vp[(r - k0) + (size_t)c * p.ldv] = (r < k0 + c) ? 0.f : (r == k0 + c ? 1.f : a);
+  }
+}
+
+__global__ void range_unscale_vec_kernel(int n, float* x, const unsigned* amax) {
+  const float s = range_scale(*amax);
+  if (s == 1.f) return;
+  const float inv = 1.f / s;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] *= inv;
+}
+
+// ------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------
 int bidiag_coop_ctas(ddcsvd_context* ctx, int m, int n) {
@@ -895,6 +995,69 @@ int bidiag_plain(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d,
   int rc = launch_coop((const void*)bidiag_plain_kernel, w.P, kBidiagThreads, smem, &pp, ctx->stream);
   ktimer_end(ctx);
   return rc;
+}
+
+int range_scale_matrix(ddcsvd_context* ctx, int m, int n, float* W, int ldw, unsigned* amax) {
+  const int sg = std::min(n, 4 * ctx->num_sms);
+  DDC_CUDA_TRY(cudaMemsetAsync(amax, 0, sizeof(unsigned), ctx->stream));
+  range_scan_kernel<<<sg, 256, 0, ctx->stream>>>(m, n, W, ldw, amax);
+  range_apply_kernel<<<sg, 256, 0, ctx->stream>>>(m, n, W, ldw, amax);
+  count_launch(2);
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+int range_unscale_vector(ddcsvd_context* ctx, int n, float* x, const unsigned* amax) {
+  range_unscale_vec_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(n, x, amax);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+void plan_qr(Arena& a, int m, int n, int P, GemmKind kind, QrWork* w) {
+  w->ldv = (int)round_up(m, 32);
+  w->P = P;
+  w->Vp = a.take<float>((size_t)w->ldv * kPanel);
+  w->UT = a.take<float>((size_t)m * kWY + 64);
+  w->W1s = a.take<float>((size_t)n * kWY + 64);
+  w->part = a.take<float>((size_t)2 * P * kPS + 64);
+  w->rowi = a.take<float>(2 * (kPanel + 4));
+  w->bar = a.take<GridBarrier>(4);
+  w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kWY, m);
+  w->gemm_scratch = a.take<char>(w->gemm_scratch_bytes);
+}
+
+int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau, QrWork& w, GemmKind kind) {
+  if (m < n || n <= 0) return DDCSVD_ERR_ARG;
+  Arena sc;
+  sc.base = w.gemm_scratch;
+  sc.plan = false;
+  sc.cap = w.gemm_scratch_bytes;
+  for (int k0 = 0; k0 < n; k0 += kPanel) {
+    const int nb = std::min(kPanel, n - k0);
+    QrParams q;
+    q.m = m; q.k0 = k0; q.nb = nb; q.ldw = ldw; q.P = w.P;
+    q.rc = (int)round_up(ceil_div(m - (k0 & ~3), w.P), 4);
+    q.W = W; q.tau = tau; q.Vp = w.Vp; q.ldv = w.ldv;
+    q.part = w.part; q.rowi = w.rowi; q.bar = w.bar; q.st = ctx->d_status;
+    DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
+    ktimer_begin(ctx, KC_QR);
+    DDC_TRY(launch_coop((const void*)qr_panel_kernel, w.P, kBidiagThreads, qr_smem_bytes(q.rc, kBidiagThreads), &q,
+                        ctx->stream));
+    ktimer_end(ctx);
+    if (k0 + nb < n) {
+      // W[k0:, k0+nb:] := (I - V T^T V^T) W[k0:, k0+nb:] on tensor cores
+      const int rows = m - k0, ncols = n - k0 - nb;
+      ktimer_begin(ctx, KC_QR);
+      DDC_TRY(wy_prepare_block(ctx, rows, nb, w.Vp, w.ldv, tau + k0, w.UT, true));
+      DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, nb, rows, W + (size_t)(k0 + nb) * ldw, ldw, k0, w.Vp, w.ldv, 0,
+                               w.W1s, kWY, 1.f, 0.f, &sc));
+      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kWY, 0, w.W1s, kWY, 0,
+                             W + k0 + (size_t)(k0 + nb) * ldw, ldw, -1.f, 1.f, &sc));
+      ktimer_end(ctx);
+    }
+  }
+  return DDCSVD_OK;
 }
 
 int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw, const float* d,

@@ -37,6 +37,8 @@ struct ddcsvd_context {
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
   int tune[8] = {16, 0, 512, 1, 8, 0, 0, 0};
+  // set while an SVD of the R factor runs inside the tall-matrix path
+  bool nested = false;
   std::mutex mu;
 };
 
@@ -69,7 +71,7 @@ struct Arena {
 };
 
 // Kernel classes for ddcsvd_get_kernel_times.
-enum KernelClass { KC_BIDIAG = 0, KC_TRAIL_GEMM = 1, KC_DC = 2, KC_VECTORS = 3, KC_BACKXFORM = 4 };
+enum KernelClass { KC_BIDIAG = 0, KC_TRAIL_GEMM = 1, KC_DC = 2, KC_VECTORS = 3, KC_BACKXFORM = 4, KC_QR = 5 };
 void ktimer_begin(ddcsvd_context* ctx, int cls);  // no-ops unless timing is on
 void ktimer_end(ddcsvd_context* ctx);
 void ktimer_collect(ddcsvd_context* ctx);        // after a stream sync
@@ -172,6 +174,25 @@ int apply_left_reflectors(ddcsvd_context* ctx, int m, int nref, const float* W, 
 int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W, int ldw,
                            const float* taup, float* C, int ldc, int ncols, GemmKind kind,
                            bool plain, Arena& a, bool plan_only);
+
+int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
+                     bool transT);
+// Householder QR of the m x n (m >= n) matrix W in place (R on and above the
+// diagonal, reflectors below in LAPACK form, tau separate), tensor-core
+// trailing updates; the input must be range-scaled (max|a| in [2^-40, 2^40]).
+struct QrWork {
+  float *Vp, *UT, *W1s, *part, *rowi;
+  GridBarrier* bar;
+  char* gemm_scratch;
+  size_t gemm_scratch_bytes;
+  int ldv, P;
+};
+void plan_qr(Arena& a, int m, int n, int P, GemmKind kind, QrWork* w);
+int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau, QrWork& w, GemmKind kind);
+// Range scaling of an m x n matrix in place (power of two; scale 1 when max|a|
+// is already in range); amax receives the bit pattern that range_scale uses.
+int range_scale_matrix(ddcsvd_context* ctx, int m, int n, float* W, int ldw, unsigned* amax);
+int range_unscale_vector(ddcsvd_context* ctx, int n, float* x, const unsigned* amax);
 
 // Explicit U (m x m) or V (n x n) from the reference's FP64 reflector storage
 // (device buffers; scratch: n * n doubles for V).

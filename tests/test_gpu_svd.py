@@ -164,6 +164,24 @@ def test_svd_large_shapes(lib, cuda, orc, m, n):
     check_metrics(orc, A, s, U, V)
 
 
+@pytest.mark.parametrize("m,n,kind", [(600, 256, "uniform"), (1200, 200, "graded"), (256, 700, "uniform"),
+                                      (2048, 130, "rank_deficient")])
+def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
+    """m >= 2n (or n >= 2m) in the tensor-core modes goes through Householder
+    QR, the SVD of R and U = Q [U_R; 0]."""
+    if not _mode_available(lib, "tf32x6"):
+        pytest.skip("tf32x6 unavailable")
+    rng = np.random.default_rng(m + 7 * n)
+    if kind == "graded":
+        A = graded(n, seed=3, m=m)[0].astype(np.float32)
+    elif kind == "rank_deficient":
+        A = (rng.uniform(-1, 1, (m, 40)) @ rng.uniform(-1, 1, (40, n))).astype(np.float32)
+    else:
+        A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    s, U, V = run(lib, cuda, A, "tf32x6")
+    check_metrics(orc, A, s, U, V)
+
+
 def _form_factors_numpy(A_mod, left):
     """The reference's form_u_par / form_v_par loops (bidiag_par.c:877-988), restated in numpy."""
     m, n = A_mod.shape
