@@ -190,7 +190,7 @@ static int stage_event(ddcsvd_context* ctx, int k) {
 // reused by each stage in turn.
 static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                          int ldu, float* dV, int ldv, int mode, bool check_finite);
-static bool use_tall_qr(int m, int n, int mode);
+static bool use_tall_qr(const ddcsvd_context* ctx, int m, int n, int mode);
 static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU, int ldu,
                        float* dV, int ldv, int mode, bool check_finite);
 
@@ -207,7 +207,7 @@ static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda,
                     int ldu, float* dV, int ldv, int mode, bool check_finite) {
   const bool tcmode = (mode >= DDCSVD_MODE_BLOCKED_TF32X3);
   auto ok = [](const float* p, int ld) { return ((reinterpret_cast<uintptr_t>(p) & 15) == 0) && (ld % 4 == 0); };
-  const bool tall = use_tall_qr(m, n, mode);
+  const bool tall = use_tall_qr(ctx, m, n, mode);
   if (!tcmode || (ok(dU, ldu) && ok(dV, ldv)))
     return tall ? svd_tall_qr(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite)
                 : svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
@@ -356,8 +356,12 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
 // U = Q [U_R; 0] with the QR reflectors (the back-transformation machinery).
 // The bidiagonalisation then runs on n x n instead of m x n: the GEMV half
 // moves 2 * 4 * n^3 / 3 bytes instead of 2 * 4 * (m - n/3) n^2 / 2.
-static bool use_tall_qr(int m, int n, int mode) {
-  return mode >= DDCSVD_MODE_BLOCKED_TF32X3 && m >= 2 * n && n >= 128 && getenv("DDCSVD_NO_QR") == nullptr;
+static bool use_tall_qr(const ddcsvd_context* ctx, int m, int n, int mode) {
+  if (mode < DDCSVD_MODE_BLOCKED_TF32X3 || m < 2 * n || n < 128) return false;
+  const int k = ctx->tune[TK_TALL_QR];
+  // auto: when the matrix no longer fits the L2-resident regime of the
+  // one-stage GEMVs (measured: 16384 x 8192 gains 1.3x, 8192 x 4096 loses 10%)
+  return k == 1 || (k == 2 && (long long)m * n >= (64ll << 20));
 }
 
 static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU, int ldu,

@@ -102,66 +102,93 @@ __host__ __device__ inline long long ut_offset(int b, int rows_total) {
   return (long long)kWY * ((long long)b * rows_total - (long long)kWY * b * (b - 1) / 2);
 }
 
-// One CTA per WY block b (reflectors j0 = b kWY ... j0 + bs - 1, rows
-// [j0, rows_total) of Uc):  G = U_b^T U_b,  the compact-WY factor T_b
-// (T[l,l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l]), and
-// UT_b = U_b T_b (row-major, ld kWY), so that applying the block is
-// C -= UT_b (U_b^T C): two tensor-core products and no per-block small kernels.
-constexpr int kPrepRows = 32;
-__global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nref, const float* __restrict__ Uc,
-                                                         int ldu, const float* __restrict__ tau, float* UT,
-                                                         int transT) {
+// WY preparation of every block b (reflectors j0 = b kWY ... j0 + bs - 1,
+// rows [j0, rows_total) of Uc), in three row-parallel kernels:
+//   wy_gram_kernel     grid (block, row chunk): partial G = U^T U of a chunk
+//   wy_tfactor_kernel  grid (block): G = sum of the chunk partials in chunk
+//                      order, then the compact-WY factor T
+//                      (T[l,l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l])
+//   wy_ut_kernel       grid (block, row chunk): UT = U T (row-major, ld kWY)
+// so that applying the block is C -= UT (U^T C) (or, with T^T, the
+// transposed block of a QR factorisation).  A single CTA per block had cost
+// 1.3 ms for an 8192-row block.
+constexpr int kPrepRows = 32;    // rows per shared-memory tile
+constexpr int kChunkRows = 512;  // rows per CTA of the chunked kernels
+
+__device__ __forceinline__ void wy_block_geom(int b, int rows_total, int nref, int& j0, int& bs, int& rows) {
+  j0 = b * kWY;
+  bs = min(kWY, nref - j0);
+  rows = rows_total - j0;
+}
+
+__device__ __forceinline__ void wy_load_tile(float (*sU)[kWY + 1], const float* U, int ldu, int r0, int rend,
+                                             int bs) {
+  for (int idx = threadIdx.x; idx < kPrepRows * kWY; idx += blockDim.x) {
+    const int rr = idx & (kPrepRows - 1), c = idx / kPrepRows;
+    const int r = r0 + rr;
+    sU[rr][c] = (r < rend && c < bs) ? U[r + (size_t)c * ldu] : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) wy_gram_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
+                                                      float* Gp, int nchunk) {
   __shared__ float sU[kPrepRows][kWY + 1];
+  int j0, bs, rows;
+  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
+  const int c0 = blockIdx.y * kChunkRows;
+  if (bs <= 0 || c0 >= rows) return;
+  const int c1 = min(rows, c0 + kChunkRows);
+  const float* U = Uc + j0 + (size_t)j0 * ldu;
+  const int t = threadIdx.x, ti = t & 15, tj = t >> 4;
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[a][c] = 0.f;
+  for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
+    __syncthreads();
+    wy_load_tile(sU, U, ldu, r0, c1, bs);
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < kPrepRows; k++) {
+      float x[4], y[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        x[a] = sU[k][4 * ti + a];
+        y[a] = sU[k][4 * tj + a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[a][c] += x[a] * y[c];
+    }
+  }
+  float* G = Gp + ((size_t)blockIdx.x * nchunk + blockIdx.y) * kWY * kWY;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) G[(4 * ti + a) + (size_t)(4 * tj + c) * kWY] = acc[a][c];
+}
+
+__global__ void __launch_bounds__(256) wy_tfactor_kernel(int rows_total, int nref, const float* __restrict__ tau,
+                                                         const float* __restrict__ Gp, int nchunk, float* Tout,
+                                                         int transT) {
   __shared__ float sG[kWY][kWY + 1];
   __shared__ float sT[kWY][kWY + 1];
-  const int b = blockIdx.x, t = threadIdx.x;
-  const int j0 = b * kWY, bs = min(kWY, nref - j0);
-  const int rows = rows_total - j0;
+  int j0, bs, rows;
+  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
   if (bs <= 0 || rows <= 0) return;
-  const float* U = Uc + j0 + (size_t)j0 * ldu;  // U_b(r, c) = U[r + c * ldu]
-  float* out = UT + ut_offset(b, rows_total);
-  auto load_tile = [&](int r0) {
-    for (int idx = t; idx < kPrepRows * kWY; idx += 256) {
-      const int rr = idx & (kPrepRows - 1), c = idx / kPrepRows;
-      const int r = r0 + rr;
-      sU[rr][c] = (r < rows && c < bs) ? U[r + (size_t)c * ldu] : 0.f;
-    }
-  };
-  // ---- G = U^T U: thread owns the 4 x 4 block (4 ti .., 4 tj ..)
-  {
-    const int ti = t & 15, tj = t >> 4;
-    float acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) acc[a][c] = 0.f;
-    for (int r0 = 0; r0 < rows; r0 += kPrepRows) {
-      __syncthreads();
-      load_tile(r0);
-      __syncthreads();
-#pragma unroll 8
-      for (int k = 0; k < kPrepRows; k++) {
-        float x[4], y[4];
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-          x[a] = sU[k][4 * ti + a];
-          y[a] = sU[k][4 * tj + a];
-        }
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) acc[a][c] += x[a] * y[c];
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) sG[4 * ti + a][4 * tj + c] = acc[a][c];
-    for (int idx = t; idx < kWY * kWY; idx += 256) sT[idx & (kWY - 1)][idx / kWY] = 0.f;
+  const int nc = ceil_div(rows, kChunkRows);
+  const int t = threadIdx.x;
+  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) {
+    const int r = idx % kWY, c = idx / kWY;
+    float g = 0.f;
+    for (int s = 0; s < nc; s++) g += Gp[((size_t)blockIdx.x * nchunk + s) * kWY * kWY + idx];
+    sG[r][c] = g;
+    sT[r][c] = 0.f;
   }
   __syncthreads();
-  // ---- T: column l from the finished columns 0..l-1; four threads per row
-  {
+  {  // column l from the finished columns 0..l-1; four threads per row
     const int row = t >> 2, part = t & 3;
     for (int l = 0; l < bs; l++) {
       float sum = 0.f;
@@ -175,54 +202,80 @@ __global__ void __launch_bounds__(256) wy_prepare_kernel(int rows_total, int nre
       __syncthreads();
     }
   }
-  // Q^T = I - U T^T U^T (applying the block from the left as a transpose, as
-  // a QR factorisation does): use T^T
-  if (transT) {
-    for (int idx = t; idx < kWY * kWY; idx += 256) {
-      const int r = idx % kWY, c = idx / kWY;
-      if (r < c) {
-        const float x = sT[r][c];
-        sT[r][c] = sT[c][r];
-        sT[c][r] = x;
-      }
-    }
-    __syncthreads();
+  // T (or T^T for a block applied as a transpose) to global, [row + col * kWY]
+  float* T = Tout + (size_t)blockIdx.x * kWY * kWY;
+  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) {
+    const int r = idx % kWY, c = idx / kWY;
+    T[idx] = transT ? sT[c][r] : sT[r][c];
   }
-  // ---- UT = U T: thread owns row t/8 of the tile and 8 consecutive columns
-  {
-    const int rr = t >> 3, c0 = (t & 7) * 8;
-    for (int r0 = 0; r0 < rows; r0 += kPrepRows) {
-      __syncthreads();
-      load_tile(r0);
-      __syncthreads();
-      float acc[8];
+}
+
+__global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
+                                                    const float* __restrict__ Tin, float* UT) {
+  __shared__ float sU[kPrepRows][kWY + 1];
+  __shared__ float sT[kWY][kWY + 1];
+  int j0, bs, rows;
+  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
+  const int c0 = blockIdx.y * kChunkRows;
+  if (bs <= 0 || c0 >= rows) return;
+  const int c1 = min(rows, c0 + kChunkRows);
+  const float* U = Uc + j0 + (size_t)j0 * ldu;
+  float* out = UT + ut_offset(blockIdx.x, rows_total);
+  const int t = threadIdx.x;
+  const float* T = Tin + (size_t)blockIdx.x * kWY * kWY;
+  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) sT[idx % kWY][idx / kWY] = T[idx];
+  const int rr = t >> 3, cb = (t & 7) * 8;  // thread: row rr of a tile, 8 consecutive columns
+  for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
+    __syncthreads();
+    wy_load_tile(sU, U, ldu, r0, c1, bs);
+    __syncthreads();
+    float acc[8];
 #pragma unroll
-      for (int c = 0; c < 8; c++) acc[c] = 0.f;
+    for (int c = 0; c < 8; c++) acc[c] = 0.f;
 #pragma unroll 8
-      for (int k = 0; k < kWY; k++) {
-        const float x = sU[rr][k];
+    for (int k = 0; k < kWY; k++) {
+      const float x = sU[rr][k];
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[c] += x * sT[k][c0 + c];
-      }
-      const int r = r0 + rr;
-      if (r < rows) {
-        float4* o = reinterpret_cast<float4*>(out + (size_t)r * kWY + c0);
-        o[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-        o[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
-      }
+      for (int c = 0; c < 8; c++) acc[c] += x * sT[k][cb + c];
+    }
+    const int r = r0 + rr;
+    if (r < c1) {
+      float4* o = reinterpret_cast<float4*>(out + (size_t)r * kWY + cb);
+      o[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      o[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
     }
   }
 }
 
-// One block of at most kWY reflectors (columns of Vp, unit lower
-// trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kWY columns.
-int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
-                     bool transT) {
-  if (nb > kWY || rows <= 0) return DDCSVD_ERR_ARG;
-  wy_prepare_kernel<<<1, 256, 0, ctx->stream>>>(rows, nb, Vp, ldv, tau, UT, transT ? 1 : 0);
-  count_launch();
+// Scratch of wy_prepare_all: chunk partials and the T factors.
+static size_t wy_scratch_floats(int rows_total, int nref) {
+  const int nblk = ceil_div(std::max(nref, 1), kWY);
+  const int nchunk = ceil_div(std::max(rows_total, 1), kChunkRows);
+  return (size_t)nblk * nchunk * kWY * kWY + (size_t)nblk * kWY * kWY + 64;
+}
+
+static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const float* Uc, int ldu, const float* tau,
+                          float* UT, bool transT, float* scratch) {
+  const int nblk = ceil_div(nref, kWY);
+  const int nchunk = ceil_div(rows_total, kChunkRows);
+  float* Gp = scratch;
+  float* T = scratch + (size_t)nblk * nchunk * kWY * kWY;
+  wy_gram_kernel<<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, Gp, nchunk);
+  wy_tfactor_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, tau, Gp, nchunk, T, transT ? 1 : 0);
+  wy_ut_kernel<<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT);
+  count_launch(3);
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
+}
+
+// One block of at most kWY reflectors (columns of Vp, unit lower
+// trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kWY columns.
+size_t wy_block_scratch_floats(int rows) { return wy_scratch_floats(rows, kWY); }
+
+int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
+                     bool transT, float* scratch) {
+  if (nb > kWY || rows <= 0) return DDCSVD_ERR_ARG;
+  return wy_prepare_all(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
 }
 
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
@@ -236,6 +289,7 @@ static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int n
   float* Uc = a.take<float>((size_t)ldu * std::max(nref, 1));
   float* UT = a.take<float>((size_t)ut_offset(nblk, rows_total) + 64);
   float* W1s = a.take<float>((size_t)kWY * ncols + 64);
+  float* wys = a.take<float>(wy_scratch_floats(rows_total, nref));
   const size_t sbytes = gemm_scratch_bytes(kind, ncols, kWY, rows_total);
   char* sc = a.take<char>(sbytes);
   if (plan_only || nref <= 0) return DDCSVD_OK;
@@ -245,8 +299,8 @@ static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int n
   scratch.cap = sbytes;
   build_reflectors_kernel<<<dim3(ceil_div(ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
       side, rows_total, nref, W, ldw, tau, Uc, ldu);
-  wy_prepare_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, tau, UT, 0);
-  count_launch(2);
+  count_launch();
+  DDC_TRY(wy_prepare_all(ctx, rows_total, nref, Uc, ldu, tau, UT, false, wys));
   DDC_CUDA_TRY(cudaGetLastError());
   for (int bi = nblk - 1; bi >= 0; bi--) {
     const int j0 = bi * kWY;

@@ -1022,6 +1022,7 @@ void plan_qr(Arena& a, int m, int n, int P, GemmKind kind, QrWork* w) {
   w->W1s = a.take<float>((size_t)n * kWY + 64);
   w->part = a.take<float>((size_t)2 * P * kPS + 64);
   w->rowi = a.take<float>(2 * (kPanel + 4));
+  w->wys = a.take<float>(wy_block_scratch_floats(m));
   w->bar = a.take<GridBarrier>(4);
   w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kWY, m);
   w->gemm_scratch = a.take<char>(w->gemm_scratch_bytes);
@@ -1049,7 +1050,7 @@ int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau,
       // W[k0:, k0+nb:] := (I - V T^T V^T) W[k0:, k0+nb:] on tensor cores
       const int rows = m - k0, ncols = n - k0 - nb;
       ktimer_begin(ctx, KC_QR);
-      DDC_TRY(wy_prepare_block(ctx, rows, nb, w.Vp, w.ldv, tau + k0, w.UT, true));
+      DDC_TRY(wy_prepare_block(ctx, rows, nb, w.Vp, w.ldv, tau + k0, w.UT, true, w.wys));
       DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, nb, rows, W + (size_t)(k0 + nb) * ldw, ldw, k0, w.Vp, w.ldv, 0,
                                w.W1s, kWY, 1.f, 0.f, &sc));
       DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kWY, 0, w.W1s, kWY, 0,

@@ -36,7 +36,7 @@ struct ddcsvd_context {
   // launch-configuration knobs (ddcsvd_set_tuning / ddcsvd_autotune_*); none
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
-  int tune[8] = {16, 0, 512, 1, 8, 0, 0, 0};
+  int tune[8] = {16, 0, 512, 1, 8, 2, 0, 0};
   // set while an SVD of the R factor runs inside the tall-matrix path
   bool nested = false;
   std::mutex mu;
@@ -49,7 +49,8 @@ enum TuneKnob {
   TK_BATCH_THREADS = 2,  // batched stage-1 CTA size (256 or 512)
   TK_BATCH_SMEM_FULL = 3,// 1: batched stage-1 problems resident up to the opt-in limit, 0: up to 24K entries
   TK_DC_TERMS = 4,       // D&C: secular-sum terms per lane that size the lane groups (2..32)
-  TK_COUNT = 5
+  TK_TALL_QR = 5,        // QR first for m >= 2n: 0 never, 1 always, 2 when the matrix exceeds 64M entries
+  TK_COUNT = 6
 };
 }  // namespace ddcsvd
 
@@ -176,12 +177,13 @@ int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W,
                            bool plain, Arena& a, bool plan_only);
 
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
-                     bool transT);
+                     bool transT, float* scratch);
+size_t wy_block_scratch_floats(int rows);  // scratch of wy_prepare_block
 // Householder QR of the m x n (m >= n) matrix W in place (R on and above the
 // diagonal, reflectors below in LAPACK form, tau separate), tensor-core
 // trailing updates; the input must be range-scaled (max|a| in [2^-40, 2^40]).
 struct QrWork {
-  float *Vp, *UT, *W1s, *part, *rowi;
+  float *Vp, *UT, *W1s, *part, *rowi, *wys;
   GridBarrier* bar;
   char* gemm_scratch;
   size_t gemm_scratch_bytes;

@@ -2,7 +2,7 @@
 //
 // The handle carries a small vector of launch knobs (TuneKnob: split-K cap
 // and tile width of the GEMMs, CTA size and shared-memory residency of the
-// batched stage 1, lane-group sizing of the D&C).  None of them changes the
+// batched stage 1, lane-group sizing of the D&C, QR first for tall matrices).  None of them changes the
 // arithmetic beyond the summation order of split-K and of the D&C sums, so
 // the tuner only measures time: a coordinate search that, knob by knob, runs
 // the caller's shape (or batch) on seeded synthetic data for each candidate
@@ -109,6 +109,7 @@ extern "C" int ddcsvd_autotune_svd(ddcsvd_handle_t h, int m, int n, int mode, in
   fill_uniform_kernel<<<4 * h->num_sms, 256, 0, h->stream>>>(dA, na, 1234567u);
   count_launch();
   std::vector<Candidates> space = {{TK_SPLITK_MAX, {1, 2, 4, 8, 16}}, {TK_TC_BN, {0, 64}}};
+  if (std::max(m, n) >= 2 * std::min(m, n)) space.push_back({TK_TALL_QR, {0, 1}});
   const int rc = coordinate_search(h, space, reps, [&]() {
     return ddcsvd_svd_f32_device(h, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode);
   });

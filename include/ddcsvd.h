@@ -194,8 +194,11 @@ int ddcsvd_svd_backward_f64_noalloc(void *stream, int batch, int m, int n, const
  *   [3] batched stage-1 residency (1 = whole problem in shared memory up to
  *       the SM's opt-in limit, default; 0 = up to 24K entries, two CTAs/SM)
  *   [4] D&C secular-sum terms per lane (2..32, default 8)
- * None changes the results beyond the summation order of split-K and of the
- * D&C sums.  get/set copy up to `count` knobs. */
+ *   [5] QR first for m >= 2n (or n >= 2m) in the tensor-core modes: 0 never,
+ *       1 always, 2 (default) when the matrix has at least 64M entries
+ * Knobs [0]-[4] change the results only through the summation order of
+ * split-K and of the D&C sums; [5] changes the algorithm (equally accurate).
+ * get/set copy up to `count` knobs. */
 int ddcsvd_get_tuning(ddcsvd_handle_t handle, int *values, int count);
 int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);
 
@@ -203,8 +206,8 @@ int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);
  * single-matrix shape / batch of shapes (host arrays m, n), timed with CUDA
  * events on the handle's stream, `reps` timed runs per candidate; the
  * fastest values stay in the handle.  Allocates its own device buffers.
- * The single-matrix tuner covers knobs [0] and [1], the batched tuner
- * [2], [3] and [4]. */
+ * The single-matrix tuner covers knobs [0], [1] and (tall shapes) [5], the
+ * batched tuner [2], [3] and [4]. */
 int ddcsvd_autotune_svd(ddcsvd_handle_t handle, int m, int n, int mode, int reps);
 int ddcsvd_autotune_batched(ddcsvd_handle_t handle, int batch, const int *m, const int *n, int reps);
 

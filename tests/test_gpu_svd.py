@@ -178,8 +178,11 @@ def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
         A = (rng.uniform(-1, 1, (m, 40)) @ rng.uniform(-1, 1, (40, n))).astype(np.float32)
     else:
         A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
-    s, U, V = run(lib, cuda, A, "tf32x6")
-    check_metrics(orc, A, s, U, V)
+    h = lib.Handle()
+    h.tuning = {"tall_qr": 1}  # these shapes are below the automatic size threshold
+    s, U, V = lib.svd_device(cuda.from_numpy(A).cuda(), mode="tf32x6", handle=h)
+    cuda.cuda.synchronize()
+    check_metrics(orc, A, s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy())
 
 
 def _form_factors_numpy(A_mod, left):
