@@ -419,8 +419,12 @@ __device__ __forceinline__ bool sec_step(bool last, T f, T psi, T dpsi, T phi, T
 // FP64 from that point inside the FP64 bracket, typically for 1-3 steps, to
 // full accuracy.  A poor FP32 start (clustered poles, range trouble) only
 // costs more FP64 steps: the FP64 phase keeps its own bisection safeguard.
+#ifdef DDCSVD_PHASE_TRACE
+__device__ unsigned g_dc_iters[64 * 84];  // [depth][FP64 iterations 0..80, 81: FP32 phase gave up early]
+#endif
+
 __device__ bool sec_root(int q, const double* d, const double* z, const float* df, const float* zf, double zz,
-                         int i, const LaneGroup& g, int* origin, double* tau_out) {
+                         int i, const LaneGroup& g, int* origin, double* tau_out, int* iters = nullptr) {
   double f, psi, dpsi, phi, dphi;
   const bool last = (i == q - 1);
   int o;
@@ -460,7 +464,8 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
   // evaluation: the rational model converges at least quadratically, so the
   // remaining error is far below FP64 resolution.
   bool conv = false;
-  for (int it = 0; it < kSecMaxIt; it++) {
+  int it = 0;
+  for (; it < kSecMaxIt; it++) {
     sec_eval(q, d, z, dorg, tau, split, g, f, psi, dpsi, phi, dphi);
     const double prev = tau;
     if (sec_step<double>(last, f, psi, dpsi, phi, dphi, da0, db0, DBL_EPSILON, lo, hi, tau)) {
@@ -472,6 +477,7 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
       break;
     }
   }
+  if (iters) *iters = it;
   *origin = o;
   *tau_out = tau;
   return conv;
@@ -594,7 +600,13 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       if (i >= q) continue;
       int o;
       double tau;
-      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau);
+      int its = 0;
+      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau, &its);
+#ifdef DDCSVD_PHASE_TRACE
+      if (g.lg == 0 && d < 64) atomicAdd(&g_dc_iters[d * 84 + min(its, 80)], 1u);
+#else
+      (void)its;
+#endif
       if (g.lg == 0) {
         p.org[pos] = o;
         p.tau[pos] = tau;
@@ -831,5 +843,8 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
 #ifdef DDCSVD_PHASE_TRACE
 extern "C" int ddcsvd_dc_trace_read(unsigned long long* out) {
   return (int)cudaMemcpyFromSymbol(out, ddcsvd::g_dc_trace, sizeof(ddcsvd::g_dc_trace));
+}
+extern "C" int ddcsvd_dc_iters_read(unsigned* out) {
+  return (int)cudaMemcpyFromSymbol(out, ddcsvd::g_dc_iters, sizeof(ddcsvd::g_dc_iters));
 }
 #endif

@@ -12,7 +12,7 @@
 //                          h*h' + h*m' + m*h' + m*m' + h*l' + l*h'  below FP32
 // (smallest products are issued first).
 //
-// One CTA computes a 128 x BN tile (BN = 128 or 64), 6 warps:
+// One CTA computes a 128 x BN tile (BN = 128, 64 or 32), 6 warps:
 //   warp 0      TMA producer: raw FP32 K-slabs (32 wide, 128-byte swizzle)
 //               of A and B into a shared-memory ring (3 stages for two
 //               parts, 2 for three);
@@ -510,11 +510,16 @@ static int tc_dispatch(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K, 
   if (M <= 0 || N <= 0) return DDCSVD_OK;
   if ((a_koff & 3) || (b_koff & 3)) return DDCSVD_ERR_ARG;
   const bool bn64 = (N <= 64) || ctx->tune[TK_TC_BN] == 64;
+  const bool bn32 = (N <= 32);  // e.g. the W1 products of the 32-column QR panels
   if (kind == GEMM_TF32X6) {
+    if (bn32)
+      return tc::launch<32, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
     if (bn64)
       return tc::launch<64, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
     return tc::launch<128, 3>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   }
+  if (bn32)
+    return tc::launch<32, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   if (bn64)
     return tc::launch<64, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);
   return tc::launch<128, 2>(ctx, M, N, K, A, lda, a_koff, B, ldb, b_koff, C, ldc, alpha, beta, scratch, trans);

@@ -96,6 +96,17 @@ def main() -> None:
         tot += seg
         print(f"  {d:2d}   " + " ".join(f"{v:7.1f}" for v in seg) + f" {seg.sum():8.1f}")
     print("  sum  " + " ".join(f"{v:7.1f}" for v in tot) + f" {tot.sum():8.1f}")
+    hist = (ctypes.c_uint * (64 * 84))()
+    lib.ddcsvd_dc_iters_read(hist)
+    H = np.array(hist, dtype=np.int64).reshape(64, 84)
+    print("FP64 iterations per secular root (counts over both runs), by depth: mean, max, roots > 10")
+    for d in range(63, -1, -1):
+        row = H[d, :81]
+        if row.sum() == 0:
+            continue
+        its = np.arange(81)
+        print(f"  {d:2d}  mean {float((row * its).sum() / row.sum()):5.2f}  max {int(its[row > 0].max()):3d}  "
+              f">10: {int(row[11:].sum())} of {int(row.sum())}")
     if args.batched:
         return
     buf = (ctypes.c_ulonglong * (128 * 16))()

@@ -36,3 +36,16 @@ def test_gemm_update_form(lib, cuda):
     for mode in ("blocked", "tf32x6"):
         C = lib.gemm_nt_device(A, B, mode=mode, C=C0.clone(), alpha=-1.0, beta=0.5)
         assert float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref)) <= 2e-5
+
+
+@pytest.mark.parametrize("mode", ["tf32x6", "tf32x3"])
+def test_gemm_narrow_output(lib, cuda, mode):
+    """N <= 32 (32-wide tensor-core tiles), long K (split-K partials)."""
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(3)
+    M, N, K = 520, 24, 1536
+    A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
+    B = torch.rand((N, K), device="cuda", generator=g) * 2 - 1
+    ref = A.double() @ B.double().T
+    C = lib.gemm_nt_device(A, B, mode=mode)
+    assert float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref)) <= 5e-6
