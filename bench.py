@@ -157,7 +157,7 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
     bounded sample of the 4096^2 workload, extrapolated to the full SVD."""
     from oracle import oracle
     oracle.build(with_ref=False)
-    threads = os.cpu_count() or 1
+    threads = 1  # the port is scalar, like the reference's bidiag_seq (>99% of the time)
     m, n = A64_host.shape
     # (1) bidiagonalisation: the first k Householder steps of the 4096^2 matrix
     A = np.asfortranarray(A64_host.copy())
