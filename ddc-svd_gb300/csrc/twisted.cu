@@ -92,29 +92,61 @@ __global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
   auto at = [&](int i) { return base + (long long)(i - lo) * nb; };
   const double lam = act ? p.sigma[k] * p.sigma[k] : 0.0;
   const double tiny = DBL_MIN / DBL_EPSILON;
+  // The recurrences below are serial in their FP64 values but not in their
+  // loads: every loop fetches its next kB inputs before the dependent chain
+  // (one loop iteration per step waited a full memory round trip per step).
+  constexpr int kB = 8;
   if (w == 0) {
     // stationary qd on the block: L D L^T - lam = L+ D+ L+^T, s_lo = -lam
     double s = -lam;
-    for (int i = lo; i < hi - 1; i++) {
-      double dp = p.dd[i] + s;
-      if (fabs(dp) < tiny) dp = -tiny;
-      const double L = p.dl[i] / dp;
-      p.Lp[at(i)] = L;
-      p.S[at(i)] = s;
-      s = L * p.ll[i] * s - lam;
+    for (int i0 = lo; i0 < hi - 1; i0 += kB) {
+      double ddv[kB], dlv[kB], llv[kB];
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = min(i0 + u, hi - 2);
+        ddv[u] = p.dd[i];
+        dlv[u] = p.dl[i];
+        llv[u] = p.ll[i];
+      }
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = i0 + u;
+        if (i < hi - 1) {
+          double dp = ddv[u] + s;
+          if (fabs(dp) < tiny) dp = -tiny;
+          const double L = dlv[u] / dp;
+          p.Lp[at(i)] = L;
+          p.S[at(i)] = s;
+          s = L * llv[u] * s - lam;
+        }
+      }
     }
     if (hi > lo) p.S[at(hi - 1)] = s;
   } else if (w == 1 && hi > lo) {
     // progressive qd on the block: L D L^T - lam = U- D- U-^T, p_{hi-1} = d_{hi-1} - lam
     double pv = p.dd[hi - 1] - lam;
     p.Pp[at(hi - 1)] = pv;
-    for (int i = hi - 2; i >= lo; i--) {
-      double dm = p.dll[i] + pv;
-      if (fabs(dm) < tiny) dm = -tiny;
-      const double tt = p.dd[i] / dm;
-      p.Um[at(i)] = p.ll[i] * tt;
-      pv = pv * tt - lam;
-      p.Pp[at(i)] = pv;
+    for (int i0 = hi - 2; i0 >= lo; i0 -= kB) {
+      double dllv[kB], ddv[kB], llv[kB];
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = max(i0 - u, lo);
+        dllv[u] = p.dll[i];
+        ddv[u] = p.dd[i];
+        llv[u] = p.ll[i];
+      }
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = i0 - u;
+        if (i >= lo) {
+          double dm = dllv[u] + pv;
+          if (fabs(dm) < tiny) dm = -tiny;
+          const double tt = ddv[u] / dm;
+          p.Um[at(i)] = llv[u] * tt;
+          pv = pv * tt - lam;
+          p.Pp[at(i)] = pv;
+        }
+      }
     }
   }
   __syncthreads();
@@ -124,9 +156,22 @@ __global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
     const int a = lo + w * seg, b = min(hi, a + seg);
     double best = INFINITY;
     int bi = -1;
-    for (int i = b - 1; i >= a; i--) {  // downward scan, strict <: keeps the larger index on ties
-      const double g = fabs(p.S[at(i)] + p.Pp[at(i)] + lam);
-      if (g < best) { best = g; bi = i; }
+    for (int i0 = b - 1; i0 >= a; i0 -= kB) {  // downward scan, strict <: keeps the larger index on ties
+      double sv[kB], pvv[kB];
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = max(i0 - u, a);
+        sv[u] = p.S[at(i)];
+        pvv[u] = p.Pp[at(i)];
+      }
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = i0 - u;
+        if (i >= a) {
+          const double g = fabs(sv[u] + pvv[u] + lam);
+          if (g < best) { best = g; bi = i; }
+        }
+      }
     }
     s_val[w][lane] = best;
     s_idx[w][lane] = bi;
@@ -146,18 +191,36 @@ __global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
   if (act && w == 0) {
     double z = 1.0, nrm = 1.0;
     p.Z[at(r)] = 1.0;
-    for (int i = r - 1; i >= lo; i--) {
-      z = -p.Lp[at(i)] * z;
-      p.Z[at(i)] = z;
-      nrm += z * z;
+    for (int i0 = r - 1; i0 >= lo; i0 -= kB) {
+      double lv[kB];
+#pragma unroll
+      for (int u = 0; u < kB; u++) lv[u] = p.Lp[at(max(i0 - u, lo))];
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = i0 - u;
+        if (i >= lo) {
+          z = -lv[u] * z;
+          p.Z[at(i)] = z;
+          nrm += z * z;
+        }
+      }
     }
     s_nrm[0][lane] = nrm;
   } else if (act && w == 1) {
     double z = 1.0, nrm = 0.0;
-    for (int i = r + 1; i < hi; i++) {
-      z = -p.Um[at(i - 1)] * z;
-      p.Z[at(i)] = z;
-      nrm += z * z;
+    for (int i0 = r + 1; i0 < hi; i0 += kB) {
+      double uv[kB];
+#pragma unroll
+      for (int u = 0; u < kB; u++) uv[u] = p.Um[at(min(i0 + u, hi - 1) - 1)];
+#pragma unroll
+      for (int u = 0; u < kB; u++) {
+        const int i = i0 + u;
+        if (i < hi) {
+          z = -uv[u] * z;
+          p.Z[at(i)] = z;
+          nrm += z * z;
+        }
+      }
     }
     s_nrm[1][lane] = nrm;
   }
@@ -168,6 +231,7 @@ __global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
     if (act) {
       const int seg = (nb + kTwWarps - 1) / kTwWarps;
       const int a = lo + w * seg, b = min(hi, a + seg);
+#pragma unroll 8
       for (int i = a; i < b; i++) {
         const double zi = p.Z[at(i)];
         const double zn = (i + 1 < hi) ? p.Z[at(i + 1)] : 0.0;
