@@ -193,10 +193,9 @@ __device__ __forceinline__ void reduce_partials(const float* __restrict__ part, 
   constexpr int kR = 12;  // records per warp held in one pass (P <= kR * nw in one pass)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   float a0 = 0.f, a1 = 0.f;
-  FF nacc{0.f, 0.f};
+  FF nacc{0.f, 0.f};  // lane u < kR accumulates the norm pairs of the warp's u-th records
   for (int b0 = w; b0 < P; b0 += kR * nw) {
     float v0[kR], v1[kR];
-    float2 nv[kR];
 #pragma unroll
     for (int u = 0; u < kR; u++) {
       const int b = b0 + u * nw;
@@ -204,15 +203,18 @@ __device__ __forceinline__ void reduce_partials(const float* __restrict__ part, 
       const bool in = b < P;
       v0[u] = (in && lane < cnt) ? __ldcg(rec + lane) : 0.f;
       v1[u] = (in && lane + 32 < cnt) ? __ldcg(rec + 32 + lane) : 0.f;
-      nv[u] = (in && lane == 0) ? __ldcg(reinterpret_cast<const float2*>(rec + kPS - 2)) : make_float2(0.f, 0.f);
     }
+    const int bn = b0 + lane * nw;
+    const float2 nv = (lane < kR && bn < P) ? __ldcg(reinterpret_cast<const float2*>(part + (size_t)bn * kPS + kPS - 2))
+                                            : make_float2(0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < kR; u++) {
       a0 += v0[u];
       a1 += v1[u];
-      nacc = ff_add(nacc, FF{nv[u].x, nv[u].y});
     }
+    nacc = ff_add(nacc, FF{nv.x, nv.y});
   }
+  nacc = warp_sum_ff(nacc);
   static_assert(2 * kPanel <= 64, "record entries beyond 64 are not reduced");
   float* rw = red + w * (kPS + 4);
   rw[lane] = a0;
@@ -224,13 +226,24 @@ __device__ __forceinline__ void reduce_partials(const float* __restrict__ part, 
   __syncthreads();
   const int t = threadIdx.x;
   if (t < cnt && t < 64) {
-    float sum = 0.f;
-    for (int k = 0; k < nw; k++) sum += red[k * (kPS + 4) + t];
-    tot[t] = sum;
-  } else if (t == 64) {
-    FF sum{0.f, 0.f};
-    for (int k = 0; k < nw; k++) sum = ff_add(sum, FF{red[k * (kPS + 4) + kPS], red[k * (kPS + 4) + kPS + 1]});
-    *ntot = sum;
+    // four independent chains over the warps, added in a fixed order
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = 0;
+    for (; k + 3 < nw; k += 4) {
+      s0 += red[k * (kPS + 4) + t];
+      s1 += red[(k + 1) * (kPS + 4) + t];
+      s2 += red[(k + 2) * (kPS + 4) + t];
+      s3 += red[(k + 3) * (kPS + 4) + t];
+    }
+    for (; k < nw; k++) s0 += red[k * (kPS + 4) + t];
+    tot[t] = (s0 + s1) + (s2 + s3);
+  } else if (t >= 64 && t < 96) {
+    // the warp partials of the norm through one shuffle tree
+    const int l = t - 64;
+    FF v{0.f, 0.f};
+    if (l < nw) v = FF{red[l * (kPS + 4) + kPS], red[l * (kPS + 4) + kPS + 1]};
+    v = warp_sum_ff(v);
+    if (l == 0) *ntot = v;
   }
   __syncthreads();
 }
