@@ -188,8 +188,17 @@ __device__ __forceinline__ void block_rows_gemv(const float* __restrict__ W, int
 // grew with cnt to ~9 us).  All loads of a warp are issued before the first
 // add; the nw warp sums are then added in warp order, so the result does not
 // depend on timing.  `red` holds nw * (kPS + 4) floats.
+struct NoHook {
+  __device__ void operator()() const {}
+};
+
+// `hook` runs in every thread after the thread's record loads have been
+// consumed and before the first barrier: callers use it to store values they
+// loaded into registers before the call, so that all loads of a phase share
+// one round trip and the stores are visible after the reduction.
+template <typename Hook = NoHook>
 __device__ __forceinline__ void reduce_partials(const float* __restrict__ part, int P, int cnt, float* red,
-                                                float* tot, FF* ntot) {
+                                                float* tot, FF* ntot, Hook hook = Hook()) {
   constexpr int kR = 12;  // records per warp held in one pass (P <= kR * nw in one pass)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   float a0 = 0.f, a1 = 0.f;
@@ -223,6 +232,7 @@ __device__ __forceinline__ void reduce_partials(const float* __restrict__ part, 
     rw[kPS] = nacc.hi;
     rw[kPS + 1] = nacc.lo;
   }
+  hook();
   __syncthreads();
   const int t = threadIdx.x;
   if (t < cnt && t < 64) {
@@ -390,20 +400,46 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     PMARK(2);
 
     // ---------------- S2: column reflector
-    if (t < j) {
-      S.Wi[t] = __ldcg(W + i + (size_t)(k0 + t) * ldw);
-      S.Xi[t] = __ldcg(X + i + (size_t)t * ldw);
-    }
-    if (t == 64) S.misc[0] = __ldcg(p.xcol + i);
-    // S3's inputs do not depend on the reflector: stage the unscaled column and
-    // row i of the own columns in the same round trip as the partial records
+    // Every load of the phase (row i of the panel's W and X, x0, S3's inputs:
+    // the unscaled column and row i of the own columns -- they do not depend
+    // on the reflector -- and the partial records) is issued into registers
+    // before any of them is used, so the phase costs one round trip; the
+    // reduction's hook stores them to shared memory.
     const int c_s = max(ca, i + 1);
     const int ncol = max(0, cb - c_s);
-    if (i < n - 1) {
-      stage_vec(S.big, p.xcol, i + 1, m);
-      for (int cl = t; cl < ncol; cl += blockDim.x) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
+    {
+      float wi = 0.f, xi = 0.f, x0v = 0.f, pw = 0.f;
+      if (t < j) {
+        wi = __ldcg(W + i + (size_t)(k0 + t) * ldw);
+        xi = __ldcg(X + i + (size_t)t * ldw);
+      }
+      if (t == 64) x0v = __ldcg(p.xcol + i);
+      const bool stage = i < n - 1;
+      const int sa = (i + 1) & ~3, snv = stage ? (m - sa + 3) >> 2 : 0;
+      const float4* src4 = reinterpret_cast<const float4*>(p.xcol + sa);
+      float4* dst4 = reinterpret_cast<float4*>(S.big + sa);
+      const int nt = blockDim.x;
+      float4 sv0 = make_float4(0.f, 0.f, 0.f, 0.f), sv1 = sv0;
+      if (t < snv) sv0 = __ldcg(src4 + t);
+      if (t + nt < snv) sv1 = __ldcg(src4 + t + nt);
+      if (stage && t < ncol) pw = __ldcg(W + i + (size_t)(c_s + t) * ldw);
+      reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm, [&]() {
+        if (t < j) {
+          S.Wi[t] = wi;
+          S.Xi[t] = xi;
+        }
+        if (t == 64) S.misc[0] = x0v;
+        if (t < snv) dst4[t] = sv0;
+        if (t + nt < snv) dst4[t + nt] = sv1;
+        if (stage && t < ncol) S.pre[t] = pw;
+      });
+      if (snv > 2 * nt || (stage && ncol > nt)) {  // very tall or wide panels: the rest in extra rounds
+        for (int q = t + 2 * nt; q < snv; q += nt) dst4[q] = __ldcg(src4 + q);
+        if (stage)
+          for (int cl = t + nt; cl < ncol; cl += nt) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
+        __syncthreads();
+      }
     }
-    reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm);
     // every thread forms the reflector from the same shared inputs (no broadcast round)
     float tq, sq;
     {
@@ -488,18 +524,38 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     PMARK(7);
 
     // ---------------- S5: row reflector
-    if (t == 64) S.misc[1] = __ldcg(p.xrow + i + 1);
-    // row i+1 of Y and VT: needed below and, unscaled, by the next step's S1
-    if (t >= 96 && t < 96 + j + 1) S.Yi[t - 96] = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
-    if (t >= 160 && t < 160 + j) S.VTi[t - 160] = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
-    // S6's inputs do not depend on the reflector: stage the unscaled row and the
-    // original column i+1 of the own rows in the same round trip as the records
-    if (i + 2 < n) stage_vec(S.big, p.xrow, i + 2, n);
+    // One round trip, as in S2: x0 of the row, row i+1 of Y and VT (needed
+    // below and, unscaled, by the next step's S1), S6's inputs (the unscaled
+    // row and the original column i+1 of the own rows) and the records.
     {
+      const int nt = blockDim.x;
+      float x1v = 0.f, yiv = 0.f, vtv = 0.f, pc = 0.f;
+      if (t == 64) x1v = __ldcg(p.xrow + i + 1);
+      if (t >= 96 && t < 96 + j + 1) yiv = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
+      if (t >= 160 && t < 160 + j) vtv = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
+      const bool stage = i + 2 < n;
+      const int sa = (i + 2) & ~3, snv = stage ? (n - sa + 3) >> 2 : 0;
+      const float4* src4 = reinterpret_cast<const float4*>(p.xrow + sa);
+      float4* dst4 = reinterpret_cast<float4*>(S.big + sa);
+      float4 sv0 = make_float4(0.f, 0.f, 0.f, 0.f), sv1 = sv0;
+      if (t < snv) sv0 = __ldcg(src4 + t);
+      if (t + nt < snv) sv1 = __ldcg(src4 + t + nt);
       const int r_lo = max(ra, i + 1);
-      for (int r = r_lo + t; r < rb; r += blockDim.x) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
+      if (r_lo + t < rb) pc = __ldcg(W + r_lo + t + (size_t)(i + 1) * ldw);
+      reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm, [&]() {
+        if (t == 64) S.misc[1] = x1v;
+        if (t >= 96 && t < 96 + j + 1) S.Yi[t - 96] = yiv;
+        if (t >= 160 && t < 160 + j) S.VTi[t - 160] = vtv;
+        if (t < snv) dst4[t] = sv0;
+        if (t + nt < snv) dst4[t + nt] = sv1;
+        if (r_lo + t < rb) S.pre[r_lo + t - ra] = pc;
+      });
+      if (snv > 2 * nt || rb - r_lo > nt) {  // very wide or tall panels: the rest in extra rounds
+        for (int q = t + 2 * nt; q < snv; q += nt) dst4[q] = __ldcg(src4 + q);
+        for (int r = r_lo + t + nt; r < rb; r += nt) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
+        __syncthreads();
+      }
     }
-    reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm);
     float tp, sp;
     {
       float beta;
