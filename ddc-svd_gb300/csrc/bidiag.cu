@@ -20,7 +20,14 @@
 //    u scaling, x = A v, X), columns for row-shaped work (y = A^T u, Y, row
 //    update, v scaling).  Because the GEMVs are fed with the *unscaled*
 //    column/row (kept in xcol / xrow) and the reflector scale is applied
-//    algebraically, each column costs exactly two grid barriers.
+//    algebraically, each column costs exactly two grid barriers.  With up to
+//    8192 rows the two GEMVs share one read of the trailing block: a CTA's
+//    column dots are complete inside the CTA, so it knows the unscaled new
+//    row values w of its columns within the pass and accumulates
+//    sum_c A[r, c] w[c] for every row as it goes (one m-vector per CTA); the
+//    row owners add the P vectors after the second barrier (the "fused"
+//    pass -- the BLAS-2.5 idea of Howell et al., "Cache efficient
+//    bidiagonalization using BLAS 2.5 operators", ACM TOMS 34(3), 2008).
 //
 //  * bidiag_plain_kernel (PLAIN_FP32): the reference's unblocked algorithm --
 //    rank-1 update of the trailing block after every reflector
@@ -65,6 +72,11 @@ struct PanelParams {
   // tensor-core trailing update: the panel's [Up X] rows (>= k0 + nb) and
   // [Y VT] rows written K-major (2 * kPanel floats per row) at the end, or null
   float *Apk, *Bpk;
+  // fused pass: float4 rows per thread (1, 2 or 4; 0 = two separate GEMVs)
+  // and the per-CTA partial products x = A w ([P][ldxp], absolute row index)
+  int rpt4;
+  float* xpart;
+  int ldxp;
 };
 
 __device__ __forceinline__ float sgn_ref(float x) { return x < 0.f ? -1.f : 1.f; }
@@ -269,8 +281,155 @@ __device__ __forceinline__ void stage_vec(float* dst, const float* __restrict__ 
   for (int q = threadIdx.x; q < nv; q += blockDim.x) d4[q] = __ldcg(s4 + q);
 }
 
-// Shared-memory layout of the panel kernel (floats unless noted).
 constexpr int kLD = kPanel + 1;  // padded row length of the cached panel blocks
+
+// Warp reduce-scatter of B per-lane values (B a power of two, at most 32):
+// lane l returns the warp sum of v[l / (32 / B)].  Partners add in the order
+// (own + received), which gives the same sum on both sides, so all 32 / B
+// lanes of a group return the same value.  B - 1 + log2(32 / B) shuffles,
+// against 5 B for B separate warp sums.
+template <int B>
+__device__ __forceinline__ float warp_reduce_scatter(float (&v)[B], int lane) {
+#pragma unroll
+  for (int nv = B, off = 16; nv > 1; nv >>= 1, off >>= 1) {
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for (int h = 0; h < nv / 2; h++) {
+      const float send = up ? v[h] : v[h + nv / 2];
+      const float keep = up ? v[h + nv / 2] : v[h];
+      v[h] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  float s = v[0];
+#pragma unroll
+  for (int off = 16 / B; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return s;
+}
+
+// Columns per batch of the fused pass for RPT4 float4 rows per thread (two
+// batches of B * RPT4 float4s in registers).  Measured on the 4096^2 and
+// 8192^2 factorisations: B * RPT4 = 4 at up to 4096 rows, B = 2 at up to 8192
+// (the longer HBM latency of a matrix beyond L2 wants the deeper buffer).
+__host__ __device__ constexpr int fused_cols(int rpt4) { return rpt4 <= 1 ? 4 : 2; }
+
+// Fused column pass of S3.  Rows [sa, sa + 4 nq) are split over the threads
+// in float4s (q = t + k * blockDim, k < RPT4: coalesced 512-byte lines per
+// warp); the own columns [c_s, c_s + ncol) are taken B at a time, the next
+// batch's loads issued into the second register buffer before the current
+// batch is used.  Per batch: dots with the unscaled column xsb (zero outside
+// rows [i+1, m)), a warp reduce-scatter and one block barrier, the new row
+// value w of each column (Y column j, xrow, owncol as in the two-GEMV form),
+// and acc[r] += W[r, c] w[c] for c >= i + 2 (column i + 1 enters x through
+// its unit coefficient).  acc ends in xp (this CTA's record, absolute row
+// index).  `prologue` runs after the first loads are issued, before a
+// barrier.
+template <int RPT4, int B, typename Prologue>
+__device__ __forceinline__ void fused_col_pass(const float* __restrict__ W, int ldw, int m, int sa, int nq, int c_s,
+                                               int ncol, int ca, int i, int j, const float* xsb, float* red,
+                                               const float* c1s, const float* c2s, const float* pre, float tq,
+                                               float sq, float* Y, int ldn, float* YS, float* owncol, float* xrow,
+                                               float* xp, Prologue prologue) {
+  constexpr int G = 32 / B;  // lanes per column after the reduce-scatter
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5, nt = blockDim.x;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int ns = (ncol + B - 1) / B;  // batches of this step
+  // rows of the last float4 at or beyond m (padding of a caller's buffer may
+  // hold anything) read as zero
+  const int mt = m - sa - 4 * (nq - 1);  // valid rows of the last float4, 1..4
+  auto msk = [&](float4 v, int k) {
+    if (t + k * nt == nq - 1 && mt < 4) {
+      if (mt < 2) v.y = 0.f;
+      if (mt < 3) v.z = 0.f;
+      v.w = 0.f;
+    }
+    return v;
+  };
+  float4 rA[B][RPT4], rB[B][RPT4];
+  auto load = [&](float4(&dst)[B][RPT4], int s) {
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      const bool cin = s * B + u < ncol;
+      const float4* col = reinterpret_cast<const float4*>(W + (size_t)(cin ? c_s + s * B + u : c_s) * ldw + sa);
+#pragma unroll
+      for (int k = 0; k < RPT4; k++) {
+        const int q = t + k * nt;
+        dst[u][k] = (cin && q < nq) ? __ldcg(col + q) : z4;
+      }
+    }
+  };
+  if (ns > 0) load(rA, 0);
+  float4 xs[RPT4], acc[RPT4];
+#pragma unroll
+  for (int k = 0; k < RPT4; k++) {
+    const int q = t + k * nt;
+    xs[k] = q < nq ? reinterpret_cast<const float4*>(xsb + sa)[q] : z4;
+    acc[k] = z4;
+  }
+  prologue();
+  __syncthreads();
+  auto body = [&](float4(&cur)[B][RPT4], float4(&nxt)[B][RPT4], int s) {
+    if (s + 1 < ns) load(nxt, s + 1);
+    float pd[B];
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      float a = 0.f;
+#pragma unroll
+      for (int k = 0; k < RPT4; k++) {
+        const float4 v = msk(cur[u][k], k);
+        a += v.x * xs[k].x + v.y * xs[k].y + v.z * xs[k].z + v.w * xs[k].w;
+      }
+      pd[u] = a;
+    }
+    const float ws = warp_reduce_scatter<B>(pd, lane);
+    const int u = lane / G, sub = lane % G;
+    float* rp = red + (s & 1) * (B * nw);  // [column][warp]
+    if (sub == 0) rp[u * nw + wid] = ws;
+    __syncthreads();
+    float tot = 0.f;
+    for (int w2 = sub; w2 < nw; w2 += G) tot += rp[u * nw + w2];
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+    const int cl = s * B + u;
+    float wv = 0.f;
+    if (cl < ncol) {
+      const float wic = pre[cl];
+      const float ycj = tq * (wic + sq * tot - c1s[cl]);
+      wv = wic - ycj - c2s[cl];
+      if (wid == 0 && sub == 0) {
+        const int c = c_s + cl;
+        Y[c + (size_t)j * ldn] = ycj;
+        YS[(c - ca) * kLD + j] = ycj;
+        owncol[cl] = wv;
+        xrow[c] = wv;
+      }
+      if (c_s + cl < i + 2) wv = 0.f;
+    }
+#pragma unroll
+    for (int uu = 0; uu < B; uu++) {
+      const float wb = __shfl_sync(0xffffffffu, wv, uu * G);
+#pragma unroll
+      for (int k = 0; k < RPT4; k++) {
+        const float4 v = msk(cur[uu][k], k);
+        acc[k].x += v.x * wb;
+        acc[k].y += v.y * wb;
+        acc[k].z += v.z * wb;
+        acc[k].w += v.w * wb;
+      }
+    }
+  };
+  for (int s = 0; s < ns; s += 2) {
+    body(rA, rB, s);
+    if (s + 1 < ns) body(rB, rA, s + 1);
+  }
+  float4* xp4 = reinterpret_cast<float4*>(xp + sa);
+#pragma unroll
+  for (int k = 0; k < RPT4; k++) {
+    const int q = t + k * nt;
+    if (q < nq) xp4[q] = acc[k];
+  }
+}
+
+// Shared-memory layout of the panel kernel (floats unless noted).
 struct PanelSmem {
   float* big;     // max(m, n) + 4: xcol / xrow by absolute index
   float4* red;    // blockDim
@@ -287,9 +446,10 @@ struct PanelSmem {
   FF* nrm;        // reduced compensated norm
   float* redp;    // (threads / 32) * (kPS + 4): per-warp partial sums
   float* scal;    // 8
+  float* xr;      // fused pass: P * rc, the P partial products of the own rows
 };
 
-__device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
+__device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P, bool fused) {
   PanelSmem s;
   float* p = smem;
   s.big = p;
@@ -323,22 +483,31 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P) {
   s.scal = p;
   p += 8;
   s.redp = p;
+  p += (blockDim.x / 32) * (kPS + 4);
+  p = reinterpret_cast<float*>(round_up(reinterpret_cast<uintptr_t>(p), 16));
+  s.xr = fused ? p : nullptr;
   return s;
 }
 
-size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P) {
+size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P, bool fused) {
   size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
              round_up(cc * 8 + 4, 4) + 2 * (size_t)rc * kLD + 2 * (size_t)cc * kLD +
              round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
-             64 + 8 + (size_t)(threads / 32) * (kPS + 4);
+             64 + 8 + (size_t)(threads / 32) * (kPS + 4) + 4;
+  if (fused) f += (size_t)P * rc;
   return f * sizeof(float) + 64;
 }
 
+// kRpt4 = p.rpt4: 0 the two-GEMV form, 1 / 2 / 4 the one-read form with that
+// many float4 rows per thread.  One instantiation per form, each with its own
+// register allocation.
+template <int kRpt4>
 __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelParams p) {
   extern __shared__ __align__(16) float smem[];
   const int m = p.m, n = p.n, k0 = p.k0, ldw = p.ldw, ldn = p.ldn;
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
-  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc, p.P);
+  constexpr bool fx = kRpt4 > 0;
+  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc, p.P, fx);
   float* W = p.W;
   float *X = p.X, *Y = p.Y, *VT = p.VT;
   // static partitions for this panel
@@ -423,18 +592,30 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       if (t < snv) sv0 = __ldcg(src4 + t);
       if (t + nt < snv) sv1 = __ldcg(src4 + t + nt);
       if (stage && t < ncol) pw = __ldcg(W + i + (size_t)(c_s + t) * ldw);
+      // entries outside rows [i+1, m) of the staged vectors are zeroed (the
+      // fused pass multiplies whole float4s)
+      auto msk = [&](int q, float4 v) {
+        const int e = sa + 4 * q;
+        if (e < i + 1 || e + 4 > m) {
+          if (e < i + 1 || e >= m) v.x = 0.f;
+          if (e + 1 < i + 1 || e + 1 >= m) v.y = 0.f;
+          if (e + 2 < i + 1 || e + 2 >= m) v.z = 0.f;
+          if (e + 3 < i + 1 || e + 3 >= m) v.w = 0.f;
+        }
+        return v;
+      };
       reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm, [&]() {
         if (t < j) {
           S.Wi[t] = wi;
           S.Xi[t] = xi;
         }
         if (t == 64) S.misc[0] = x0v;
-        if (t < snv) dst4[t] = sv0;
-        if (t + nt < snv) dst4[t + nt] = sv1;
+        if (t < snv) dst4[t] = msk(t, sv0);
+        if (t + nt < snv) dst4[t + nt] = msk(t + nt, sv1);
         if (stage && t < ncol) S.pre[t] = pw;
       });
       if (snv > 2 * nt || (stage && ncol > nt)) {  // very tall or wide panels: the rest in extra rounds
-        for (int q = t + 2 * nt; q < snv; q += nt) dst4[q] = __ldcg(src4 + q);
+        for (int q = t + 2 * nt; q < snv; q += nt) dst4[q] = msk(q, __ldcg(src4 + q));
         if (stage)
           for (int cl = t + nt; cl < ncol; cl += nt) S.pre[cl] = __ldcg(W + i + (size_t)(c_s + cl) * ldw);
         __syncthreads();
@@ -463,7 +644,37 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
     if (i == n - 1) break;  // last column: no right reflector
     PMARK(3);
     // ---------------- S3: y = A^T u on own columns, Y column j, row-i update
-    {
+    if constexpr (fx) {
+      // one pass over the own columns: y, w and the partial x = A w
+      PMARK(4);
+      float* c1s = S.ypart;
+      float* c2s = S.ypart + p.cc;
+      auto corr = [&]() {  // Y / VT corrections of y and of the row update, warp per column
+        for (int cl = wid; cl < ncol; cl += nw) {
+          const int lc = c_s + cl - ca;
+          float a1 = 0.f, a2 = 0.f;
+          if (lane < j) {
+            const float yl = S.YS[lc * kLD + lane], vl = S.VTS[lc * kLD + lane];
+            const float wl = S.Wi[lane], xl = S.Xi[lane];
+            a1 = yl * (wl + sq * S.tot[1 + lane]) + vl * (xl + sq * S.tot[1 + j + lane]);
+            a2 = yl * wl + vl * xl;
+          }
+          a1 = warp_sum(a1);
+          a2 = warp_sum(a2);
+          if (lane == 0) {
+            c1s[cl] = a1;
+            c2s[cl] = a2;
+          }
+        }
+      };
+      const int sa = (i + 1) & ~3, nq = (m - sa + 3) >> 2;
+      float* xp = p.xpart + (size_t)b * p.ldxp;
+      float* red = reinterpret_cast<float*>(S.red);
+      constexpr int kR = fx ? kRpt4 : 1;
+      fused_col_pass<kR, fused_cols(kR)>(W, ldw, m, sa, nq, c_s, ncol, ca, i, j, S.big, red, c1s, c2s, S.pre, tq, sq,
+                                         Y, ldn, S.YS, S.owncol, p.xrow, xp, corr);
+      PMARK(5);
+    } else {
       PMARK(4);
       if (ncol > 0) {
         int segs = min(8, max(1, nw / ncol));
@@ -500,6 +711,8 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
           }
         }
       }
+    }
+    {
       __syncthreads();
       // partials over own columns c > i+1: [1..j+1] Y^T w, [j+2..2j+1] VT^T w,
       // and ||w||^2 as a compensated pair at [kPS-2, kPS-1]
@@ -533,7 +746,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       if (t == 64) x1v = __ldcg(p.xrow + i + 1);
       if (t >= 96 && t < 96 + j + 1) yiv = __ldcg(Y + i + 1 + (size_t)(t - 96) * ldn);
       if (t >= 160 && t < 160 + j) vtv = __ldcg(VT + i + 1 + (size_t)(t - 160) * ldn);
-      const bool stage = i + 2 < n;
+      const bool stage = !fx && i + 2 < n;  // the two-GEMV form stages the unscaled row for S6
       const int sa = (i + 2) & ~3, snv = stage ? (n - sa + 3) >> 2 : 0;
       const float4* src4 = reinterpret_cast<const float4*>(p.xrow + sa);
       float4* dst4 = reinterpret_cast<float4*>(S.big + sa);
@@ -542,6 +755,21 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       if (t + nt < snv) sv1 = __ldcg(src4 + t + nt);
       const int r_lo = max(ra, i + 1);
       if (r_lo + t < rb) pc = __ldcg(W + r_lo + t + (size_t)(i + 1) * ldw);
+      // fused pass: the P partial products of the own rows (float4 items
+      // (record, q), rows below i + 1 skipped), into S.xr as [P][R4]
+      constexpr int kXR = 5;
+      const int R4 = fx ? max(0, (rb - ra + 3) >> 2) : 0;
+      const int nxi = p.P * R4;
+      float4* xr4 = reinterpret_cast<float4*>(S.xr);
+      const int R4d = max(R4, 1);
+      auto xload = [&](int it) {
+        const int bq = it / R4d, q = it - bq * R4d;
+        return (ra + 4 * q + 3 >= i + 1) ? __ldcg(reinterpret_cast<const float4*>(p.xpart + (size_t)bq * p.ldxp + ra) + q)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      };
+      float4 xv[kXR];
+#pragma unroll
+      for (int u = 0; u < kXR; u++) xv[u] = (t + u * nt < nxi) ? xload(t + u * nt) : make_float4(0.f, 0.f, 0.f, 0.f);
       reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm, [&]() {
         if (t == 64) S.misc[1] = x1v;
         if (t >= 96 && t < 96 + j + 1) S.Yi[t - 96] = yiv;
@@ -549,11 +777,26 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         if (t < snv) dst4[t] = sv0;
         if (t + nt < snv) dst4[t + nt] = sv1;
         if (r_lo + t < rb) S.pre[r_lo + t - ra] = pc;
+#pragma unroll
+        for (int u = 0; u < kXR; u++)
+          if (t + u * nt < nxi) xr4[t + u * nt] = xv[u];
       });
-      if (snv > 2 * nt || rb - r_lo > nt) {  // very wide or tall panels: the rest in extra rounds
+      if (snv > 2 * nt || rb - r_lo > nt || nxi > kXR * nt) {  // very wide or tall panels: the rest in extra rounds
         for (int q = t + 2 * nt; q < snv; q += nt) dst4[q] = __ldcg(src4 + q);
         for (int r = r_lo + t + nt; r < rb; r += nt) S.pre[r - ra] = __ldcg(W + r + (size_t)(i + 1) * ldw);
+        for (int it = t + kXR * nt; it < nxi; it += nt) xr4[it] = xload(it);
         __syncthreads();
+      }
+      if (fx) {
+        // x of the own rows: the P records summed in record order, four
+        // chains per row combined by a symmetric butterfly
+        const int lr = t >> 2, h = t & 3;
+        float sx = 0.f;
+        if (lr < rb - ra)
+          for (int bq = h; bq < p.P; bq += 4) sx += S.xr[bq * 4 * R4 + lr];
+        sx += __shfl_xor_sync(0xffffffffu, sx, 1);
+        sx += __shfl_xor_sync(0xffffffffu, sx, 2);
+        if (lr < rb - ra && h == 0) S.own[lr] = sx;
       }
     }
     float tp, sp;
@@ -593,7 +836,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       const int r_lo = max(ra, i + 1);
       if (rb > r_lo) {
         const int R4 = (rb - ra + 3) >> 2;
-        if (tp != 0.f) block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
+        if (tp != 0.f && !fx) block_rows_gemv(W, ldw, ra, R4, i + 2, n, S.big, S.red, S.own);
         PMARK(10);
         for (int r = r_lo + wid; r < rb; r += nw) {  // warp per row, lanes over l
           const int lr = r - ra;
@@ -967,6 +1210,11 @@ void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWo
   const bool tc = (kind != GEMM_SIMT);
   w->Apk = a.take<float>(tc ? (size_t)m * 2 * kPanel + 64 : 16);
   w->Bpk = a.take<float>(tc ? (size_t)n * 2 * kPanel + 64 : 16);
+  // partial products of the fused pass, when some panel has at most
+  // kFusedRows rows from its first staged float4 down
+  const int k0_last = ((n - 1) / kPanel) * kPanel;
+  w->ldxp = ldw;
+  w->xpart = (m - k0_last <= kFusedRows) ? a.take<float>((size_t)P * ldw + 4) : nullptr;
 }
 
 static int launch_coop(const void* fn, int P, int threads, size_t smem, void* args,
@@ -1008,10 +1256,26 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
     const bool fused_pack = (kind != GEMM_SIMT) && nb == kPanel && k0 + nb < n;
     pp.Apk = fused_pack ? w.Apk : nullptr;
     pp.Bpk = fused_pack ? w.Bpk : nullptr;
+    // one read of the trailing block per column when the rows fit 4 float4s
+    // per thread (and a row owner's P records fit 4 lanes per row)
+    {
+      const int nq0 = (m - ((k0 + 1) & ~3) + 3) >> 2;
+      int rpt4 = ceil_div(nq0, kBidiagThreads);
+      if (rpt4 == 3) rpt4 = 4;
+      const bool fuse = ctx->tune[TK_PANEL_FUSED] != 0 && w.xpart != nullptr && rpt4 <= 4 &&
+                        4 * pp.rc <= kBidiagThreads;
+      pp.rpt4 = fuse ? rpt4 : 0;
+      pp.xpart = w.xpart;
+      pp.ldxp = w.ldxp;
+    }
     DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
-    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads, P);
+    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads, P, pp.rpt4 > 0);
     ktimer_begin(ctx, KC_BIDIAG);
-    DDC_TRY(launch_coop((const void*)bidiag_panel_kernel, P, kBidiagThreads, smem, &pp, ctx->stream));
+    const void* kfn = pp.rpt4 == 1   ? (const void*)bidiag_panel_kernel<1>
+                      : pp.rpt4 == 2 ? (const void*)bidiag_panel_kernel<2>
+                      : pp.rpt4 == 4 ? (const void*)bidiag_panel_kernel<4>
+                                     : (const void*)bidiag_panel_kernel<0>;
+    DDC_TRY(launch_coop(kfn, P, kBidiagThreads, smem, &pp, ctx->stream));
     ktimer_end(ctx);
     const int kn = k0 + nb;
     if (kn < n) {

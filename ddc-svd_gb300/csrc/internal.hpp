@@ -36,7 +36,7 @@ struct ddcsvd_context {
   // launch-configuration knobs (ddcsvd_set_tuning / ddcsvd_autotune_*); none
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
-  int tune[8] = {16, 0, 512, 1, 8, 2, 0, 0};
+  int tune[8] = {16, 0, 512, 1, 8, 2, 1, 0};
   // set while an SVD of the R factor runs inside the tall-matrix path
   bool nested = false;
   std::mutex mu;
@@ -50,7 +50,8 @@ enum TuneKnob {
   TK_BATCH_SMEM_FULL = 3,// 1: batched stage-1 problems resident up to the opt-in limit, 0: up to 24K entries
   TK_DC_TERMS = 4,       // D&C: secular-sum terms per lane that size the lane groups (2..32)
   TK_TALL_QR = 5,        // QR first for m >= 2n: 0 never, 1 always, 2 when the matrix exceeds 64M entries
-  TK_COUNT = 6
+  TK_PANEL_FUSED = 6,    // panel kernel: 1 one read of the trailing block per column (<= 8192 rows), 0 two GEMVs
+  TK_COUNT = 7
 };
 }  // namespace ddcsvd
 
@@ -124,8 +125,11 @@ struct BidiagWork {
   int P;  // CTAs of the cooperative launch
   char* gemm_scratch;
   float *Apk, *Bpk;  // K-major packed trailing-update operands (tensor-core modes)
+  float* xpart;      // fused panel pass: P partial products x = A w (ld ldxp), or null
+  int ldxp;
 };
 constexpr int kPanel = 32;       // bidiagonalisation panel width
+constexpr int kFusedRows = 8192; // fused panel pass: rows (from the first staged float4) it covers
 constexpr int kBidiagThreads = 512;
 void plan_bidiag(Arena& a, int m, int n, int ldw, int P, GemmKind kind, BidiagWork* w);
 int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,

@@ -153,7 +153,8 @@ class Handle:
               "get_kernel_times")
         return [float(x) for x in ms], [int(x) for x in nl]
 
-    TUNING_KNOBS = ("splitk_max", "tc_bn", "batch_threads", "batch_smem_full", "dc_terms", "tall_qr")
+    TUNING_KNOBS = ("splitk_max", "tc_bn", "batch_threads", "batch_smem_full", "dc_terms", "tall_qr",
+                    "panel_fused")
 
     @property
     def tuning(self) -> dict:

@@ -196,8 +196,12 @@ int ddcsvd_svd_backward_f64_noalloc(void *stream, int batch, int m, int n, const
  *   [4] D&C secular-sum terms per lane (2..32, default 8)
  *   [5] QR first for m >= 2n (or n >= 2m) in the tensor-core modes: 0 never,
  *       1 always, 2 (default) when the matrix has at least 64M entries
- * Knobs [0]-[4] change the results only through the summation order of
- * split-K and of the D&C sums; [5] changes the algorithm (equally accurate).
+ *   [6] bidiagonalisation panels with at most 8192 rows: 1 (default) one
+ *       read of the trailing block per column (y = A^T u and x = A v in one
+ *       pass), 0 two separate products
+ * Knobs [0]-[4] and [6] change the results only through the summation order
+ * of split-K, of the D&C sums and of the panel products; [5] changes the
+ * algorithm (equally accurate).
  * get/set copy up to `count` knobs. */
 int ddcsvd_get_tuning(ddcsvd_handle_t handle, int *values, int count);
 int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);

@@ -185,6 +185,47 @@ def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
     check_metrics(orc, A, s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy())
 
 
+@pytest.mark.parametrize("fused", [0, 1])
+@pytest.mark.parametrize("m,n", [(1023, 517), (2050, 2050), (8200, 100)])
+def test_panel_one_pass_and_two_gemv_forms(lib, cuda, orc, fused, m, n):
+    """The panel kernel's one-read form (knob panel_fused = 1, the default up to
+    8192 rows) and its two-GEMV form meet the same bounds.  Row counts that are
+    not multiples of 4 exercise the ragged last float4; with 8200 rows the first
+    panel runs the two-GEMV form and the later ones the one-read form."""
+    mode = "tf32x6" if _mode_available(lib, "tf32x6") else "blocked"
+    rng = np.random.default_rng(m * 13 + n + fused)
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    h = lib.Handle()
+    h.tuning = {"panel_fused": fused, "tall_qr": 0}
+    s, U, V = lib.svd_device(cuda.from_numpy(A).cuda(), mode=mode, handle=h)
+    cuda.cuda.synchronize()
+    check_metrics(orc, A, s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy())
+
+
+@pytest.mark.parametrize("mode", ["blocked", "tf32x6"])
+def test_bidiag_caller_padding_not_used(lib, cuda, mode):
+    """Rows m .. lda-1 of a caller's buffer may hold anything: with NaN there the
+    bidiagonal is bit-identical to the zero-padded run (m = 301, lda = 320)."""
+    if mode == "tf32x6" and not _mode_available(lib, mode):
+        pytest.skip("tf32x6 unavailable")
+    torch = cuda
+    m, n = 301, 150
+    ldw = 320
+    A = torch.from_numpy(np.random.default_rng(5).uniform(-1, 1, (m, n)).astype(np.float32)).cuda()
+    h = lib.Handle()
+    outs = []
+    for fill in (0.0, float("nan")):
+        W = torch.full((n, ldw), fill, dtype=torch.float32, device="cuda")
+        W[:, :m] = A.t()
+        d, e, tq, tp = (torch.zeros(n, dtype=torch.float32, device="cuda") for _ in range(4))
+        lib.check(lib.load().ddcsvd_bidiag_f32_device(h.ptr, m, n, W.data_ptr(), ldw, d.data_ptr(), e.data_ptr(),
+                                                      tq.data_ptr(), tp.data_ptr(), lib._mode(mode)), "bidiag")
+        torch.cuda.synchronize()
+        outs.append((d.cpu().numpy(), e[: n - 1].cpu().numpy()))
+    assert np.all(np.isfinite(outs[1][0])) and np.all(np.isfinite(outs[1][1]))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
 def _form_factors_numpy(A_mod, left):
     """The reference's form_u_par / form_v_par loops (bidiag_par.c:877-988), restated in numpy."""
     m, n = A_mod.shape
