@@ -196,7 +196,7 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
 # --mode tf32x6 --reps 1 --kind uniform` (metrics dram__bytes_read.sum and
 # dram__bytes_write.sum, all 128 launches).  Far below the algorithmic GEMV
 # bytes: the trailing block is re-read from L2, not HBM.
-PANEL_DRAM_BYTES_PER_LAUNCH = 23177000
+PANEL_DRAM_BYTES_PER_LAUNCH = 22818818
 
 
 def bench_tall(torch, lib, h, steps):
