@@ -40,7 +40,7 @@ __global__ void pack_reflectors_kernel(int side, int rows, int bs, int j0, int s
 
 // T (bs x bs, col-major) from the Gram matrix G = U^T U:
 //   T[l,l] = tau_l,  T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l].
-__global__ void wy_tfactor_kernel(int bs, int j0, const float* __restrict__ tau, const float* __restrict__ G,
+__global__ void wy_tfactor_single_kernel(int bs, int j0, const float* __restrict__ tau, const float* __restrict__ G,
                                   float* T) {
   __shared__ float sT[kWY][kWY + 1];
   __shared__ float sG[kWY][kWY + 1];
@@ -97,93 +97,105 @@ __global__ void build_reflectors_kernel(int side, int rows_total, int nref, cons
 }
 
 // Offset (floats) of block b's U_b T_b in the packed UT array: block b covers
-// rows [b kWY, rows_total) and is stored row-major with kWY columns.
+// rows [b NB, rows_total) and is stored row-major with NB columns.
+template <int NB = kWY>
 __host__ __device__ inline long long ut_offset(int b, int rows_total) {
-  return (long long)kWY * ((long long)b * rows_total - (long long)kWY * b * (b - 1) / 2);
+  return (long long)NB * ((long long)b * rows_total - (long long)NB * b * (b - 1) / 2);
 }
 
-// WY preparation of every block b (reflectors j0 = b kWY ... j0 + bs - 1,
+// WY preparation of every block b (reflectors j0 = b NB ... j0 + bs - 1,
 // rows [j0, rows_total) of Uc), in three row-parallel kernels:
 //   wy_gram_kernel     grid (block, row chunk): partial G = U^T U of a chunk
 //   wy_tfactor_kernel  grid (block): G = sum of the chunk partials in chunk
 //                      order, then the compact-WY factor T
 //                      (T[l,l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l])
-//   wy_ut_kernel       grid (block, row chunk): UT = U T (row-major, ld kWY)
+//   wy_ut_kernel       grid (block, row chunk): UT = U T (row-major, ld NB)
 // so that applying the block is C -= UT (U^T C) (or, with T^T, the
 // transposed block of a QR factorisation).  A single CTA per block had cost
-// 1.3 ms for an 8192-row block.
+// 1.3 ms for an 8192-row block.  NB = 64 (QR path) or 128 (back-transformation:
+// half the passes over C of 64-reflector blocks).
 constexpr int kPrepRows = 32;    // rows per shared-memory tile
 constexpr int kChunkRows = 512;  // rows per CTA of the chunked kernels
+constexpr int kWYT = 128;        // reflectors per WY block of the tensor-core back-transformation
 
+template <int NB>
 __device__ __forceinline__ void wy_block_geom(int b, int rows_total, int nref, int& j0, int& bs, int& rows) {
-  j0 = b * kWY;
-  bs = min(kWY, nref - j0);
+  j0 = b * NB;
+  bs = min(NB, nref - j0);
   rows = rows_total - j0;
 }
 
-__device__ __forceinline__ void wy_load_tile(float (*sU)[kWY + 1], const float* U, int ldu, int r0, int rend,
+template <int NB>
+__device__ __forceinline__ void wy_load_tile(float (*sU)[NB + 1], const float* U, int ldu, int r0, int rend,
                                              int bs) {
-  for (int idx = threadIdx.x; idx < kPrepRows * kWY; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < kPrepRows * NB; idx += blockDim.x) {
     const int rr = idx & (kPrepRows - 1), c = idx / kPrepRows;
     const int r = r0 + rr;
     sU[rr][c] = (r < rend && c < bs) ? U[r + (size_t)c * ldu] : 0.f;
   }
 }
 
+// 256 threads as 16 x 16, each an (NB/16) x (NB/16) tile of G.
+template <int NB>
 __global__ void __launch_bounds__(256) wy_gram_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
                                                       float* Gp, int nchunk) {
-  __shared__ float sU[kPrepRows][kWY + 1];
+  constexpr int R = NB / 16;
+  __shared__ float sU[kPrepRows][NB + 1];
   int j0, bs, rows;
-  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
+  wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
   const int c0 = blockIdx.y * kChunkRows;
   if (bs <= 0 || c0 >= rows) return;
   const int c1 = min(rows, c0 + kChunkRows);
   const float* U = Uc + j0 + (size_t)j0 * ldu;
   const int t = threadIdx.x, ti = t & 15, tj = t >> 4;
-  float acc[4][4];
+  float acc[R][R];
 #pragma unroll
-  for (int a = 0; a < 4; a++)
+  for (int a = 0; a < R; a++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) acc[a][c] = 0.f;
+    for (int c = 0; c < R; c++) acc[a][c] = 0.f;
   for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
     __syncthreads();
-    wy_load_tile(sU, U, ldu, r0, c1, bs);
+    wy_load_tile<NB>(sU, U, ldu, r0, c1, bs);
     __syncthreads();
-#pragma unroll 8
+#pragma unroll 4
     for (int k = 0; k < kPrepRows; k++) {
-      float x[4], y[4];
+      float x[R], y[R];
 #pragma unroll
-      for (int a = 0; a < 4; a++) {
-        x[a] = sU[k][4 * ti + a];
-        y[a] = sU[k][4 * tj + a];
+      for (int a = 0; a < R; a++) {
+        x[a] = sU[k][R * ti + a];
+        y[a] = sU[k][R * tj + a];
       }
 #pragma unroll
-      for (int a = 0; a < 4; a++)
+      for (int a = 0; a < R; a++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[a][c] += x[a] * y[c];
+        for (int c = 0; c < R; c++) acc[a][c] += x[a] * y[c];
     }
   }
-  float* G = Gp + ((size_t)blockIdx.x * nchunk + blockIdx.y) * kWY * kWY;
+  float* G = Gp + ((size_t)blockIdx.x * nchunk + blockIdx.y) * NB * NB;
 #pragma unroll
-  for (int a = 0; a < 4; a++)
+  for (int a = 0; a < R; a++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) G[(4 * ti + a) + (size_t)(4 * tj + c) * kWY] = acc[a][c];
+    for (int c = 0; c < R; c++) G[(R * ti + a) + (size_t)(R * tj + c) * NB] = acc[a][c];
 }
 
-__global__ void __launch_bounds__(256) wy_tfactor_kernel(int rows_total, int nref, const float* __restrict__ tau,
-                                                         const float* __restrict__ Gp, int nchunk, float* Tout,
-                                                         int transT) {
-  __shared__ float sG[kWY][kWY + 1];
-  __shared__ float sT[kWY][kWY + 1];
+// 4 * NB threads, four per row of T; sG and sT in dynamic shared memory
+// (2 NB (NB + 1) floats).
+template <int NB>
+__global__ void __launch_bounds__(4 * NB) wy_tfactor_kernel(int rows_total, int nref, const float* __restrict__ tau,
+                                                            const float* __restrict__ Gp, int nchunk, float* Tout,
+                                                            int transT) {
+  extern __shared__ float wsm[];
+  float(*sG)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm);
+  float(*sT)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + NB * (NB + 1));
   int j0, bs, rows;
-  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
+  wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
   if (bs <= 0 || rows <= 0) return;
   const int nc = ceil_div(rows, kChunkRows);
   const int t = threadIdx.x;
-  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) {
-    const int r = idx % kWY, c = idx / kWY;
+  for (int idx = t; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx % NB, c = idx / NB;
     float g = 0.f;
-    for (int s = 0; s < nc; s++) g += Gp[((size_t)blockIdx.x * nchunk + s) * kWY * kWY + idx];
+    for (int s = 0; s < nc; s++) g += Gp[((size_t)blockIdx.x * nchunk + s) * NB * NB + idx];
     sG[r][c] = g;
     sT[r][c] = 0.f;
   }
@@ -202,67 +214,80 @@ __global__ void __launch_bounds__(256) wy_tfactor_kernel(int rows_total, int nre
       __syncthreads();
     }
   }
-  // T (or T^T for a block applied as a transpose) to global, [row + col * kWY]
-  float* T = Tout + (size_t)blockIdx.x * kWY * kWY;
-  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) {
-    const int r = idx % kWY, c = idx / kWY;
+  // T (or T^T for a block applied as a transpose) to global, [row + col * NB]
+  float* T = Tout + (size_t)blockIdx.x * NB * NB;
+  for (int idx = t; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx % NB, c = idx / NB;
     T[idx] = transT ? sT[c][r] : sT[r][c];
   }
 }
 
+// 256 threads: row rr = t / 8 of a 32-row tile, NB / 8 consecutive columns
+// each; sU and sT in dynamic shared memory ((kPrepRows + NB) (NB + 1) floats).
+template <int NB>
 __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
                                                     const float* __restrict__ Tin, float* UT) {
-  __shared__ float sU[kPrepRows][kWY + 1];
-  __shared__ float sT[kWY][kWY + 1];
+  constexpr int CW = NB / 8;
+  extern __shared__ float wsm[];
+  float(*sU)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm);
+  float(*sT)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + kPrepRows * (NB + 1));
   int j0, bs, rows;
-  wy_block_geom(blockIdx.x, rows_total, nref, j0, bs, rows);
+  wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
   const int c0 = blockIdx.y * kChunkRows;
   if (bs <= 0 || c0 >= rows) return;
   const int c1 = min(rows, c0 + kChunkRows);
   const float* U = Uc + j0 + (size_t)j0 * ldu;
-  float* out = UT + ut_offset(blockIdx.x, rows_total);
+  float* out = UT + ut_offset<NB>(blockIdx.x, rows_total);
   const int t = threadIdx.x;
-  const float* T = Tin + (size_t)blockIdx.x * kWY * kWY;
-  for (int idx = t; idx < kWY * kWY; idx += blockDim.x) sT[idx % kWY][idx / kWY] = T[idx];
-  const int rr = t >> 3, cb = (t & 7) * 8;  // thread: row rr of a tile, 8 consecutive columns
+  const float* T = Tin + (size_t)blockIdx.x * NB * NB;
+  for (int idx = t; idx < NB * NB; idx += blockDim.x) sT[idx % NB][idx / NB] = T[idx];
+  const int rr = t >> 3, cb = (t & 7) * CW;
   for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
     __syncthreads();
-    wy_load_tile(sU, U, ldu, r0, c1, bs);
+    wy_load_tile<NB>(sU, U, ldu, r0, c1, bs);
     __syncthreads();
-    float acc[8];
+    float acc[CW];
 #pragma unroll
-    for (int c = 0; c < 8; c++) acc[c] = 0.f;
-#pragma unroll 8
-    for (int k = 0; k < kWY; k++) {
+    for (int c = 0; c < CW; c++) acc[c] = 0.f;
+#pragma unroll 4
+    for (int k = 0; k < NB; k++) {
       const float x = sU[rr][k];
 #pragma unroll
-      for (int c = 0; c < 8; c++) acc[c] += x * sT[k][cb + c];
+      for (int c = 0; c < CW; c++) acc[c] += x * sT[k][cb + c];
     }
     const int r = r0 + rr;
     if (r < c1) {
-      float4* o = reinterpret_cast<float4*>(out + (size_t)r * kWY + cb);
-      o[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-      o[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      float4* o = reinterpret_cast<float4*>(out + (size_t)r * NB + cb);
+#pragma unroll
+      for (int c = 0; c < CW / 4; c++) o[c] = make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
     }
   }
 }
 
 // Scratch of wy_prepare_all: chunk partials and the T factors.
+template <int NB = kWY>
 static size_t wy_scratch_floats(int rows_total, int nref) {
-  const int nblk = ceil_div(std::max(nref, 1), kWY);
+  const int nblk = ceil_div(std::max(nref, 1), NB);
   const int nchunk = ceil_div(std::max(rows_total, 1), kChunkRows);
-  return (size_t)nblk * nchunk * kWY * kWY + (size_t)nblk * kWY * kWY + 64;
+  return (size_t)nblk * nchunk * NB * NB + (size_t)nblk * NB * NB + 64;
 }
 
+template <int NB>
 static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const float* Uc, int ldu, const float* tau,
                           float* UT, bool transT, float* scratch) {
-  const int nblk = ceil_div(nref, kWY);
+  const int nblk = ceil_div(nref, NB);
   const int nchunk = ceil_div(rows_total, kChunkRows);
   float* Gp = scratch;
-  float* T = scratch + (size_t)nblk * nchunk * kWY * kWY;
-  wy_gram_kernel<<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, Gp, nchunk);
-  wy_tfactor_kernel<<<nblk, 256, 0, ctx->stream>>>(rows_total, nref, tau, Gp, nchunk, T, transT ? 1 : 0);
-  wy_ut_kernel<<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT);
+  float* T = scratch + (size_t)nblk * nchunk * NB * NB;
+  const int tf_smem = 2 * NB * (NB + 1) * (int)sizeof(float);
+  const int ut_smem = (kPrepRows + NB) * (NB + 1) * (int)sizeof(float);
+  DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_tfactor_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    tf_smem));
+  DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_ut_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    ut_smem));
+  wy_gram_kernel<NB><<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, Gp, nchunk);
+  wy_tfactor_kernel<NB><<<nblk, 4 * NB, tf_smem, ctx->stream>>>(rows_total, nref, tau, Gp, nchunk, T, transT ? 1 : 0);
+  wy_ut_kernel<NB><<<dim3(nblk, nchunk), 256, ut_smem, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT);
   count_launch(3);
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
@@ -270,12 +295,12 @@ static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const f
 
 // One block of at most kWY reflectors (columns of Vp, unit lower
 // trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kWY columns.
-size_t wy_block_scratch_floats(int rows) { return wy_scratch_floats(rows, kWY); }
+size_t wy_block_scratch_floats(int rows) { return wy_scratch_floats<kWY>(rows, kWY); }
 
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
                      bool transT, float* scratch) {
   if (nb > kWY || rows <= 0) return DDCSVD_ERR_ARG;
-  return wy_prepare_all(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
+  return wy_prepare_all<kWY>(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
 }
 
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
@@ -284,13 +309,14 @@ int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int
 static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw,
                             const float* tau, float* C, int ldc, int ncols, GemmKind kind, Arena& a,
                             bool plan_only) {
+  constexpr int NB = kWYT;
   const int ldu = (int)round_up(rows_total, 32);
-  const int nblk = ceil_div(std::max(nref, 1), kWY);
+  const int nblk = ceil_div(std::max(nref, 1), NB);
   float* Uc = a.take<float>((size_t)ldu * std::max(nref, 1));
-  float* UT = a.take<float>((size_t)ut_offset(nblk, rows_total) + 64);
-  float* W1s = a.take<float>((size_t)kWY * ncols + 64);
-  float* wys = a.take<float>(wy_scratch_floats(rows_total, nref));
-  const size_t sbytes = gemm_scratch_bytes(kind, ncols, kWY, rows_total);
+  float* UT = a.take<float>((size_t)ut_offset<NB>(nblk, rows_total) + 64);
+  float* W1s = a.take<float>((size_t)NB * ncols + 64);
+  float* wys = a.take<float>(wy_scratch_floats<NB>(rows_total, nref));
+  const size_t sbytes = gemm_scratch_bytes(kind, ncols, NB, rows_total);
   char* sc = a.take<char>(sbytes);
   if (plan_only || nref <= 0) return DDCSVD_OK;
   Arena scratch;
@@ -300,18 +326,18 @@ static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int n
   build_reflectors_kernel<<<dim3(ceil_div(ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
       side, rows_total, nref, W, ldw, tau, Uc, ldu);
   count_launch();
-  DDC_TRY(wy_prepare_all(ctx, rows_total, nref, Uc, ldu, tau, UT, false, wys));
+  DDC_TRY(wy_prepare_all<NB>(ctx, rows_total, nref, Uc, ldu, tau, UT, false, wys));
   DDC_CUDA_TRY(cudaGetLastError());
   for (int bi = nblk - 1; bi >= 0; bi--) {
-    const int j0 = bi * kWY;
-    const int bs = std::min(kWY, nref - j0);
+    const int j0 = bi * NB;
+    const int bs = std::min(NB, nref - j0);
     const int rows = rows_total - j0;
     if (rows <= 0 || bs <= 0) continue;
-    // W1^T = C[j0:, :]^T U_b, stored as W1s[j + n * kWY]
-    DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, Uc + (size_t)j0 * ldu, ldu, j0, W1s, kWY, 1.f,
+    // W1^T = C[j0:, :]^T U_b, stored as W1s[j + n * NB]
+    DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, Uc + (size_t)j0 * ldu, ldu, j0, W1s, NB, 1.f,
                              0.f, &scratch));
     // C[j0:, :] -= UT_b W1
-    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, UT + ut_offset(bi, rows_total), kWY, 0, W1s, kWY, 0,
+    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, UT + ut_offset<NB>(bi, rows_total), NB, 0, W1s, NB, 0,
                            C + j0, ldc, -1.f, 1.f, &scratch));
   }
   return DDCSVD_OK;
@@ -352,7 +378,7 @@ static int apply_blocked(ddcsvd_context* ctx, int side, int rows_total, int nref
     Mat UT{Pk, ldp, 1}, U{Pk, 1, ldp};
     // G = U^T U (bs x bs) and the triangular factor T
     DDC_TRY(gemm(ctx, GEMM_SIMT, bs, bs, rows, UT, U, 0, none, none, 1.f, 0.f, G, bs, &scratch));
-    wy_tfactor_kernel<<<1, kWY, 0, ctx->stream>>>(bs, j0, tau, G, T);
+    wy_tfactor_single_kernel<<<1, kWY, 0, ctx->stream>>>(bs, j0, tau, G, T);
     count_launch();
     float* Cb = C + off_al;
     if (!tc) {
