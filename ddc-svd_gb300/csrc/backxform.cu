@@ -222,15 +222,19 @@ __global__ void __launch_bounds__(4 * NB) wy_tfactor_kernel(int rows_total, int 
   }
 }
 
-// 256 threads: row rr = t / 8 of a 32-row tile, NB / 8 consecutive columns
-// each; sU and sT in dynamic shared memory ((kPrepRows + NB) (NB + 1) floats).
+// 256 threads in NB / 4 column groups of 4 columns and 1024 / NB row groups
+// of NB / 32 rows (a 32-row tile): per k one broadcast load of U per row and
+// one 16-byte load of T for 4 NB / 32 FMAs.  sU ([32][NB + 1]) and sT
+// ([NB][NB], T[k][c]) in dynamic shared memory.
 template <int NB>
 __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
                                                     const float* __restrict__ Tin, float* UT) {
-  constexpr int CW = NB / 8;
-  extern __shared__ float wsm[];
+  constexpr int CG = NB / 4;    // column groups
+  constexpr int RPT = NB / 32;  // rows per thread
+  static_assert(256 / CG * RPT == kPrepRows, "row groups must cover the tile");
+  extern __shared__ __align__(16) float wsm[];
   float(*sU)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm);
-  float(*sT)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + kPrepRows * (NB + 1));
+  float(*sT)[NB] = reinterpret_cast<float(*)[NB]>(wsm + kPrepRows * (NB + 1));
   int j0, bs, rows;
   wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
   const int c0 = blockIdx.y * kChunkRows;
@@ -241,25 +245,30 @@ __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, co
   const int t = threadIdx.x;
   const float* T = Tin + (size_t)blockIdx.x * NB * NB;
   for (int idx = t; idx < NB * NB; idx += blockDim.x) sT[idx % NB][idx / NB] = T[idx];
-  const int rr = t >> 3, cb = (t & 7) * CW;
+  const int cg = t % CG, rg = t / CG;
   for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
     __syncthreads();
     wy_load_tile<NB>(sU, U, ldu, r0, c1, bs);
     __syncthreads();
-    float acc[CW];
+    float4 acc[RPT];
 #pragma unroll
-    for (int c = 0; c < CW; c++) acc[c] = 0.f;
+    for (int a = 0; a < RPT; a++) acc[a] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
     for (int k = 0; k < NB; k++) {
-      const float x = sU[rr][k];
+      const float4 y = *reinterpret_cast<const float4*>(&sT[k][4 * cg]);
 #pragma unroll
-      for (int c = 0; c < CW; c++) acc[c] += x * sT[k][cb + c];
+      for (int a = 0; a < RPT; a++) {
+        const float x = sU[rg * RPT + a][k];
+        acc[a].x += x * y.x;
+        acc[a].y += x * y.y;
+        acc[a].z += x * y.z;
+        acc[a].w += x * y.w;
+      }
     }
-    const int r = r0 + rr;
-    if (r < c1) {
-      float4* o = reinterpret_cast<float4*>(out + (size_t)r * NB + cb);
 #pragma unroll
-      for (int c = 0; c < CW / 4; c++) o[c] = make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
+    for (int a = 0; a < RPT; a++) {
+      const int r = r0 + rg * RPT + a;
+      if (r < c1) reinterpret_cast<float4*>(out + (size_t)r * NB)[cg] = acc[a];
     }
   }
 }
@@ -280,7 +289,7 @@ static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const f
   float* Gp = scratch;
   float* T = scratch + (size_t)nblk * nchunk * NB * NB;
   const int tf_smem = 2 * NB * (NB + 1) * (int)sizeof(float);
-  const int ut_smem = (kPrepRows + NB) * (NB + 1) * (int)sizeof(float);
+  const int ut_smem = (kPrepRows * (NB + 1) + NB * NB) * (int)sizeof(float);
   DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_tfactor_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     tf_smem));
   DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_ut_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
