@@ -65,9 +65,9 @@ constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m 
 // max|M| in [2^-40, 2^40]); every thread forms them from the same reduced
 // value, so no broadcast round is needed.
 __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, float* tq, float* tp,
-                           float* vrow, float* red) {
+                           float* vrow, float* red, int iend) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
-  for (int i = 0; i < n; i++) {
+  for (int i = 0; i < iend; i++) {
     // ---- left reflector from column i
     const float x0 = M[i + (size_t)i * ld];
     FF s2{0.f, 0.f};
@@ -194,6 +194,11 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
     const BatchTask T = tasks[order[q]];
     const int m = T.m, n = T.n, ld = m;
     const bool fits = (long long)m * n <= smem_floats;
+    // a problem beyond the shared memory: columns [0, k0) run in global memory
+    // until the trailing block fits (k0 = n: none fits)
+    int k0 = 0;
+    if (!fits)
+      while (k0 < n && (long long)(m - k0) * (n - k0) > smem_floats) k0++;
     float* Wg = W + T.offW;
     float* M = fits ? Ms : Wg;
     // load the (oriented) problem; max|a| for the range scaling of the norms
@@ -215,7 +220,23 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
     if (sc != 1.f)
       for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) M[(idx % m) + (size_t)(idx / m) * ld] *= sc;
     __syncthreads();
-    cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red);
+    if (fits || k0 >= n) {
+      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, n);
+    } else {
+      // the first k0 columns in global memory, then the (m - k0) x (n - k0)
+      // trailing block (the only part later columns touch) in shared memory
+      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, k0);
+      __syncthreads();
+      const int mt = m - k0, nt = n - k0;
+      for (int idx = threadIdx.x; idx < mt * nt; idx += blockDim.x)
+        Ms[idx] = Wg[(k0 + idx % mt) + (size_t)(k0 + idx / mt) * ld];
+      __syncthreads();
+      cta_bidiag(Ms, mt, mt, nt, d + T.offD + k0, e + T.offD + k0, tq + T.offD + k0, tp + T.offD + k0, vrow, red,
+                 nt);
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < mt * nt; idx += blockDim.x)
+        Wg[(k0 + idx % mt) + (size_t)(k0 + idx / mt) * ld] = Ms[idx];
+    }
     __syncthreads();
     if (sc != 1.f) {
       const float inv = 1.f / sc;
