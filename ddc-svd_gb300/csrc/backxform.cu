@@ -302,14 +302,17 @@ static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const f
   return DDCSVD_OK;
 }
 
-// One block of at most kWY reflectors (columns of Vp, unit lower
-// trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kWY columns.
-size_t wy_block_scratch_floats(int rows) { return wy_scratch_floats<kWY>(rows, kWY); }
+// One block of at most kPanel reflectors (a QR panel: columns of Vp, unit
+// lower trapezoidal, rows x nb): UT = Vp T (or Vp T^T), row-major with kPanel
+// columns.  The 32-wide kernels compute only the panel's 32 x 32 Gram matrix
+// and T (the 64-wide ones had cost 34 ms over the 256 panels of a
+// 16384 x 8192 QR).
+size_t wy_block_scratch_floats(int rows) { return wy_scratch_floats<kPanel>(rows, kPanel); }
 
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
                      bool transT, float* scratch) {
-  if (nb > kWY || rows <= 0) return DDCSVD_ERR_ARG;
-  return wy_prepare_all<kWY>(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
+  if (nb > kPanel || rows <= 0) return DDCSVD_ERR_ARG;
+  return wy_prepare_all<kPanel>(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
 }
 
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,

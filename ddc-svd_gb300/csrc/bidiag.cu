@@ -1351,13 +1351,13 @@ void plan_qr(Arena& a, int m, int n, int P, GemmKind kind, QrWork* w) {
   w->ldv = (int)round_up(m, 32);
   w->P = P;
   w->Vp = a.take<float>((size_t)w->ldv * kPanel);
-  w->UT = a.take<float>((size_t)m * kWY + 64);
-  w->W1s = a.take<float>((size_t)n * kWY + 64);
+  w->UT = a.take<float>((size_t)m * kPanel + 64);
+  w->W1s = a.take<float>((size_t)n * kPanel + 64);
   w->part = a.take<float>((size_t)2 * P * kPS + 64);
   w->rowi = a.take<float>(2 * (kPanel + 4));
   w->wys = a.take<float>(wy_block_scratch_floats(m));
   w->bar = a.take<GridBarrier>(4);
-  w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kWY, m);
+  w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kPanel, m);
   w->gemm_scratch = a.take<char>(w->gemm_scratch_bytes);
 }
 
@@ -1385,8 +1385,8 @@ int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau,
       ktimer_begin(ctx, KC_QR);
       DDC_TRY(wy_prepare_block(ctx, rows, nb, w.Vp, w.ldv, tau + k0, w.UT, true, w.wys));
       DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, nb, rows, W + (size_t)(k0 + nb) * ldw, ldw, k0, w.Vp, w.ldv, 0,
-                               w.W1s, kWY, 1.f, 0.f, &sc));
-      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kWY, 0, w.W1s, kWY, 0,
+                               w.W1s, kPanel, 1.f, 0.f, &sc));
+      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kPanel, 0, w.W1s, kPanel, 0,
                              W + k0 + (size_t)(k0 + nb) * ldw, ldw, -1.f, 1.f, &sc));
       ktimer_end(ctx);
     }

@@ -180,6 +180,7 @@ int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W,
                            const float* taup, float* C, int ldc, int ncols, GemmKind kind,
                            bool plain, Arena& a, bool plan_only);
 
+// UT = Vp T (or Vp T^T) of one QR panel (nb <= kPanel reflectors), row-major with kPanel columns.
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
                      bool transT, float* scratch);
 size_t wy_block_scratch_floats(int rows);  // scratch of wy_prepare_block
