@@ -315,6 +315,17 @@ int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int
   return wy_prepare_all<kPanel>(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
 }
 
+// The same for a block of at most kWideWY reflectors (UT row-major with
+// kWideWY columns): the far trailing update of a 128-column QR super-block.
+size_t wy_wide_scratch_floats(int rows) { return wy_scratch_floats<kWYT>(rows, kWYT); }
+
+int wy_prepare_wide(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
+                    bool transT, float* scratch) {
+  static_assert(kWYT == kWideWY, "one wide WY width");
+  if (nb > kWYT || rows <= 0) return DDCSVD_ERR_ARG;
+  return wy_prepare_all<kWYT>(ctx, rows, nb, Vp, ldv, tau, UT, transT, scratch);
+}
+
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
 // last first:  W1 = U_b^T C (stored K-major for the next product) and
 // C -= UT_b W1.

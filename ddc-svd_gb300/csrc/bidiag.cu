@@ -1350,44 +1350,70 @@ int range_unscale_vector(ddcsvd_context* ctx, int n, float* x, const unsigned* a
 void plan_qr(Arena& a, int m, int n, int P, GemmKind kind, QrWork* w) {
   w->ldv = (int)round_up(m, 32);
   w->P = P;
-  w->Vp = a.take<float>((size_t)w->ldv * kPanel);
+  w->Vp = a.take<float>((size_t)w->ldv * kWideWY);  // the reflectors of one super-block
   w->UT = a.take<float>((size_t)m * kPanel + 64);
   w->W1s = a.take<float>((size_t)n * kPanel + 64);
+  w->UTw = a.take<float>((size_t)m * kWideWY + 64);
+  w->W1w = a.take<float>((size_t)n * kWideWY + 64);
   w->part = a.take<float>((size_t)2 * P * kPS + 64);
   w->rowi = a.take<float>(2 * (kPanel + 4));
-  w->wys = a.take<float>(wy_block_scratch_floats(m));
+  w->wys = a.take<float>(std::max(wy_block_scratch_floats(m), wy_wide_scratch_floats(m)));
   w->bar = a.take<GridBarrier>(4);
-  w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kPanel, m);
+  w->gemm_scratch_bytes = gemm_scratch_bytes(kind, n, kWideWY, m);
   w->gemm_scratch = a.take<char>(w->gemm_scratch_bytes);
 }
 
+// Two-level blocking: super-blocks of kWideWY columns, each factored as
+// kPanel-column panels (qr_panel_kernel) whose reflectors are applied at once
+// only to the super-block's own remaining columns; the far trailing matrix is
+// updated once per super-block with a kWideWY-reflector WY block (K = 128
+// tensor-core products instead of four K = 32 passes over it).
 int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau, QrWork& w, GemmKind kind) {
   if (m < n || n <= 0) return DDCSVD_ERR_ARG;
   Arena sc;
   sc.base = w.gemm_scratch;
   sc.plan = false;
   sc.cap = w.gemm_scratch_bytes;
-  for (int k0 = 0; k0 < n; k0 += kPanel) {
-    const int nb = std::min(kPanel, n - k0);
-    QrParams q;
-    q.m = m; q.k0 = k0; q.nb = nb; q.ldw = ldw; q.P = w.P;
-    q.rc = (int)round_up(ceil_div(m - (k0 & ~3), w.P), 4);
-    q.W = W; q.tau = tau; q.Vp = w.Vp; q.ldv = w.ldv;
-    q.part = w.part; q.rowi = w.rowi; q.bar = w.bar; q.st = ctx->d_status;
-    DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
-    ktimer_begin(ctx, KC_QR);
-    DDC_TRY(launch_coop((const void*)qr_panel_kernel, w.P, kBidiagThreads, qr_smem_bytes(q.rc, kBidiagThreads), &q,
-                        ctx->stream));
-    ktimer_end(ctx);
-    if (k0 + nb < n) {
-      // W[k0:, k0+nb:] := (I - V T^T V^T) W[k0:, k0+nb:] on tensor cores
-      const int rows = m - k0, ncols = n - k0 - nb;
+  for (int K0 = 0; K0 < n; K0 += kWideWY) {
+    const int NB = std::min(kWideWY, n - K0);
+    // reflector block of the super-block: column c = reflector K0 + c over
+    // rows K0.. (zero above its unit entry)
+    DDC_CUDA_TRY(cudaMemsetAsync(w.Vp, 0, sizeof(float) * (size_t)w.ldv * NB, ctx->stream));
+    for (int k0 = K0; k0 < K0 + NB; k0 += kPanel) {
+      const int nb = std::min(kPanel, K0 + NB - k0);
+      const int off = k0 - K0;
+      QrParams q;
+      q.m = m; q.k0 = k0; q.nb = nb; q.ldw = ldw; q.P = w.P;
+      q.rc = (int)round_up(ceil_div(m - (k0 & ~3), w.P), 4);
+      q.W = W; q.tau = tau; q.Vp = w.Vp + off + (size_t)off * w.ldv; q.ldv = w.ldv;
+      q.part = w.part; q.rowi = w.rowi; q.bar = w.bar; q.st = ctx->d_status;
+      DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
       ktimer_begin(ctx, KC_QR);
-      DDC_TRY(wy_prepare_block(ctx, rows, nb, w.Vp, w.ldv, tau + k0, w.UT, true, w.wys));
-      DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, nb, rows, W + (size_t)(k0 + nb) * ldw, ldw, k0, w.Vp, w.ldv, 0,
-                               w.W1s, kPanel, 1.f, 0.f, &sc));
-      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kPanel, 0, w.W1s, kPanel, 0,
-                             W + k0 + (size_t)(k0 + nb) * ldw, ldw, -1.f, 1.f, &sc));
+      DDC_TRY(launch_coop((const void*)qr_panel_kernel, w.P, kBidiagThreads, qr_smem_bytes(q.rc, kBidiagThreads), &q,
+                          ctx->stream));
+      ktimer_end(ctx);
+      if (k0 + nb < K0 + NB) {
+        // the super-block's remaining columns: W[k0:, k0+nb:K0+NB] := (I - V T^T V^T) W[...]
+        const int rows = m - k0, ncols = K0 + NB - k0 - nb;
+        const float* Vpan = w.Vp + (size_t)off * w.ldv;  // panel's reflectors, rows from K0
+        ktimer_begin(ctx, KC_QR);
+        DDC_TRY(wy_prepare_block(ctx, rows, nb, Vpan + off, w.ldv, tau + k0, w.UT, true, w.wys));
+        DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, nb, rows, W + (size_t)(k0 + nb) * ldw, ldw, k0, Vpan, w.ldv, off,
+                                 w.W1s, kPanel, 1.f, 0.f, &sc));
+        DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, nb, w.UT, kPanel, 0, w.W1s, kPanel, 0,
+                               W + k0 + (size_t)(k0 + nb) * ldw, ldw, -1.f, 1.f, &sc));
+        ktimer_end(ctx);
+      }
+    }
+    if (K0 + NB < n) {
+      // far trailing update: W[K0:, K0+NB:] := (I - V T^T V^T) W[K0:, K0+NB:]
+      const int rows = m - K0, ncols = n - K0 - NB;
+      ktimer_begin(ctx, KC_QR);
+      DDC_TRY(wy_prepare_wide(ctx, rows, NB, w.Vp, w.ldv, tau + K0, w.UTw, true, w.wys));
+      DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, NB, rows, W + (size_t)(K0 + NB) * ldw, ldw, K0, w.Vp, w.ldv, 0,
+                               w.W1w, kWideWY, 1.f, 0.f, &sc));
+      DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, NB, w.UTw, kWideWY, 0, w.W1w, kWideWY, 0,
+                             W + K0 + (size_t)(K0 + NB) * ldw, ldw, -1.f, 1.f, &sc));
       ktimer_end(ctx);
     }
   }

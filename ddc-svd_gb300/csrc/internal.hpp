@@ -184,11 +184,17 @@ int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W,
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
                      bool transT, float* scratch);
 size_t wy_block_scratch_floats(int rows);  // scratch of wy_prepare_block
+constexpr int kWideWY = 128;  // reflectors per wide WY block (back-transformation, QR super-blocks)
+// UT of at most kWideWY reflectors, row-major with kWideWY columns.
+int wy_prepare_wide(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,
+                    bool transT, float* scratch);
+size_t wy_wide_scratch_floats(int rows);
 // Householder QR of the m x n (m >= n) matrix W in place (R on and above the
 // diagonal, reflectors below in LAPACK form, tau separate), tensor-core
 // trailing updates; the input must be range-scaled (max|a| in [2^-40, 2^40]).
 struct QrWork {
   float *Vp, *UT, *W1s, *part, *rowi, *wys;
+  float *UTw, *W1w;  // far trailing update of a super-block (kWideWY reflectors)
   GridBarrier* bar;
   char* gemm_scratch;
   size_t gemm_scratch_bytes;

@@ -165,10 +165,12 @@ def test_svd_large_shapes(lib, cuda, orc, m, n):
 
 
 @pytest.mark.parametrize("m,n,kind", [(600, 256, "uniform"), (1200, 200, "graded"), (256, 700, "uniform"),
-                                      (2048, 130, "rank_deficient")])
+                                      (2048, 130, "rank_deficient"), (1001, 300, "uniform"), (4100, 1030, "graded")])
 def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
     """m >= 2n (or n >= 2m) in the tensor-core modes goes through Householder
-    QR, the SVD of R and U = Q [U_R; 0]."""
+    QR, the SVD of R and U = Q [U_R; 0].  QR works in 128-column super-blocks
+    of 32-column panels: 200, 300 and 1030 columns end in partial super-blocks
+    and partial panels; 1001 rows are not a multiple of 4."""
     if not _mode_available(lib, "tf32x6"):
         pytest.skip("tf32x6 unavailable")
     rng = np.random.default_rng(m + 7 * n)
