@@ -485,6 +485,7 @@ static int create_ctx(ddcsvd_context** out, int device) {
   ddcsvd_context* c = new ddcsvd_context();
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
   DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->own_stream = true;
   DDC_CUDA_TRY(cudaMalloc(&c->d_status, sizeof(DevStatus)));

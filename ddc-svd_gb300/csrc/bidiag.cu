@@ -1237,6 +1237,13 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
   count_launch(2);
   DDC_CUDA_TRY(cudaGetLastError());
   for (int k0 = 0; k0 < n; k0 += kPanel) {
+    // the remaining columns on one thread-block cluster once they fit
+    if (bidiag_tail_columns(ctx, m, n, k0) > 0) {
+      ktimer_begin(ctx, KC_BIDIAG);
+      DDC_TRY(bidiag_tail(ctx, m, n, k0, W, ldw, d, e, tauq, taup));
+      ktimer_end(ctx);
+      break;
+    }
     const int nb = std::min(kPanel, n - k0);
     PanelParams pp;
     pp.m = m; pp.n = n; pp.k0 = k0; pp.nb = nb; pp.ldw = ldw; pp.ldn = w.ldn; pp.P = P;

@@ -12,6 +12,8 @@
 struct ddcsvd_context {
   int device = 0;
   int num_sms = 0;
+  size_t smem_optin = 0;  // opt-in shared memory per block (bytes)
+  int tail_cluster = -1;  // cluster size of the bidiagonalisation tail (0 = none, -1 = not yet probed)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device workspace (grown on demand, reused across calls)
@@ -36,7 +38,7 @@ struct ddcsvd_context {
   // launch-configuration knobs (ddcsvd_set_tuning / ddcsvd_autotune_*); none
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
-  int tune[8] = {16, 0, 512, 1, 8, 2, 1, 0};
+  int tune[8] = {16, 0, 512, 1, 8, 2, 1, 512};
   // set while an SVD of the R factor runs inside the tall-matrix path
   bool nested = false;
   std::mutex mu;
@@ -51,7 +53,8 @@ enum TuneKnob {
   TK_DC_TERMS = 4,       // D&C: secular-sum terms per lane that size the lane groups (2..32)
   TK_TALL_QR = 5,        // QR first for m >= 2n: 0 never, 1 always, 2 when the matrix exceeds 64M entries
   TK_PANEL_FUSED = 6,    // panel kernel: 1 one read of the trailing block per column (<= 8192 rows), 0 two GEMVs
-  TK_COUNT = 7
+  TK_PANEL_TAIL = 7,     // most columns left to the thread-block-cluster tail (0: never)
+  TK_COUNT = 8
 };
 }  // namespace ddcsvd
 
@@ -137,6 +140,12 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
 int bidiag_plain(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d, float* e,
                  float* tauq, float* taup, BidiagWork& w);
 int bidiag_coop_ctas(ddcsvd_context* ctx, int m, int n);
+// Columns from k0 on that the cluster tail can finish (0 = none: knob off,
+// no co-schedulable cluster, or the trailing block does not fit), and the
+// launch: the trailing block W[k0:m, k0:n] bidiagonalised on one cluster.
+int bidiag_tail_columns(ddcsvd_context* ctx, int m, int n, int k0);
+int bidiag_tail(ddcsvd_context* ctx, int m, int n, int k0, float* W, int ldw, float* d, float* e, float* tauq,
+                float* taup);
 // LAPACK-form reflectors -> the reference's normalised form, FP64 output (ld = m).
 int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw, const float* d,
                       const float* e, const float* tauq, const float* taup, double* A_out);

@@ -108,7 +108,8 @@ extern "C" int ddcsvd_autotune_svd(ddcsvd_handle_t h, int m, int n, int mode, in
   float* dS = dV + nv;
   fill_uniform_kernel<<<4 * h->num_sms, 256, 0, h->stream>>>(dA, na, 1234567u);
   count_launch();
-  std::vector<Candidates> space = {{TK_SPLITK_MAX, {1, 2, 4, 8, 16}}, {TK_TC_BN, {0, 64}}};
+  std::vector<Candidates> space = {{TK_SPLITK_MAX, {1, 2, 4, 8, 16}}, {TK_TC_BN, {0, 64}},
+                                   {TK_PANEL_TAIL, {0, 256, 512, 768}}};
   if (std::max(m, n) >= 2 * std::min(m, n)) space.push_back({TK_TALL_QR, {0, 1}});
   const int rc = coordinate_search(h, space, reps, [&]() {
     return ddcsvd_svd_f32_device(h, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode);

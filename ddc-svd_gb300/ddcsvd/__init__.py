@@ -154,7 +154,7 @@ class Handle:
         return [float(x) for x in ms], [int(x) for x in nl]
 
     TUNING_KNOBS = ("splitk_max", "tc_bn", "batch_threads", "batch_smem_full", "dc_terms", "tall_qr",
-                    "panel_fused")
+                    "panel_fused", "panel_tail")
 
     @property
     def tuning(self) -> dict:

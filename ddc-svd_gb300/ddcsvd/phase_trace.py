@@ -130,6 +130,18 @@ def main() -> None:
         print("        " + " ".join(f"{v:7.2f}" for v in est) + f" {est.sum():7.2f}")
         dur = [(t[r][13] - t[r][12]) / 1e3 for r in range(128) if t[r][12] and t[r][13]]
         print(f"  panel launches: {len(dur)}, entry->exit sum {sum(dur) / 1e3:.2f} ms")
+    # cluster tail: CTA 0, every 8th tail column
+    buf = (ctypes.c_ulonglong * (128 * 16))()
+    if lib.ddcsvd_tail_trace_read(buf) == 0:
+        t = np.array(buf, dtype=np.float64).reshape(128, 16)
+        names = ["A", "bar1", "B", "bar2", "C-red", "C-x", "bar3", "D1", "bar4", "D2"]
+        rows = [r for r in range(128) if t[r][0] and t[r][10]]
+        if rows:
+            print("cluster tail phases (us), CTA 0, every 8th column")
+            print("  col   " + " ".join(f"{n:>6s}" for n in names) + "   total")
+            for r in rows[::4]:
+                d = np.diff(t[r][:11]) / 1e3
+                print(f"  {8 * r:5d} " + " ".join(f"{v:6.2f}" for v in d) + f" {d.sum():7.2f}")
 
 
 if __name__ == "__main__":

@@ -199,9 +199,13 @@ int ddcsvd_svd_backward_f64_noalloc(void *stream, int batch, int m, int n, const
  *   [6] bidiagonalisation panels with at most 8192 rows: 1 (default) one
  *       read of the trailing block per column (y = A^T u and x = A v in one
  *       pass), 0 two separate products
+ *   [7] bidiagonalisation tail: the last columns (at most this many,
+ *       default 512; 0 never) run on one thread-block cluster with the
+ *       trailing block in its shared memory (unblocked, no grid-wide
+ *       barriers)
  * Knobs [0]-[4] and [6] change the results only through the summation order
- * of split-K, of the D&C sums and of the panel products; [5] changes the
- * algorithm (equally accurate).
+ * of split-K, of the D&C sums and of the panel products; [5] and [7] change
+ * the algorithm (equally accurate).
  * get/set copy up to `count` knobs. */
 int ddcsvd_get_tuning(ddcsvd_handle_t handle, int *values, int count);
 int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);

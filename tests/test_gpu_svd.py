@@ -198,10 +198,35 @@ def test_panel_one_pass_and_two_gemv_forms(lib, cuda, orc, fused, m, n):
     rng = np.random.default_rng(m * 13 + n + fused)
     A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
     h = lib.Handle()
-    h.tuning = {"panel_fused": fused, "tall_qr": 0}
+    h.tuning = {"panel_fused": fused, "tall_qr": 0, "panel_tail": 0}
     s, U, V = lib.svd_device(cuda.from_numpy(A).cuda(), mode=mode, handle=h)
     cuda.cuda.synchronize()
     check_metrics(orc, A, s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy())
+
+
+@pytest.mark.parametrize("m,n,kind", [(100, 37, "uniform"), (512, 256, "uniform"), (2050, 2050, "uniform"),
+                                      (3000, 40, "uniform"), (900, 900, "graded"), (1023, 1001, "uniform")])
+def test_bidiag_cluster_tail(lib, cuda, orc, m, n, kind):
+    """The last columns on one thread-block cluster (knob panel_tail: at most
+    that many columns, default 512) against the panel kernel alone (0): with
+    4096 every column that fits the cluster goes there (all of the smaller
+    shapes, the last 898 of 2050 x 2050), with 512 the hand-over is at
+    n - 512 where n > 512; all must meet the bounds and agree on sigma."""
+    mode = "tf32x6" if _mode_available(lib, "tf32x6") else "blocked"
+    rng = np.random.default_rng(m * 3 + n)
+    A = graded(n, seed=4, m=m)[0].astype(np.float32) if kind == "graded" else \
+        rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    outs = []
+    for tail in (4096, 512, 0):
+        h = lib.Handle()
+        h.tuning = {"panel_tail": tail, "tall_qr": 0}
+        s, U, V = lib.svd_device(cuda.from_numpy(A).cuda(), mode=mode, handle=h)
+        cuda.cuda.synchronize()
+        s, U, V = s.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy()
+        check_metrics(orc, A, s, U, V)
+        outs.append(s)
+    for o in outs[:2]:
+        assert np.max(np.abs(o - outs[2])) <= TOL * outs[2].max()
 
 
 @pytest.mark.parametrize("mode", ["blocked", "tf32x6"])

@@ -18,7 +18,7 @@ def test_tuning_roundtrip(lib, cuda):
     h = lib.Handle()
     t0 = h.tuning
     assert t0 == {"splitk_max": 16, "tc_bn": 0, "batch_threads": 512, "batch_smem_full": 1, "dc_terms": 8,
-                  "tall_qr": 2, "panel_fused": 1}
+                  "tall_qr": 2, "panel_fused": 1, "panel_tail": 512}
     h.tuning = {"splitk_max": 4, "dc_terms": 16}
     assert h.tuning["splitk_max"] == 4 and h.tuning["dc_terms"] == 16 and h.tuning["tc_bn"] == 0
     h.tuning = t0
