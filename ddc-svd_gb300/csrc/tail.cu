@@ -6,8 +6,9 @@
 // C = 16 where the GPU can co-schedule that many, else 8), the remaining
 // columns no longer pay the grid-wide costs of the panel kernel (two grid
 // barriers and two reductions over 152 partial records per column, ~9 us at
-// any size).  Here every CTA holds a block of columns of the trailing block,
-// all rows, in its shared memory and the algorithm is the unblocked one of
+// any size).  Here CTA k holds columns k, k + C, k + 2C, ... of the trailing
+// block (cyclic, so the work stays even while columns retire), all rows, in
+// its shared memory and the algorithm is the unblocked one of
 // the reference (bidiag_par.c:310-397, left_update_mat.cl / right_update_mat.cl):
 // per column a left reflector and its rank-1 update, then a right reflector
 // and its rank-1 update, exchanged through distributed shared memory with
@@ -48,7 +49,7 @@ __device__ unsigned long long g_tail_trace[128 * 16];
 
 struct TailParams {
   int mt, nt;     // trailing block: rows, columns (mt >= nt)
-  int ncb;        // columns per CTA
+  int ncb;        // columns per CTA (at most)
   float* W;       // trailing block (its row 0 / column 0 = the first tail column)
   int ldw;
   float *d, *e, *tauq, *taup;  // offset to the first tail column
@@ -85,7 +86,10 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
   const int rank = (int)cluster.block_rank();
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5, nt_ = blockDim.x;
   const int mt = p.mt, ncols = p.nt, ncb = p.ncb;
-  const int c0 = rank * ncb, c1 = min(ncols, c0 + ncb);
+  // own columns: c = rank + l * C, l < nown (local index l)
+  const int nown = rank < ncols ? (ncols - rank + C - 1) / C : 0;
+  // first local index whose column is >= c
+  auto lfirst = [&](int c) { return c <= rank ? 0 : (c - rank + C - 1) / C; };
   float* A = sm;
   float* u = A + (((size_t)mt * ncb + 3) & ~(size_t)3);
   float* xp = u + tail_vec_floats(mt);
@@ -96,17 +100,17 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
   FF* nrm = reinterpret_cast<FF*>(scal + 8);
 
   // own columns into shared memory
-  for (int c = c0; c < c1; c++)
-    for (int r = t; r < mt; r += nt_) A[r + (size_t)(c - c0) * mt] = p.W[r + (size_t)c * p.ldw];
+  for (int l = 0; l < nown; l++)
+    for (int r = t; r < mt; r += nt_) A[r + (size_t)l * mt] = p.W[r + (size_t)(rank + l * C) * p.ldw];
   __syncthreads();
   cluster.sync();
 
   for (int i = 0; i < ncols; i++) {
-    const int own_i = i / ncb;  // rank owning column i
+    const int own_i = i % C;  // rank owning column i (its local index i / C)
     TMARK(0);
     // ---- A: left reflector from column i (its owner)
     if (rank == own_i) {
-      float* col = A + (size_t)(i - c0) * mt;
+      float* col = A + (size_t)(i / C) * mt;
       FF s2{0.f, 0.f};
       for (int r = i + 1 + t; r < mt; r += nt_) s2 = ff_add_sq(s2, col[r]);
       s2 = tail_sum_ff(s2, red);
@@ -125,13 +129,13 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
     TMARK(2);
     // ---- B: left update of the own columns > i, partial norm of row i
     {
-      const float* ucol = cluster.map_shared_rank(A + (size_t)(i - own_i * ncb) * mt, own_i);
+      const float* ucol = cluster.map_shared_rank(A + (size_t)(i / C) * mt, own_i);
       const float tq = *cluster.map_shared_rank(scal, own_i);
       for (int r = i + t; r < mt; r += nt_) u[r] = ucol[r];
       __syncthreads();
       if (tq != 0.f) {
-        for (int c = max(c0, i + 1) + wid; c < c1; c += nw) {  // warp per column
-          float* col = A + (size_t)(c - c0) * mt;
+        for (int l = lfirst(i + 1) + wid; l < nown; l += nw) {  // warp per column
+          float* col = A + (size_t)l * mt;
           float y = 0.f;
           for (int r = i + lane; r < mt; r += 32) y += u[r] * col[r];
           y = warp_sum(y) * tq;
@@ -140,12 +144,12 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
       }
       __syncthreads();
       FF s{0.f, 0.f};
-      for (int c = max(c0, i + 2) + t; c < c1; c += nt_) s = ff_add_sq(s, A[i + (size_t)(c - c0) * mt]);
+      for (int l = lfirst(i + 2) + t; l < nown; l += nt_) s = ff_add_sq(s, A[i + (size_t)l * mt]);
       s = tail_sum_ff(s, red);
       if (t == 0) {
         *nrm = s;
         // the row's first element, published before its owner overwrites it in C
-        if (i + 1 >= c0 && i + 1 < c1) scal[3] = A[i + (size_t)(i + 1 - c0) * mt];
+        if (i + 1 < ncols && (i + 1) % C == rank) scal[3] = A[i + (size_t)((i + 1) / C) * mt];
       }
     }
     if (i == ncols - 1) break;  // last column: no right reflector
@@ -155,10 +159,11 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
     // ---- C: right reflector from row i (every CTA forms it), partial x
     float tp;
     {
-      if (t == 0) {
-        FF tot{0.f, 0.f};
-        for (int k = 0; k < C; k++) tot = ff_add(tot, *cluster.map_shared_rank(nrm, k));
-        const float x0 = *cluster.map_shared_rank(scal + 3, (i + 1) / ncb);
+      if (t < 32) {
+        // the C partial norms fetched by lanes 0..C-1 at once, added by one shuffle tree
+        FF v = t < C ? *cluster.map_shared_rank(nrm, t) : FF{0.f, 0.f};
+        const FF tot = warp_sum_ff(v);
+        const float x0 = *cluster.map_shared_rank(scal + 3, (i + 1) % C);
         float beta, tpv, sp;
         if (i < ncols - 2) {
           householder_ff(x0, tot, &beta, &tpv, &sp);
@@ -167,25 +172,28 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
           tpv = 0.f;
           sp = 0.f;
         }
-        if (rank == 0) {
-          p.e[i] = beta;
-          p.taup[i] = tpv;
+        if (t == 0) {
+          if (rank == 0) {
+            p.e[i] = beta;
+            p.taup[i] = tpv;
+          }
+          scal[1] = tpv;
+          scal[2] = sp;
         }
-        scal[1] = tpv;
-        scal[2] = sp;
       }
       __syncthreads();
       TMARK(5);
       tp = scal[1];
       const float sp = scal[2];
-      for (int c = max(c0, i + 1) + t; c < c1; c += nt_) {
-        float* a = A + i + (size_t)(c - c0) * mt;
-        *a = (c == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
+      const int lf = lfirst(i + 1);
+      for (int l = lf + t; l < nown; l += nt_) {
+        float* a = A + i + (size_t)l * mt;
+        *a = (rank + l * C == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
       }
       __syncthreads();
       for (int r = i + 1 + t; r < mt; r += nt_) {
         float s = 0.f;
-        for (int c = max(c0, i + 1); c < c1; c++) s += A[r + (size_t)(c - c0) * mt] * A[i + (size_t)(c - c0) * mt];
+        for (int l = lf; l < nown; l++) s += A[r + (size_t)l * mt] * A[i + (size_t)l * mt];
         xp[r] = s;
       }
     }
@@ -207,9 +215,10 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
       for (int r = i + 1 + t; r < mt; r += nt_) x[r] = cluster.map_shared_rank(xs, (r - i - 1) / len)[r];
       __syncthreads();
       if (tp != 0.f) {
+        const int lf = lfirst(i + 1);
         for (int r = i + 1 + t; r < mt; r += nt_) {
           const float f = tp * x[r];
-          for (int c = max(c0, i + 1); c < c1; c++) A[r + (size_t)(c - c0) * mt] -= f * A[i + (size_t)(c - c0) * mt];
+          for (int l = lf; l < nown; l++) A[r + (size_t)l * mt] -= f * A[i + (size_t)l * mt];
         }
       }
       __syncthreads();
@@ -218,8 +227,8 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
   }
   // reflectors and the bidiagonal's neighbourhood back to the working matrix
   cluster.sync();
-  for (int c = c0; c < c1; c++)
-    for (int r = t; r < mt; r += nt_) p.W[r + (size_t)c * p.ldw] = A[r + (size_t)(c - c0) * mt];
+  for (int l = 0; l < nown; l++)
+    for (int r = t; r < mt; r += nt_) p.W[r + (size_t)(rank + l * C) * p.ldw] = A[r + (size_t)l * mt];
 }
 
 // Cluster size the device can co-schedule (16, else 8, else 0), cached.
