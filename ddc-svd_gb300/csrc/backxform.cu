@@ -104,10 +104,11 @@ __host__ __device__ inline long long ut_offset(int b, int rows_total) {
 }
 
 // WY preparation of every block b (reflectors j0 = b NB ... j0 + bs - 1,
-// rows [j0, rows_total) of Uc), in three row-parallel kernels:
+// rows [j0, rows_total) of Uc), in four row- or entry-parallel kernels:
 //   wy_gram_kernel     grid (block, row chunk): partial G = U^T U of a chunk
-//   wy_tfactor_kernel  grid (block): G = sum of the chunk partials in chunk
-//                      order, then the compact-WY factor T
+//   wy_gsum_kernel     grid (entries, block): G = sum of the chunk partials
+//                      in chunk order, thread per entry
+//   wy_tfactor_kernel  grid (block): the compact-WY factor T from G
 //                      (T[l,l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l])
 //   wy_ut_kernel       grid (block, row chunk): UT = U T (row-major, ld NB)
 // so that applying the block is C -= UT (U^T C) (or, with T^T, the
@@ -115,7 +116,9 @@ __host__ __device__ inline long long ut_offset(int b, int rows_total) {
 // 1.3 ms for an 8192-row block.  NB = 64 (QR path) or 128 (back-transformation:
 // half the passes over C of 64-reflector blocks).
 constexpr int kPrepRows = 32;    // rows per shared-memory tile
-constexpr int kChunkRows = 512;  // rows per CTA of the chunked kernels
+constexpr int kChunkRows = 512;  // rows per CTA of the chunked kernels (many blocks)
+constexpr int kChunkRowsFew = 128;  // the same when a call has at most two blocks (QR panels / super-blocks)
+__host__ __device__ inline int wy_chunk_rows(int nblk) { return nblk <= 2 ? kChunkRowsFew : kChunkRows; }
 constexpr int kWYT = 128;        // reflectors per WY block of the tensor-core back-transformation
 
 template <int NB>
@@ -138,14 +141,14 @@ __device__ __forceinline__ void wy_load_tile(float (*sU)[NB + 1], const float* U
 // 256 threads as 16 x 16, each an (NB/16) x (NB/16) tile of G.
 template <int NB>
 __global__ void __launch_bounds__(256) wy_gram_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
-                                                      float* Gp, int nchunk) {
+                                                      float* Gp, int nchunk, int chunk) {
   constexpr int R = NB / 16;
   __shared__ float sU[kPrepRows][NB + 1];
   int j0, bs, rows;
   wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
-  const int c0 = blockIdx.y * kChunkRows;
+  const int c0 = blockIdx.y * chunk;
   if (bs <= 0 || c0 >= rows) return;
-  const int c1 = min(rows, c0 + kChunkRows);
+  const int c1 = min(rows, c0 + chunk);
   const float* U = Uc + j0 + (size_t)j0 * ldu;
   const int t = threadIdx.x, ti = t & 15, tj = t >> 4;
   float acc[R][R];
@@ -178,25 +181,38 @@ __global__ void __launch_bounds__(256) wy_gram_kernel(int rows_total, int nref, 
     for (int c = 0; c < R; c++) G[(R * ti + a) + (size_t)(R * tj + c) * NB] = acc[a][c];
 }
 
+// G of every block: the chunk partials of each entry added in chunk order
+// (thread per entry; grid (NB^2 / 256, blocks)).
+template <int NB>
+__global__ void __launch_bounds__(256) wy_gsum_kernel(int rows_total, int nref, const float* __restrict__ Gp,
+                                                      int nchunk, int chunk, float* G) {
+  int j0, bs, rows;
+  wy_block_geom<NB>(blockIdx.y, rows_total, nref, j0, bs, rows);
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bs <= 0 || rows <= 0 || idx >= NB * NB) return;
+  const int nc = ceil_div(rows, chunk);
+  const float* src = Gp + (size_t)blockIdx.y * nchunk * NB * NB + idx;
+  float g = 0.f;
+  for (int s = 0; s < nc; s++) g += src[(size_t)s * NB * NB];
+  G[(size_t)blockIdx.y * NB * NB + idx] = g;
+}
+
 // 4 * NB threads, four per row of T; sG and sT in dynamic shared memory
 // (2 NB (NB + 1) floats).
 template <int NB>
 __global__ void __launch_bounds__(4 * NB) wy_tfactor_kernel(int rows_total, int nref, const float* __restrict__ tau,
-                                                            const float* __restrict__ Gp, int nchunk, float* Tout,
-                                                            int transT) {
+                                                            const float* __restrict__ G, float* Tout, int transT) {
   extern __shared__ float wsm[];
   float(*sG)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm);
   float(*sT)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + NB * (NB + 1));
   int j0, bs, rows;
   wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
   if (bs <= 0 || rows <= 0) return;
-  const int nc = ceil_div(rows, kChunkRows);
   const int t = threadIdx.x;
+  const float* Gb = G + (size_t)blockIdx.x * NB * NB;
   for (int idx = t; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, c = idx / NB;
-    float g = 0.f;
-    for (int s = 0; s < nc; s++) g += Gp[((size_t)blockIdx.x * nchunk + s) * NB * NB + idx];
-    sG[r][c] = g;
+    sG[r][c] = Gb[idx];
     sT[r][c] = 0.f;
   }
   __syncthreads();
@@ -228,7 +244,7 @@ __global__ void __launch_bounds__(4 * NB) wy_tfactor_kernel(int rows_total, int 
 // ([NB][NB], T[k][c]) in dynamic shared memory.
 template <int NB>
 __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
-                                                    const float* __restrict__ Tin, float* UT) {
+                                                    const float* __restrict__ Tin, float* UT, int chunk) {
   constexpr int CG = NB / 4;    // column groups
   constexpr int RPT = NB / 32;  // rows per thread
   static_assert(256 / CG * RPT == kPrepRows, "row groups must cover the tile");
@@ -237,9 +253,9 @@ __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, co
   float(*sT)[NB] = reinterpret_cast<float(*)[NB]>(wsm + kPrepRows * (NB + 1));
   int j0, bs, rows;
   wy_block_geom<NB>(blockIdx.x, rows_total, nref, j0, bs, rows);
-  const int c0 = blockIdx.y * kChunkRows;
+  const int c0 = blockIdx.y * chunk;
   if (bs <= 0 || c0 >= rows) return;
-  const int c1 = min(rows, c0 + kChunkRows);
+  const int c1 = min(rows, c0 + chunk);
   const float* U = Uc + j0 + (size_t)j0 * ldu;
   float* out = UT + ut_offset<NB>(blockIdx.x, rows_total);
   const int t = threadIdx.x;
@@ -277,27 +293,31 @@ __global__ void __launch_bounds__(256) wy_ut_kernel(int rows_total, int nref, co
 template <int NB = kWY>
 static size_t wy_scratch_floats(int rows_total, int nref) {
   const int nblk = ceil_div(std::max(nref, 1), NB);
-  const int nchunk = ceil_div(std::max(rows_total, 1), kChunkRows);
-  return (size_t)nblk * nchunk * NB * NB + (size_t)nblk * NB * NB + 64;
+  const int nchunk = ceil_div(std::max(rows_total, 1), wy_chunk_rows(nblk));
+  return (size_t)nblk * nchunk * NB * NB + 2 * (size_t)nblk * NB * NB + 64;
 }
 
 template <int NB>
 static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const float* Uc, int ldu, const float* tau,
                           float* UT, bool transT, float* scratch) {
   const int nblk = ceil_div(nref, NB);
-  const int nchunk = ceil_div(rows_total, kChunkRows);
+  const int chunk = wy_chunk_rows(nblk);
+  const int nchunk = ceil_div(rows_total, chunk);
   float* Gp = scratch;
-  float* T = scratch + (size_t)nblk * nchunk * NB * NB;
+  float* G = scratch + (size_t)nblk * nchunk * NB * NB;
+  float* T = G + (size_t)nblk * NB * NB;
   const int tf_smem = 2 * NB * (NB + 1) * (int)sizeof(float);
   const int ut_smem = (kPrepRows * (NB + 1) + NB * NB) * (int)sizeof(float);
   DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_tfactor_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     tf_smem));
   DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_ut_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     ut_smem));
-  wy_gram_kernel<NB><<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, Gp, nchunk);
-  wy_tfactor_kernel<NB><<<nblk, 4 * NB, tf_smem, ctx->stream>>>(rows_total, nref, tau, Gp, nchunk, T, transT ? 1 : 0);
-  wy_ut_kernel<NB><<<dim3(nblk, nchunk), 256, ut_smem, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT);
-  count_launch(3);
+  wy_gram_kernel<NB><<<dim3(nblk, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, Uc, ldu, Gp, nchunk, chunk);
+  wy_gsum_kernel<NB><<<dim3(ceil_div(NB * NB, 256), nblk), 256, 0, ctx->stream>>>(rows_total, nref, Gp, nchunk,
+                                                                                  chunk, G);
+  wy_tfactor_kernel<NB><<<nblk, 4 * NB, tf_smem, ctx->stream>>>(rows_total, nref, tau, G, T, transT ? 1 : 0);
+  wy_ut_kernel<NB><<<dim3(nblk, nchunk), 256, ut_smem, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT, chunk);
+  count_launch(4);
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
 }
