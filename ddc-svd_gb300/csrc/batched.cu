@@ -520,6 +520,20 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   float* he = hd + Ntot + 8;
   DDC_CUDA_TRY(cudaMemcpyAsync(hd, d, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
   DDC_CUDA_TRY(cudaMemcpyAsync(he, e, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
+  // while stage 1 runs: the D&C forest and vector layout for one block per
+  // problem (a split inside a problem is rare; prep_build lays out anew then)
+  Prep P;
+  {
+    std::vector<int> starts0;
+    starts0.reserve(batch + 1);
+    int off = 0;
+    for (int b = 0; b < batch; b++) {
+      if (gn[b] > 0) starts0.push_back(off);
+      off += gn[b];
+    }
+    starts0.push_back(off);
+    DDC_TRY(prep_layout(h, gn, gout, starts0, pin + tb + rb + ab, blob, &P));
+  }
   DDC_CUDA_TRY(cudaStreamSynchronize(h->stream));
   double* a64 = (double*)(pin + tb + rb);
   double* b64 = a64 + Ntot + 8;
@@ -531,7 +545,6 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
       b64[o + i] = (i < nb - 1) ? (double)he[o + i] : 0.0;
     }
   }
-  Prep P;
   DDC_TRY(prep_build(h, gn, gout, a64, b64, FLT_EPSILON, false, pin + tb + rb + ab, blob, &P));
   // ---- stages 2-4
   {

@@ -691,6 +691,167 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
   }
 }
 
+// ---------------------------------------------------------------- tree per CTA
+// A forest of many small trees (a batch of small bidiagonals): every CTA takes
+// whole trees, largest first, from an atomic counter and runs their depths
+// bottom-up with block barriers only -- the same leaf, set-up, root, z-hat,
+// row and finish steps as dc_kernel, without its grid barriers (where CTAs
+// waited for the slowest one at every phase of every depth).
+struct DcTrees {
+  int ntrees;
+  const int* tree_seg;   // [ntrees + 1] ranges of segments
+  const int* seg_lo;     // [nseg + 1] ranges of `nodes` (merges, then leaves)
+  const int* seg_mid;    // [nseg] end of the merges
+  const int* seg_depth;  // [nseg]
+  const int* seg_G;      // [nseg] lanes per root
+  const int* nodes;
+  const int* order;      // trees, largest first
+  int* counter;
+};
+constexpr int kDcTreeThreads = 256;
+
+// merge node of segment [lo, mid) containing slot position pos (or -1)
+__device__ __forceinline__ int seg_find(const DcParams& p, const int* nodes, int lo, int mid, int pos) {
+  int a = lo, b = mid;
+  while (a < b) {
+    const int c = (a + b) >> 1;
+    if (p.nd_slot[nodes[c]] <= pos) a = c + 1; else b = c;
+  }
+  if (a == lo) return -1;
+  const int node = nodes[a - 1];
+  return (pos < p.nd_slot[node] + p.nd_nn[node]) ? node : -1;
+}
+
+__global__ void __launch_bounds__(kDcTreeThreads, 2) dc_tree_kernel(DcParams p, DcTrees tr) {
+  __shared__ int shi[40];
+  __shared__ double shd[40];
+  __shared__ int s_tree;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  while (true) {
+    if (t == 0) s_tree = atomicAdd(tr.counter, 1);
+    __syncthreads();
+    const int qi = s_tree;
+    __syncthreads();
+    if (qi >= tr.ntrees) break;
+    const int tree = tr.order[qi];
+    for (int k = tr.tree_seg[tree]; k < tr.tree_seg[tree + 1]; k++) {
+      const int lo = tr.seg_lo[k], mid = tr.seg_mid[k], hi = tr.seg_lo[k + 1];
+      const int d = tr.seg_depth[k], par = d & 1;
+      const bool rows = d > 0;
+      // ---- leaves (thread each)
+      for (int x = mid + t; x < hi; x += blockDim.x) {
+        const int node = tr.nodes[x];
+        const int nn = p.nd_nn[node], slot = p.nd_slot[node], r0 = p.nd_r0[node];
+        double phi, psi;
+        dc_leaf(nn, p.b1 + r0, p.b2 + r0, p.sig[par] + slot, p.F[par] + slot, p.L[par] + slot, &phi, &psi);
+        p.phi[node] = phi;
+        p.psi[node] = psi;
+      }
+      if (mid == lo) {  // only leaves at this depth
+        __syncthreads();
+        continue;
+      }
+      // ---- merge set-up: the CTA for large nodes, a warp for small ones
+      {
+        const CtaGroup cg{shi, shd};
+        for (int x = lo; x < mid; x++)
+          if (p.nd_nn[tr.nodes[x]] > kWarpNode) dc_setup_node(p, tr.nodes[x], par, cg);
+        const WarpGroup wg;
+        for (int x = lo + wid; x < mid; x += nw)
+          if (p.nd_nn[tr.nodes[x]] <= kWarpNode) dc_setup_node(p, tr.nodes[x], par, wg);
+      }
+      __syncthreads();
+      const LaneGroup g = make_group(tr.seg_G[k], lane);
+      const int gid = t / g.G, ngroups = blockDim.x / g.G;
+      const int pos0 = p.nd_slot[tr.nodes[lo]];
+      const int pos1 = p.nd_slot[tr.nodes[mid - 1]] + p.nd_nn[tr.nodes[mid - 1]];
+      // ---- secular roots (lane group per root)
+      for (int pos = pos0 + gid; pos < pos1; pos += ngroups) {
+        const int node = seg_find(p, tr.nodes, lo, mid, pos);
+        if (node < 0) continue;
+        const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
+        if (i >= q) continue;
+        int o;
+        double tau;
+        const bool ok =
+            sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau);
+        if (g.lg == 0) {
+          p.org[pos] = o;
+          p.tau[pos] = tau;
+          const double dorg = p.dq[slot + o];
+          p.rS[pos] = sqrt(dorg * dorg + tau);
+          if (!ok) set_error(p.st, DDCSVD_ERR_NOCONV, pos);
+        }
+      }
+      __syncthreads();
+      if (rows) {
+        // ---- z-hat (lane group per component)
+        for (int pos = pos0 + gid; pos < pos1; pos += ngroups) {
+          const int node = seg_find(p, tr.nodes, lo, mid, pos);
+          if (node < 0) continue;
+          const int slot = p.nd_slot[node], j = pos - slot, q = p.nq[node];
+          if (j >= q) continue;
+          const double* dq = p.dq + slot;
+          const double* tau = p.tau + slot;
+          const int* org = p.org + slot;
+          const double dj = dq[j];
+          double prod = 1.0;
+          for (int kk = g.lg; kk < q - 1; kk += g.G) {
+            const int ok = org[kk];
+            const double num = tau[kk] - (dj - dq[ok]) * (dj + dq[ok]);
+            const int k2 = (kk < j) ? kk : kk + 1;
+            const double den = (dq[k2] - dj) * (dq[k2] + dj);
+            prod *= num / den;
+          }
+          prod = gprod(prod, g);
+          if (g.lg == 0) {
+            const int ol = org[q - 1];
+            prod *= tau[q - 1] - (dj - dq[ol]) * (dj + dq[ol]);
+            const double a = sqrt(fabs(prod));
+            p.zh[pos] = (p.zq[pos] >= 0.0) ? a : -a;
+          }
+        }
+        __syncthreads();
+        // ---- rows of the merged right vectors (lane group per root)
+        for (int pos = pos0 + gid; pos < pos1; pos += ngroups) {
+          const int node = seg_find(p, tr.nodes, lo, mid, pos);
+          if (node < 0) continue;
+          const int slot = p.nd_slot[node], i = pos - slot, q = p.nq[node];
+          if (i >= q) continue;
+          const double* dq = p.dq + slot;
+          const double dorg = dq[p.org[pos]], ti = p.tau[pos];
+          double nv = 0.0, sf = 0.0, sl = 0.0;
+          for (int j = g.lg; j < q; j += g.G) {
+            const double dj = dq[j];
+            const double del = (dj - dorg) * (dj + dorg) - ti;
+            const double v = p.zh[slot + j] / del;
+            nv += v * v;
+            sf += v * p.fq[slot + j];
+            sl += v * p.lq[slot + j];
+          }
+          nv = gsum(nv, g); sf = gsum(sf, g); sl = gsum(sl, g);
+          if (g.lg == 0) {
+            nv = sqrt(nv);
+            p.rF[pos] = sf / nv;
+            p.rL[pos] = sl / nv;
+          }
+        }
+        __syncthreads();
+      }
+      // ---- final merge + normalisation
+      {
+        const CtaGroup cg{shi, shd};
+        for (int x = lo; x < mid; x++)
+          if (p.nd_nn[tr.nodes[x]] > kWarpNode) dc_finish_node(p, tr.nodes[x], par, rows, cg);
+        const WarpGroup wg;
+        for (int x = lo + wid; x < mid; x += nw)
+          if (p.nd_nn[tr.nodes[x]] <= kWarpNode) dc_finish_node(p, tr.nodes[x], par, rows, wg);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 __global__ void dc_copy_out(int N, const double* s, double* out) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) out[i] = s[i];
 }
@@ -732,9 +893,16 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H, int terms_p
   const size_t cap = 2 * (size_t)N + 8;
   T.r0.reserve(cap); T.nn.reserve(cap); T.slot.reserve(cap); T.K.reserve(cap);
   T.c1.reserve(cap); T.c2.reserve(cap); T.depth.reserve(cap);
+  std::vector<int> tree_of;  // creation index -> tree
+  tree_of.reserve(cap);
+  int ntrees = 0;
   for (size_t b = 0; b + 1 < starts.size(); b++) {
     const int lo = starts[b], hi = starts[b + 1];
-    if (hi > lo) T.build(lo, hi - lo, lo, 0);
+    if (hi > lo) {
+      T.build(lo, hi - lo, lo, 0);
+      tree_of.resize(T.r0.size(), ntrees);
+      ntrees++;
+    }
   }
   const int nnodes = (int)T.r0.size();
   const int md = T.maxdepth;
@@ -744,9 +912,10 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H, int terms_p
   for (int d = 0; d <= md; d++) ds[d + 1] += ds[d];
   std::vector<int> newid(nnodes), fill(ds.begin(), ds.end() - 1);
   for (int i = 0; i < nnodes; i++) newid[i] = fill[T.depth[i]]++;
-  std::vector<int> r0(nnodes), nn(nnodes), slot(nnodes), K(nnodes), c1(nnodes), c2(nnodes);
+  std::vector<int> r0(nnodes), nn(nnodes), slot(nnodes), K(nnodes), c1(nnodes), c2(nnodes), dep(nnodes);
   for (int o = 0; o < nnodes; o++) {
     const int i = newid[o];
+    dep[i] = T.depth[o];
     r0[i] = T.r0[o]; nn[i] = T.nn[o]; slot[i] = T.slot[o]; K[i] = T.K[o];
     c1[i] = T.c1[o] >= 0 ? newid[T.c1[o]] : -1;
     c2[i] = T.c2[o] >= 0 ? newid[T.c2[o]] : -1;
@@ -775,9 +944,67 @@ void dc_build_host(int N, const std::vector<int>& starts, DcHost& H, int terms_p
   H.ints.reserve(6 * (size_t)nnodes + 3 * (md + 2) + dmerge.size());
   auto app = [&](const std::vector<int>& v) { H.ints.insert(H.ints.end(), v.begin(), v.end()); };
   app(r0); app(nn); app(slot); app(K); app(c1); app(c2); app(ds); app(dms); app(dmerge); app(dgroup);
+  // ---- per-tree schedule: each tree's nodes by depth, deepest first; within
+  // a depth its merge nodes (ascending slot) then its leaves.  New ids are
+  // sorted by (depth, slot), so one ascending pass lists every tree's nodes
+  // by depth already.
+  // stable counting sort of the node ids by tree (keeps (depth, slot) order)
+  std::vector<int> tstart(ntrees + 1, 0), bytree(nnodes);
+  for (int o = 0; o < nnodes; o++) tstart[tree_of[o] + 1]++;
+  for (int tr = 0; tr < ntrees; tr++) tstart[tr + 1] += tstart[tr];
+  {
+    std::vector<int> tree_new(nnodes), cur(tstart.begin(), tstart.end() - 1);
+    for (int o = 0; o < nnodes; o++) tree_new[newid[o]] = tree_of[o];
+    for (int i = 0; i < nnodes; i++) bytree[cur[tree_new[i]]++] = i;
+  }
+  std::vector<int> tree_seg(ntrees + 1, 0), seg_lo, seg_mid, seg_depth, seg_G, nodes_out, order(ntrees), tsize(ntrees);
+  nodes_out.reserve(nnodes);
+  seg_lo.reserve(nnodes + 1); seg_mid.reserve(nnodes); seg_depth.reserve(nnodes); seg_G.reserve(nnodes);
+  std::vector<int> bounds;  // depth-group boundaries of one tree (reused)
+  for (int tr = 0; tr < ntrees; tr++) {
+    const int* v = bytree.data() + tstart[tr];
+    const int cnt = tstart[tr + 1] - tstart[tr];
+    tsize[tr] = cnt ? nn[v[0]] : 0;  // the root (depth 0) comes first
+    tree_seg[tr] = (int)seg_lo.size();
+    bounds.clear();
+    bounds.push_back(0);
+    for (int x = 1; x < cnt; x++)
+      if (dep[v[x]] != dep[v[x - 1]]) bounds.push_back(x);
+    bounds.push_back(cnt);
+    for (int gi = (int)bounds.size() - 2; gi >= 0; gi--) {  // deepest first
+      const int a = bounds[gi], b = bounds[gi + 1];
+      seg_lo.push_back((int)nodes_out.size());
+      int mx = 0;
+      for (int x = a; x < b; x++)
+        if (K[v[x]] >= 0) {
+          nodes_out.push_back(v[x]);
+          mx = std::max(mx, nn[v[x]]);
+        }
+      seg_mid.push_back((int)nodes_out.size());
+      for (int x = a; x < b; x++)
+        if (K[v[x]] < 0) nodes_out.push_back(v[x]);
+      seg_depth.push_back(dep[v[a]]);
+      int G = 1;
+      while (G < 32 && G * tpl < mx) G <<= 1;
+      seg_G.push_back(G);
+    }
+  }
+  const int nseg = (int)seg_lo.size();
+  tree_seg[ntrees] = nseg;
+  seg_lo.push_back((int)nodes_out.size());
+  for (int tr = 0; tr < ntrees; tr++) order[tr] = tr;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return tsize[a] > tsize[b]; });
+  H.ntrees = ntrees;
+  H.nseg = nseg;
+  H.maxtree = ntrees ? tsize[order[0]] : 0;
+  H.tree_off = H.ints.size();
+  app(tree_seg); app(seg_lo); app(seg_mid); app(seg_depth); app(seg_G); app(nodes_out); app(order);
 }
 
-size_t dc_max_ints(int N) { return 9 * (size_t)(2 * N + 8) + 2 * 64 + 16; }
+// ints of the node table: 9 arrays of at most 2N + 8 entries, the per-depth
+// tables, and the per-tree schedule (at most N trees, 2N + 8 segments and nodes)
+size_t dc_max_ints(int N) { return 9 * (size_t)(2 * N + 8) + 2 * 64 + 16 + 2 * ((size_t)N + 1) + 5 * (2 * (size_t)N + 9); }
+
 
 int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, double* sigma,
              const DcHost* H, const int* dints, Arena& a, bool plan_only) {
@@ -817,6 +1044,33 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
   p.out = sigma;
   p.bar = bar;
   p.st = ctx->d_status;
+  // a forest of many small trees: whole trees per CTA, no grid barriers
+  if (H->ntrees >= 64 && H->maxtree <= 1024) {
+    DcTrees tr;
+    size_t q2 = H->tree_off;
+    const int nt = H->ntrees, ns = H->nseg;
+    tr.ntrees = nt;
+    tr.tree_seg = dints + q2; q2 += nt + 1;
+    tr.seg_lo = dints + q2; q2 += ns + 1;
+    tr.seg_mid = dints + q2; q2 += ns;
+    tr.seg_depth = dints + q2; q2 += ns;
+    tr.seg_G = dints + q2; q2 += ns;
+    tr.nodes = dints + q2; q2 += nnodes;
+    tr.order = dints + q2;
+    tr.counter = reinterpret_cast<int*>(bar);
+    int occ = 0;
+    DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dc_tree_kernel, kDcTreeThreads, 0));
+    const int grid = std::max(1, std::min(nt, ctx->num_sms * std::max(occ, 1)));
+    DDC_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), ctx->stream));
+    ktimer_begin(ctx, KC_DC);
+    dc_tree_kernel<<<grid, kDcTreeThreads, 0, ctx->stream>>>(p, tr);
+    ktimer_end(ctx);
+    count_launch();
+    dc_copy_out<<<std::min(ceil_div(N, 256), 1024), 256, 0, ctx->stream>>>(N, p.sig[0], sigma);
+    count_launch();
+    DDC_CUDA_TRY(cudaGetLastError());
+    return DDCSVD_OK;
+  }
   int occ = 0;
   DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dc_kernel, kDcThreads, 0));
   if (occ < 1) {

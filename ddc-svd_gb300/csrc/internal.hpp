@@ -155,6 +155,10 @@ int export_reflectors(ddcsvd_context* ctx, int m, int n, const float* W, int ldw
 struct DcHost {
   int maxdepth = 0;
   int nnodes = 0, ndm = 0;
+  // per-tree schedule (the tree kernel): trees, their depth segments, the
+  // largest tree, and the offset of these arrays in `ints`
+  int ntrees = 0, nseg = 0, maxtree = 0;
+  size_t tree_off = 0;
   std::vector<int> ints;  // packed node table uploaded to the device
 };
 void dc_build_host(int N, const std::vector<int>& block_starts, DcHost& H, int terms_per_lane = 8);

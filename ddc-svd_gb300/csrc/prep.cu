@@ -43,46 +43,41 @@ PrepBounds prep_bounds(const std::vector<int>& gn) {
   return B;
 }
 
-int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vector<GroupOut>& out, double* a64,
-               double* b64, double eps, bool keep_last, char* hblob, char* dblob, Prep* P) {
+// Blob sections that depend on the block starts (not on the bidiagonal's
+// values): forest, per-row block bounds, compact block bases, tiles, group
+// tables and node tables; b1 / b2 keep their fixed offsets at the front.
+int prep_layout(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vector<GroupOut>& out,
+                const std::vector<int>& starts, char* hblob, char* dblob, Prep* P) {
   const int G = (int)gn.size();
   int N = 0;
   for (int n : gn) N += n;
-  // ---- split each group, collect block starts (global)
-  std::vector<int> starts;
-  std::vector<int> blo(N), bhi(N), grp(N);
-  std::vector<int> g_lo(G);
-  int off = 0;
-  for (int g = 0; g < G; g++) {
-    const int n = gn[g];
-    g_lo[g] = off;
-    std::vector<int> st;
-    const double keep = (keep_last && n > 0) ? b64[off + n - 1] : 0.0;
-    split_bidiagonal(n, a64 + off, b64 + off, eps, st, blo.data() + off, bhi.data() + off);
-    if (keep_last && n > 0) b64[off + n - 1] = keep;
-    for (size_t i = 0; i + 1 < st.size(); i++) starts.push_back(off + st[i]);
-    for (int i = 0; i < n; i++) {
-      blo[off + i] += off;
-      bhi[off + i] += off;
-      grp[off + i] = g;
+  std::vector<int> g_lo(G), blo(N), bhi(N), grp(N);
+  {
+    int off = 0;
+    for (int g = 0; g < G; g++) {
+      g_lo[g] = off;
+      for (int i = 0; i < gn[g]; i++) grp[off + i] = g;
+      off += gn[g];
     }
-    off += n;
   }
-  starts.push_back(N);
   // ---- D&C forest over all blocks
   dc_build_host(N, starts, P->H, ctx->tune[TK_DC_TERMS]);
-  // ---- compact block storage and finalize tiles
+  // ---- compact block storage, per-row block bounds and finalize tiles
   std::vector<long long> base(N);
   std::vector<int4> tiles;
   long long store = 0;
   for (size_t s = 0; s + 1 < starts.size(); s++) {
     const int lo = starts[s], hi = starts[s + 1], nb = hi - lo;
-    for (int i = lo; i < hi; i++) base[i] = store;
+    for (int i = lo; i < hi; i++) {
+      base[i] = store;
+      blo[i] = lo;
+      bhi[i] = hi;
+    }
     store += (long long)nb * nb;
     for (int k0 = 0; k0 < nb; k0 += 32)
       for (int i0 = 0; i0 < nb; i0 += 32) tiles.push_back(make_int4(lo, nb, k0, i0));
   }
-  // ---- blob (same layout on host and device)
+  // ---- blob (same layout on host and device); b1, b2 first
   size_t o = 0;
   auto put = [&](const void* src, size_t bytes) {
     const size_t at = o;
@@ -90,8 +85,10 @@ int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vecto
     o = align256(o + bytes);
     return at;
   };
-  const size_t o_b1 = put(a64, sizeof(double) * N);
-  const size_t o_b2 = put(b64, sizeof(double) * N);
+  const size_t o_b1 = o;
+  o = align256(o + sizeof(double) * N);
+  const size_t o_b2 = o;
+  o = align256(o + sizeof(double) * N);
   const size_t o_base = put(base.data(), sizeof(long long) * N);
   const size_t o_blo = o;
   memcpy(hblob + o, blo.data(), sizeof(int) * N);
@@ -113,7 +110,9 @@ int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vecto
   const size_t o_tiles = put(tiles.data(), sizeof(int4) * tiles.size());
   const size_t o_ints = put(P->H.ints.data(), sizeof(int) * P->H.ints.size());
   P->used = o;
-  DDC_CUDA_TRY(cudaMemcpyAsync(dblob, hblob, o, cudaMemcpyHostToDevice, ctx->stream));
+  P->o_b1 = o_b1;
+  P->o_b2 = o_b2;
+  P->starts = starts;
   P->N = N;
   P->store = store;
   P->b1 = reinterpret_cast<const double*>(dblob + o_b1);
@@ -133,6 +132,35 @@ int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vecto
   L.tiles = reinterpret_cast<const int4*>(dblob + o_tiles);
   L.ntiles = (int)tiles.size();
   P->single_block = (starts.size() == 2);
+  P->laid_out = true;
+  return DDCSVD_OK;
+}
+
+int prep_build(ddcsvd_context* ctx, const std::vector<int>& gn, const std::vector<GroupOut>& out, double* a64,
+               double* b64, double eps, bool keep_last, char* hblob, char* dblob, Prep* P) {
+  const int G = (int)gn.size();
+  int N = 0;
+  for (int n : gn) N += n;
+  // ---- split each group, collect block starts (global)
+  std::vector<int> starts;
+  std::vector<int> blo(N), bhi(N);
+  int off = 0;
+  std::vector<int> st;
+  for (int g = 0; g < G; g++) {
+    const int n = gn[g];
+    st.clear();
+    const double keep = (keep_last && n > 0) ? b64[off + n - 1] : 0.0;
+    split_bidiagonal(n, a64 + off, b64 + off, eps, st, blo.data() + off, bhi.data() + off);
+    if (keep_last && n > 0) b64[off + n - 1] = keep;
+    for (size_t i = 0; i + 1 < st.size(); i++) starts.push_back(off + st[i]);
+    off += n;
+  }
+  starts.push_back(N);
+  // ---- layout (reused when prep_layout already ran for the same blocks)
+  if (!(P->laid_out && P->starts == starts)) DDC_TRY(prep_layout(ctx, gn, out, starts, hblob, dblob, P));
+  memcpy(hblob + P->o_b1, a64, sizeof(double) * N);
+  memcpy(hblob + P->o_b2, b64, sizeof(double) * N);
+  DDC_CUDA_TRY(cudaMemcpyAsync(dblob, hblob, P->used, cudaMemcpyHostToDevice, ctx->stream));
   return DDCSVD_OK;
 }
 

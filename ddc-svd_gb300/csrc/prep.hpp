@@ -49,8 +49,11 @@ struct Prep {
   const int* dints;
   long long store;
   size_t used;
+  size_t o_b1 = 0, o_b2 = 0;  // blob offsets of the bidiagonal
   int N;
   bool single_block;
+  bool laid_out = false;      // prep_layout ran for `starts`
+  std::vector<int> starts;
 };
 
 PrepBounds prep_bounds(const std::vector<int>& group_sizes);
@@ -61,5 +64,12 @@ PrepBounds prep_bounds(const std::vector<int>& group_sizes);
 // prep_bounds().blob_bytes (pinned), dblob the same on the device.
 int prep_build(ddcsvd_context* ctx, const std::vector<int>& group_sizes, const std::vector<GroupOut>& out,
                double* a64, double* b64, double eps, bool keep_last, char* hblob, char* dblob, Prep* P);
+
+// Everything of the blob but the bidiagonal's values, for the given block
+// starts (ascending, ending with N).  A caller that expects no split inside
+// a group can run it with the group boundaries while stage 1 is still on the
+// GPU; prep_build then reuses it when the splits agree (else lays out anew).
+int prep_layout(ddcsvd_context* ctx, const std::vector<int>& group_sizes, const std::vector<GroupOut>& out,
+                const std::vector<int>& starts, char* hblob, char* dblob, Prep* P);
 
 }  // namespace ddcsvd
