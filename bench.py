@@ -488,7 +488,7 @@ def main():
 
     host_call()
     e2e = []
-    for _ in range(max(2, args.steps // 2)):
+    for _ in range(max(3, args.steps)):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -53,6 +53,28 @@ def test_batched_structured(lib, cuda, orc):
     check_all(orc, mats, outs)
 
 
+def test_batched_many_trees_with_splits(lib, cuda, orc):
+    """Enough problems for the tree-per-CTA D&C (>= 64 trees) with some whose
+    bidiagonals split inside the problem (identity, diagonal, block-diagonal):
+    the layout prepared while stage 1 runs assumes one block per problem and
+    must be redone for these."""
+    rng = np.random.default_rng(8)
+    mats = uneven_batch(rng, 72, mhi=96)
+    for k in range(24):
+        n = 8 + (k % 5) * 6
+        if k % 3 == 0:
+            A = np.eye(n)
+        elif k % 3 == 1:
+            A = np.diag(np.repeat([3.0, 1.0], n // 2))
+        else:
+            A = np.zeros((n + 4, n))
+            A[:n // 2, :n // 2] = rng.standard_normal((n // 2, n // 2))
+            A[n // 2:, n // 2:] = rng.standard_normal((n + 4 - n // 2, n - n // 2))
+        mats.append(A.astype(np.float32))
+    outs = lib.svd_batched_device([cuda.from_numpy(A).cuda() for A in mats])
+    check_all(orc, mats, outs)
+
+
 def test_batched_matches_single(lib, cuda):
     """The batched and single-matrix paths agree (both against the same input)."""
     rng = np.random.default_rng(6)
