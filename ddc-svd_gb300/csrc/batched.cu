@@ -161,13 +161,28 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
       vrow[c] = v;
     }
     __syncthreads();
-    // ---- right update of rows > i (right_dotprods + right_update_mat)
+    // ---- right update of rows > i (right_dotprods + right_update_mat):
+    // two threads per row (alternate columns, partial dots joined by one
+    // shuffle) while the rows fit, so every thread works (more threads per
+    // row measured slower: shuffles and shared-memory bank conflicts)
     if (taup != 0.f) {
-      for (int r = i + 1 + t; r < m; r += blockDim.x) {
+      if (2 * (m - i - 1) <= (int)blockDim.x) {
+        const int r = i + 1 + (t >> 1), h = t & 1;
+        const bool act = r < m;
         float z = 0.f;
-        for (int c = i + 1; c < n; c++) z += M[r + (size_t)c * ld] * vrow[c];
+        if (act)
+          for (int c = i + 1 + h; c < n; c += 2) z += M[r + (size_t)c * ld] * vrow[c];
+        z += __shfl_xor_sync(0xffffffffu, z, 1);
         z *= taup;
-        for (int c = i + 1; c < n; c++) M[r + (size_t)c * ld] -= z * vrow[c];
+        if (act)
+          for (int c = i + 1 + h; c < n; c += 2) M[r + (size_t)c * ld] -= z * vrow[c];
+      } else {
+        for (int r = i + 1 + t; r < m; r += blockDim.x) {
+          float z = 0.f;
+          for (int c = i + 1; c < n; c++) z += M[r + (size_t)c * ld] * vrow[c];
+          z *= taup;
+          for (int c = i + 1; c < n; c++) M[r + (size_t)c * ld] -= z * vrow[c];
+        }
       }
     }
     __syncthreads();
