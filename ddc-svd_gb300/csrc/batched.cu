@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
 // owns rows lane + 32 k).  Reflector j is the vector v(r) = vec(j, r) for
 // rows r >= j + shift (unit leading entry stored), zero above.
 constexpr int kRowsPerLane = 8;  // register-resident columns: rows <= 256
-constexpr int kCW = 4;           // columns per warp at a time
+constexpr int kCW = 8;           // columns per warp at a time
 template <typename VecFn>
 __device__ __forceinline__ void apply_reflectors_regs(float (&c)[kCW][kRowsPerLane], int rows, int jhi, int shift,
                                                       const float* __restrict__ tau, VecFn vec, int lane) {
