@@ -114,6 +114,28 @@ def test_svd_graded_1024(lib, cuda, orc, mode):
     check_metrics(orc, A, s, U, V)
 
 
+@pytest.mark.parametrize("mode", BASE_MODES)
+@pytest.mark.parametrize("kind", ["orthogonal", "two_values", "near_repeated"])
+def test_svd_rotated_clusters(lib, cuda, orc, mode, kind):
+    """Repeated and nearly repeated singular values behind random rotations, so
+    that no zero appears in A: the FP32 bidiagonal carries superdiagonal
+    entries at rounding level, which split off at the bidiagonal's own
+    accuracy and leave every cluster member in a block of its own."""
+    rng = np.random.default_rng(17)
+    m, n = {"orthogonal": (600, 600), "two_values": (700, 520), "near_repeated": (640, 480)}[kind]
+    if kind == "orthogonal":
+        sig = np.ones(n)
+    elif kind == "two_values":
+        sig = np.repeat([2.0, 1.0], n // 2)
+    else:
+        sig = np.repeat([3.0, 1.0, 0.25], n // 3) * (1 + 1e-6 * rng.standard_normal(n))
+    Q1, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = ((Q1 * sig) @ Q2.T).astype(np.float32)
+    s, U, V = run(lib, cuda, A, mode)
+    check_metrics(orc, A, s, U, V)
+
+
 def test_svd_matches_oracle_vectors(lib, cuda, orc):
     """Per-vector agreement with the FP64 oracle (up to sign) where sigma is well separated."""
     rng = np.random.default_rng(21)
