@@ -795,7 +795,12 @@ int svd_gpu_ex(int m, int n, double* A, double* sigma, double* U, double* V, int
   std::lock_guard<std::mutex> g(h->mu);
   const int k = std::min(m, n);
   const size_t na = (size_t)m * n, nu = (size_t)m * k, nv = (size_t)n * k;
-  DDC_TRY(ensure_pinned(h, sizeof(float) * (na + k + nu + nv + 64)));
+  // at least what the bidiagonal read-back inside the call asks for, so the
+  // buffer is never reallocated under pa / pu / pv
+  const size_t own = sizeof(float) * (na + k + nu + nv + 64);
+  const size_t readback = (size_t)round_up(sizeof(float) * 2 * (k + 4), 256) +
+                          (size_t)round_up(sizeof(double) * 2 * (k + 4), 256) + prep_bounds({k}).blob_bytes;
+  DDC_TRY(ensure_pinned(h, std::max(own, readback)));
   float* pa = (float*)h->pinned;
   float* ps = pa + na;
   float* pu = ps + k;
@@ -818,44 +823,70 @@ void svd_gpu(int m, int n, double* A, double* sigma, double* U, double* V) {
   }
 }
 
+// Wide inputs (m < n, bidiag.c:130-155 / bidiag_par.c:361-383): the upper
+// reduction of A to an m x (m+1) bidiagonal is the reduction of the tall
+// C = [0 | A^T] (n x (m+1)) step for step.  Left reflector i of A is right
+// reflector i of C (row i, columns i+1..m); right reflector i of A is left
+// reflector i+1 of C; C's zero first column takes the identity; A's final
+// "no reflection on the left" is C's "one element left, no reflection on
+// the right" (bidiag.c:125-129); A's last right reflector is C's last left
+// one.  So alpha_i = e_C[i], beta_i = d_C[i+1], A[i, j] = C[j, i+1].
 void bidiag_par(int m, int n, double* A, double* alpha, double* beta) {
   t_last_error.clear();
   int rc = DDCSVD_OK;
   ddcsvd_context* h = nullptr;
-  if (m <= 0 || n <= 0 || !A || !alpha || !beta || m < n) rc = DDCSVD_ERR_ARG;
+  if (m <= 0 || n <= 0 || !A || !alpha || !beta) rc = DDCSVD_ERR_ARG;
   if (rc == DDCSVD_OK) rc = default_ctx(&h);
   if (rc == DDCSVD_OK) {
     std::lock_guard<std::mutex> g(h->mu);
-    const int ldw = (int)round_up(m, 32);
-    const size_t na = (size_t)m * n;
+    const bool wide = m < n;
+    const int mc = wide ? n : m, nc = wide ? m + 1 : n;  // the tall matrix reduced on the GPU
+    const int ldw = (int)round_up(mc, 32);
+    const size_t na = (size_t)mc * nc;
     float* dW = nullptr;
     double* dOut = nullptr;
     do {
-      if (cudaMallocAsync((void**)&dW, sizeof(float) * ((size_t)ldw * n + 4 * (size_t)n + 64), h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+      if (cudaMallocAsync((void**)&dW, sizeof(float) * ((size_t)ldw * nc + 4 * (size_t)nc + 64), h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
       if (cudaMallocAsync((void**)&dOut, sizeof(double) * na, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
-      float* dd = dW + (size_t)ldw * n;
-      float* de = dd + n;
-      float* tq = de + n;
-      float* tp = tq + n;
-      rc = ensure_pinned(h, sizeof(float) * na + sizeof(double) * na + 64);
+      float* dd = dW + (size_t)ldw * nc;
+      float* de = dd + nc;
+      float* tq = de + nc;
+      float* tp = tq + nc;
+      // [float copy of the input | 256-byte aligned FP64 reflectors]; d, e reuse the front
+      rc = ensure_pinned(h, round_up(sizeof(float) * na, 256) + sizeof(double) * na + 64);
       if (rc) break;
       float* pa = (float*)h->pinned;
-      for (size_t i = 0; i < na; i++) pa[i] = (float)A[i];
-      if (cudaMemsetAsync(dW, 0, sizeof(float) * (size_t)ldw * n, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-      if (cudaMemcpy2DAsync(dW, sizeof(float) * ldw, pa, sizeof(float) * m, sizeof(float) * m, n,
+      if (!wide) {
+        for (size_t i = 0; i < na; i++) pa[i] = (float)A[i];
+      } else {
+        for (int r = 0; r < mc; r++) pa[r] = 0.f;
+        for (int c = 0; c < m; c++)
+          for (int r = 0; r < n; r++) pa[r + (size_t)(c + 1) * mc] = (float)A[c + (size_t)r * m];
+      }
+      if (cudaMemsetAsync(dW, 0, sizeof(float) * (size_t)ldw * nc, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      if (cudaMemcpy2DAsync(dW, sizeof(float) * ldw, pa, sizeof(float) * mc, sizeof(float) * mc, nc,
                             cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-      rc = bidiag_device(h, m, n, dW, ldw, dd, de, tq, tp, DDCSVD_MODE_AUTO);
+      rc = bidiag_device(h, mc, nc, dW, ldw, dd, de, tq, tp, DDCSVD_MODE_AUTO);
       if (rc) break;
-      rc = export_reflectors(h, m, n, dW, ldw, dd, de, tq, tp, dOut);
+      rc = export_reflectors(h, mc, nc, dW, ldw, dd, de, tq, tp, dOut);
       if (rc) break;
       double* po = (double*)((char*)h->pinned + round_up(sizeof(float) * na, 256));
       float* pd = (float*)h->pinned;
       if (cudaMemcpyAsync(po, dOut, sizeof(double) * na, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-      if (cudaMemcpyAsync(pd, dd, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+      if (cudaMemcpyAsync(pd, dd, sizeof(float) * 2 * nc, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
       if (cudaStreamSynchronize(h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-      memcpy(A, po, sizeof(double) * na);
-      for (int i = 0; i < n; i++) alpha[i] = pd[i];
-      for (int i = 0; i < n - 1; i++) beta[i] = pd[n + i];
+      if (!wide) {
+        memcpy(A, po, sizeof(double) * na);
+        for (int i = 0; i < n; i++) alpha[i] = pd[i];
+        for (int i = 0; i < n - 1; i++) beta[i] = pd[n + i];
+      } else {
+        for (int c = 0; c < m; c++)
+          for (int r = 0; r < n; r++) A[c + (size_t)r * m] = po[r + (size_t)(c + 1) * mc];
+        for (int i = 0; i < m; i++) {
+          alpha[i] = pd[nc + i];
+          beta[i] = pd[i + 1];
+        }
+      }
     } while (0);
     if (dW) cudaFreeAsync(dW, h->stream);
     if (dOut) cudaFreeAsync(dOut, h->stream);

@@ -61,18 +61,22 @@ def svd_gpu_void(A: np.ndarray):
 
 
 def bidiag_par(A: np.ndarray):
-    """bidiag_par (bidiag_par.c:34) on a float64 host matrix (m >= n).
+    """bidiag_par (bidiag_par.c:34) on a float64 host matrix, any shape.
 
-    Returns (A_reflectors, alpha, beta) in the reference's storage."""
+    Returns (A_reflectors, alpha, beta) in the reference's storage: alpha has
+    min(m, n) entries, beta min(m, n) - 1 when m >= n and m when m < n (the
+    m x (m+1) upper bidiagonal of a wide matrix, bidiag.c:59-60)."""
     lib = load()
     A = np.array(A, dtype=np.float64, order="F", copy=True)
     m, n = A.shape
-    al = np.zeros(n)
-    be = np.zeros(max(n - 1, 1))
+    mn = min(m, n)
+    lb = mn - 1 if m >= n else mn
+    al = np.zeros(mn)
+    be = np.zeros(max(lb, 1))
     lib.bidiag_par(m, n, _addr(A), _addr(al), _addr(be))
     if np.isnan(al).any():
         raise DdcsvdError(2, "bidiag_par")
-    return A, al, be[: n - 1]
+    return A, al, be[:lb]
 
 
 def form_u_par(A_mod: np.ndarray):

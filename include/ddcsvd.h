@@ -73,8 +73,10 @@ typedef struct ddcsvd_context *ddcsvd_handle_t;
  * bidiagonal vectors. */
 void svd_gpu(int m, int n, double *A, double *sigma, double *U, double *V);
 
-/* Replaces bidiag_par.h:30 / bidiag_par.c:34 (m >= n).  Host buffers.
- * alpha: min(m,n) diagonal entries, beta: n-1 superdiagonal entries.  A is
+/* Replaces bidiag_par.h:30 / bidiag_par.c:34.  Host buffers, any shape.
+ * alpha: min(m,n) diagonal entries; beta: n-1 superdiagonal entries when
+ * m >= n, m entries when m < n (the m x (m+1) upper bidiagonal of a wide
+ * matrix, with the reference's last-row edge case, bidiag_par.c:361-383).  A is
  * overwritten with the reflectors as bidiag_par leaves it: the i-th left
  * reflector v in the partial column from A[i,i], the i-th right reflector in
  * the partial row from A[i,i+1], each with H = I - 2 v v^T and ||v|| = 1. */

@@ -295,7 +295,7 @@ def _form_factors_numpy(A_mod, left):
     return Q
 
 
-@pytest.mark.parametrize("m,n", [(40, 40), (90, 57), (257, 130)])
+@pytest.mark.parametrize("m,n", [(40, 40), (90, 57), (257, 130), (57, 90), (1, 6), (130, 131)])
 def test_form_factors_dropin(lib, cuda, m, n):
     """form_u_par / form_v_par on bidiag_par's reflectors: the reference's loops
     (numpy restatement) to FP64 accuracy; orthogonality and A = U [B; 0] V^T
@@ -311,9 +311,7 @@ def test_form_factors_dropin(lib, cuda, m, n):
     # orthogonal to the FP32 level
     assert np.linalg.norm(U.T @ U - np.eye(m)) / m ** 0.5 <= TOL
     assert np.linalg.norm(V.T @ V - np.eye(n)) / n ** 0.5 <= TOL
-    B = np.zeros((m, n))
-    B[np.arange(n), np.arange(n)] = al
-    B[np.arange(n - 1), np.arange(1, n)] = be
+    B = _bidiagonal(m, n, al, be)
     A32 = A.astype(np.float32).astype(np.float64)
     assert np.linalg.norm(U @ B @ V.T - A32) / np.linalg.norm(A32) <= 1e-5
 
@@ -352,37 +350,50 @@ def test_bidiag_stage_vs_oracle(lib, cuda, orc, mode, m, n):
 
 def _reflector_factors(A_r, m, n):
     """Q, P from reflectors stored the reference's way (bidiag_par.c:63-68):
-    left reflector i in A_r[i:, i], right reflector i in A_r[i, i+1:], H = I - 2 v v^T."""
+    left reflector i in A_r[i:, i], right reflector i in A_r[i, i+1:], H = I - 2 v v^T.
+    A wide matrix (m < n) has m left reflectors (the last one zero: no
+    reflection) and m right ones (bidiag.c:130-155)."""
     Q, P = np.eye(m), np.eye(n)
-    for i in range(n):
+    for i in range(min(m, n)):
         v = np.zeros(m)
         v[i:] = A_r[i:, i]
         Q = Q - 2.0 * np.outer(Q @ v, v)
-    for i in range(max(n - 2, 0)):
+    for i in range(m if m < n else max(n - 2, 0)):
         v = np.zeros(n)
         v[i + 1:] = A_r[i, i + 1:]
         P = P - 2.0 * np.outer(P @ v, v)
     return Q, P
 
 
-@pytest.mark.parametrize("name", [g for g in golden_names("bidiag_") if
-                                  (lambda s: int(s.split("_")[1].split("x")[0]) >= int(s.split("x")[1]))(g)])
+def _bidiagonal(m, n, al, be):
+    """The m x n upper bidiagonal: alpha on the diagonal, beta above it
+    (min(m, n) - 1 entries when m >= n, m when m < n)."""
+    B = np.zeros((m, n))
+    k = min(m, n)
+    B[np.arange(k), np.arange(k)] = al
+    nb = len(be)
+    B[np.arange(nb), np.arange(1, nb + 1)] = be
+    return B
+
+
+@pytest.mark.parametrize("name", golden_names("bidiag_"))
 def test_bidiag_par_dropin_vs_reference(lib, cuda, name):
+    """Square, tall and wide matrices against the reference's own outputs;
+    wide ones reduce to the m x (m+1) upper bidiagonal with the reference's
+    last-row edge case."""
     g = golden(name)
     A = g["A"]
     m, n = A.shape
     A_r, al, be = lib.bidiag_par(A)
+    assert al.shape == g["alpha"].shape and be.shape == g["beta"].shape
     scale = np.linalg.norm(A, 2)
-    tol = 1e-5 * np.sqrt(n) * scale
+    tol = 1e-5 * np.sqrt(max(m, n)) * scale
     assert np.max(np.abs(al - g["alpha"])) <= tol
-    if n > 1:
+    if len(be):
         assert np.max(np.abs(be - g["beta"])) <= tol
     # the exported reflectors (reference storage) reproduce A = Q B P^T
     Q, P = _reflector_factors(A_r, m, n)
-    B = np.zeros((m, n))
-    B[np.arange(n), np.arange(n)] = al
-    if n > 1:
-        B[np.arange(n - 1), np.arange(1, n)] = be
+    B = _bidiagonal(m, n, al, be)
     assert np.linalg.norm(A - Q @ B @ P.T) <= 1e-5 * np.linalg.norm(A)
     assert np.linalg.norm(Q.T @ Q - np.eye(m)) <= 1e-5 * np.sqrt(m)
     # and agree with the reference's FP64 reflectors to FP32 conditioning

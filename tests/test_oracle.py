@@ -17,6 +17,24 @@ def test_bidiag_matches_reference(orc, name):
     assert np.allclose(A_r[ok], g["A_refl"][ok], rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("name", [g for g in golden_names("bidiag_") if golden(g)["A"].shape[0] < golden(g)["A"].shape[1]])
+def test_wide_bidiag_is_tall_bidiag_of_padded_transpose(orc, name):
+    """The identity the GPU bidiag_par uses for m < n: the reference's wide
+    reduction (bidiag.c:130-155) is the tall reduction of C = [0 | A^T]
+    (n x (m+1)) step for step -- alpha_i = e_C[i], beta_i = d_C[i+1],
+    A_refl[i, j] = C_refl[j, i+1] -- checked on the reference's own outputs."""
+    g = golden(name)
+    A = g["A"]
+    m, n = A.shape
+    C = np.zeros((n, m + 1))
+    C[:, 1:] = A.T
+    C_r, d, e = orc.bidiag(C)
+    scale = np.abs(A).max()
+    assert np.allclose(e[:m], g["alpha"], rtol=0, atol=1e-12 * scale)
+    assert np.allclose(d[1:m + 1], g["beta"], rtol=0, atol=1e-12 * scale)
+    assert np.allclose(C_r[:, 1:].T, g["A_refl"], rtol=0, atol=1e-10)
+
+
 @pytest.mark.parametrize("name", golden_names("svd_"))
 def test_sigma_matches_reference_within_its_accuracy(orc, name):
     g = golden(name)
