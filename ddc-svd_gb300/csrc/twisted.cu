@@ -250,6 +250,188 @@ __global__ void __launch_bounds__(32 * kTwWarps) twisted_kernel(TwParams p) {
   }
 }
 
+// ---- clusters of (numerically) equal singular values inside one block
+// The twisted solve of sigma_k is accurate to about eps * sigma_max / gap, so
+// values that coincide to working precision inside one unreduced block get
+// the same vector from it (the reference assumes distinct values,
+// Calculations-Parallel.c:43).  Runs of sigmas closer than kClusterRel *
+// sigma_max get their vectors from a shared subspace instead: distinct
+// starts (the twisted vector plus a fixed pseudo-random vector), three steps
+// of inverse iteration with the run's mid shift, and modified Gram-Schmidt
+// (against the singleton neighbours, then the earlier members) after each
+// step, as LAPACK's xSTEIN does for close eigenvalues.  Any orthonormal basis
+// of the cluster's right singular subspace is a valid set of vectors when the
+// values coincide; when they differ by less than the threshold the mixing
+// adds at most that difference to the residual.  Singletons are untouched.
+constexpr double kClusterRel = 1e-10;
+constexpr int kClThreads = 256;
+
+// deterministic value in [-1, 1) from (i, j): integer mixing (xorshift-multiply)
+__device__ __forceinline__ double cl_start(int i, int j) {
+  unsigned h = (unsigned)i * 0x9E3779B1u ^ ((unsigned)j * 0x85EBCA77u + 0x165667B1u);
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return (double)(h >> 8) * (2.0 / 16777216.0) - 1.0;
+}
+
+__device__ __forceinline__ double cl_block_max(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int q = 0; q < nw; q++) r = fmax(r, red[q]);
+  return r;
+}
+
+// slot k starts a run of at least two close values
+__device__ __forceinline__ bool cl_leader(const TwParams& p, int k) {
+  const int lo = p.L.blo[k], hi = p.L.bhi[k];
+  if (hi - lo < 2 || k + 1 >= hi) return false;
+  const double* sg = p.sigma;  // ascending within the block
+  const double smax = fabs(sg[hi - 1]);
+  const double tol = kClusterRel * smax;
+  return smax > 0.0 && (k == lo || sg[k] - sg[k - 1] > tol) && sg[k + 1] - sg[k] <= tol;
+}
+
+__device__ void cl_refine(const TwParams& p, int k0, double* red);
+
+// each thread tests one slot; the CTA then refines the runs that start in
+// its chunk (runs are independent, so their order does not matter)
+__global__ void __launch_bounds__(kClThreads) tw_cluster_kernel(TwParams p) {
+  __shared__ double red[kClThreads / 32];
+  __shared__ int s_list[kClThreads];
+  __shared__ int s_cnt;
+  const int N = p.N, t = threadIdx.x, nt = blockDim.x;
+  for (int c0 = blockIdx.x * nt; c0 < N; c0 += gridDim.x * nt) {
+    if (t == 0) s_cnt = 0;
+    __syncthreads();
+    if (c0 + t < N && cl_leader(p, c0 + t)) s_list[atomicAdd(&s_cnt, 1)] = c0 + t;
+    __syncthreads();
+    const int cnt = s_cnt;
+    for (int q = 0; q < cnt; q++) cl_refine(p, s_list[q], red);
+    __syncthreads();
+  }
+}
+
+__device__ void cl_refine(const TwParams& p, int k0, double* red) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  {
+    const int lo = p.L.blo[k0], hi = p.L.bhi[k0], nb = hi - lo;
+    const double* sg = p.sigma;
+    const double smax = fabs(sg[hi - 1]);
+    const double tol = kClusterRel * smax;
+    int c = 2;
+    while (k0 + c < hi && sg[k0 + c] - sg[k0 + c - 1] <= tol) c++;
+    const long long base = p.L.base[lo];
+    const long long zc = base + (k0 - lo);  // Z column of member 0, element i at zc + j + (i - lo) * nb
+    // contiguous work rows (free after the twisted solve; clusters own disjoint rows)
+    double* W = p.Um + base + (long long)(k0 - lo) * nb;  // member j, element i at W[j * nb + i - lo]
+    double* Lf = p.Pp + base + (long long)(k0 - lo) * nb;
+    double* Df = Lf + nb;
+    // neighbours that are singletons (their vectors are accurate and final)
+    const int kl = (k0 > lo && (k0 - 1 == lo || sg[k0 - 1] - sg[k0 - 2] > tol)) ? k0 - 1 : -1;
+    const int kr = (k0 + c < hi && (k0 + c + 1 == hi || sg[k0 + c + 1] - sg[k0 + c] > tol)) ? k0 + c : -1;
+    // L+ D+ L+^T = (B^T B - lam I) / smax^2 by the stationary qd transform,
+    // pivots kept at least 4 eps away from zero
+    if (t == 0) {
+      const double is = 1.0 / smax;
+      const double sm = 0.5 * (sg[k0] + sg[k0 + c - 1]) * is;
+      const double lam = sm * sm, fl = 4.0 * DBL_EPSILON;
+      double s = -lam;
+      for (int i = lo; i < hi; i++) {
+        double dp = p.dd[i] * is * is + s;
+        if (fabs(dp) < fl) dp = (dp < 0.0) ? -fl : fl;
+        Df[i - lo] = dp;
+        if (i + 1 < hi) {
+          const double L = p.dl[i] * is * is / dp;
+          Lf[i - lo] = L;
+          s = L * p.ll[i] * s - lam;
+        }
+      }
+    }
+    const double rs = rsqrt((double)nb);
+    for (int q = t; q < c * nb; q += nt) {
+      const int j = q / nb, i = lo + q % nb;
+      W[q] = p.Z[zc + j + (long long)(i - lo) * nb] * p.xinv[k0 + j] + cl_start(i, j) * rs;
+    }
+    __syncthreads();
+    for (int it = 0; it < 3; it++) {
+      // inverse iteration: W_j <- (L+ D+ L+^T)^{-1} W_j, one thread per member
+      for (int j = t; j < c; j += nt) {
+        double* w = W + (long long)j * nb;
+        double u = 0.0;
+        for (int i = 0; i < nb; i++) {
+          u = w[i] - (i > 0 ? Lf[i - 1] * u : 0.0);
+          w[i] = u;
+        }
+        double z = 0.0;
+        for (int i = nb - 1; i >= 0; i--) {
+          z = w[i] / Df[i] - (i + 1 < nb ? Lf[i] * z : 0.0);
+          w[i] = z;
+        }
+      }
+      __syncthreads();
+      // modified Gram-Schmidt, members in order; every thread keeps the same
+      // elements i throughout, so the updates need no barrier of their own
+      for (int j = 0; j < c; j++) {
+        double* w = W + (long long)j * nb;
+        double mx = 0.0;
+        for (int i = t; i < nb; i += nt) mx = fmax(mx, fabs(w[i]));
+        mx = cl_block_max(mx, red);
+        if (mx > 0.0 && mx < INFINITY) {
+          const double sc = 1.0 / mx;
+          for (int i = t; i < nb; i += nt) w[i] *= sc;
+        }
+        for (int side = 0; side < 2; side++) {
+          const int kn = side ? kr : kl;
+          if (kn < 0) continue;
+          const long long zn = base + (kn - lo);
+          const double xn = p.xinv[kn];
+          double d = 0.0;
+          for (int i = t; i < nb; i += nt) d += w[i] * p.Z[zn + (long long)i * nb] * xn;
+          d = block_sum(d, red);
+          for (int i = t; i < nb; i += nt) w[i] -= d * p.Z[zn + (long long)i * nb] * xn;
+        }
+        for (int l = 0; l < j; l++) {
+          const double* v = W + (long long)l * nb;
+          double d = 0.0;
+          for (int i = t; i < nb; i += nt) d += w[i] * v[i];
+          d = block_sum(d, red);
+          for (int i = t; i < nb; i += nt) w[i] -= d * v[i];
+        }
+        double n2 = 0.0;
+        for (int i = t; i < nb; i += nt) n2 += w[i] * w[i];
+        n2 = block_sum(n2, red);
+        const double inv = (n2 > 0.0) ? 1.0 / sqrt(n2) : 0.0;
+        for (int i = t; i < nb; i += nt) w[i] *= inv;
+      }
+      __syncthreads();
+    }
+    // back into the compact layout; unit norm, and 1 / ||B x|| for the left vector
+    for (int j = 0; j < c; j++) {
+      const double* w = W + (long long)j * nb;
+      double by = 0.0;
+      for (int i = t; i < nb; i += nt) {
+        const double y = p.a[lo + i] * w[i] + (i + 1 < nb ? p.b[lo + i] * w[i + 1] : 0.0);
+        by += y * y;
+        p.Z[zc + j + (long long)i * nb] = w[i];
+      }
+      by = block_sum(by, red);
+      if (t == 0) {
+        p.xinv[k0 + j] = 1.0;
+        p.yinv[k0 + j] = (by > 0.0) ? 1.0 / sqrt(by) : 0.0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // rank of sigma_k among the sigmas of its group (ascending, stable).
 __global__ void tw_rank_kernel(int N, const double* __restrict__ sigma, VecLayout L, int* rank,
                                double* sorted) {
@@ -374,6 +556,8 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
   tw_setup_kernel<<<sg, 256, 0, ctx->stream>>>(N, a, b, amax, dd, ll, dl, dll);
   count_launch(2);
   twisted_kernel<<<ceil_div(N, 32), 32 * kTwWarps, 0, ctx->stream>>>(p);
+  count_launch();
+  tw_cluster_kernel<<<std::min(ceil_div(N, kClThreads), 2 * ctx->num_sms), kClThreads, 0, ctx->stream>>>(p);
   count_launch();
   tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, p.L, rank, sigma_sorted);
   count_launch();

@@ -467,6 +467,45 @@ def test_vector_stage_vs_oracle(lib, cuda, orc, N, kind):
         assert abs(abs(X[:, j] @ Xo[:, j]) - 1) <= 1e-6
 
 
+def _clustered_bidiagonal(kind):
+    """Unreduced bidiagonals (every superdiagonal entry 1, nothing splits) whose
+    singular values coincide to working precision: large diagonal entries at
+    both ends give pairs, three peaks give triples."""
+    if kind in ("pairs41", "pairs201"):
+        h = 20 if kind == "pairs41" else 100
+        a = np.abs(np.arange(2 * h + 1) - h) + 1.0
+    else:
+        P = 24
+        a = np.abs((np.arange(3 * P + 1) % P) - P / 2) + 1.0
+    return a, np.ones(len(a) - 1)
+
+
+@pytest.mark.parametrize("kind", ["pairs41", "pairs201", "triples73"])
+def test_vector_stage_clusters(lib, cuda, orc, kind):
+    """Singular values equal to working precision inside one unreduced block:
+    the twisted solve alone returns the same vector for equal values (the FP64
+    oracle, which follows the reference's method, is far from orthogonal
+    here); the cluster step must give orthonormal X and Y with B X = Y S."""
+    a, b = _clustered_bidiagonal(kind)
+    N = len(a)
+    B = np.diag(a) + np.diag(b, 1)
+    st = np.sort(np.linalg.svd(B, compute_uv=False))
+    assert np.sum(np.diff(st) <= 1e-10 * st.max()) >= 10  # the case really has clusters
+    _, Xo, _ = orc.bdsvd(a, b)
+    assert np.linalg.norm(Xo.T @ Xo - np.eye(N)) / np.sqrt(N) > 1e-2  # and the plain method fails on it
+    T = cuda
+    b2 = np.r_[b, 0.0]
+    s = lib.bdsdc_sigma_device(T.from_numpy(a).cuda(), T.from_numpy(b2).cuda())
+    X, Y = lib.bdvec_device(T.from_numpy(a).cuda(), T.from_numpy(b2).cuda(), s)
+    s = s.cpu().numpy()
+    X = X.double().cpu().numpy()
+    Y = Y.double().cpu().numpy()
+    assert np.max(np.abs(s - st)) <= 1e-12 * st.max()
+    assert np.linalg.norm(X.T @ X - np.eye(N)) / np.sqrt(N) <= 1e-6
+    assert np.linalg.norm(Y.T @ Y - np.eye(N)) / np.sqrt(N) <= 1e-6
+    assert np.linalg.norm(B @ X - Y * s) <= 1e-6 * np.linalg.norm(B) * np.sqrt(N)
+
+
 # ------------------------------------------------------------------ drop-ins vs the reference
 @pytest.mark.parametrize("name", golden_names("svd_"))
 def test_svd_gpu_dropin_vs_reference(lib, cuda, orc, name):
