@@ -133,7 +133,10 @@ int ddcsvd_bdsdc_sigma_device(ddcsvd_handle_t handle, int N, const double *dB1, 
 /* Stages 3-4 alone (parallel-twisted.c:554 CalcRightSingularVectors and :530
  * RighttoLeftSingularVectors): right (dX) and left (dY) singular vectors of
  * the N x N upper bidiagonal (dA diagonal N, dB superdiagonal N-1) for the
- * given ascending dSigma.  dX, dY: N x N column-major FP32, ld = N. */
+ * given ascending dSigma.  dX, dY: N x N column-major FP32, ld = N.  Values
+ * that coincide to working precision inside one unreduced block (which the
+ * reference's method maps to one repeated vector) get an orthonormal basis of
+ * their common subspace. */
 int ddcsvd_bdvec_device(ddcsvd_handle_t handle, int N, const double *dA, const double *dB,
                         const double *dSigma, float *dX, float *dY);
 
