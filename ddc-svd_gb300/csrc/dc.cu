@@ -423,6 +423,35 @@ __device__ __forceinline__ bool sec_step(bool last, T f, T psi, T dpsi, T phi, T
 __device__ unsigned g_dc_iters[64 * 84];  // [depth][FP64 iterations 0..80, 81: FP32 phase gave up early]
 #endif
 
+// f at the midpoint of (d_i, d_i+1) on the FP32 copies, with a bound on its
+// error: the copies carry relative error eps32, so the difference
+// del_j = (d_j - d_o)(d_j + d_o) - tau is off by about
+// 3 eps32 ((|d_j| + |d_o|)^2 + |tau|); term j is off by its size times that
+// over |del_j| (plus a few roundings), and the sum by q eps32 of the total.
+// A term whose del_j may change sign, or lies near the FP32 subnormal range
+// (where the copies lose relative precision), makes the bound infinite.
+__device__ __forceinline__ void sec_mid32(int q, const float* d, const float* z, float dorg, float tau,
+                                          const LaneGroup& g, float& f, float& err) {
+  constexpr float e32 = FLT_EPSILON;
+  float s = 0.f, sa = 0.f, ea = 0.f;
+  for (int j = g.lg; j < q; j += g.G) {
+    const float dj = d[j];
+    const float del = (dj - dorg) * (dj + dorg) - tau;
+    const float tt = z[j] * z[j] / del;
+    const float ad = fabsf(dj) + fabsf(dorg);
+    const float ed = 3.f * e32 * (ad * ad + fabsf(tau));
+    const float at = fabsf(tt);
+    s += tt;
+    sa += at;
+    ea += (ed < 0.5f * fabsf(del) && fabsf(del) >= 0x1p-100f) ? at * (2.f * ed / fabsf(del) + 4.f * e32) : INFINITY;
+  }
+  s = gsum(s, g);
+  sa = gsum(sa, g);
+  ea = gsum(ea, g);
+  f = 1.f + s;
+  err = ea + (float)(q + 2) * e32 * (1.f + sa);
+}
+
 __device__ bool sec_root(int q, const double* d, const double* z, const float* df, const float* zf, double zz,
                          int i, const LaneGroup& g, int* origin, double* tau_out, int* iters = nullptr) {
   double f, psi, dpsi, phi, dphi;
@@ -431,11 +460,18 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
   double lo, hi, tau, da0 = 0.0, db0 = 0.0;
   if (!last) {
     const double dd = (d[i + 1] - d[i]) * (d[i + 1] + d[i]);
-    // origin = nearer pole, from the sign of f at the midpoint (FP64: an FP32
-    // sign taken at an FP32-rounded midpoint picked the wrong half on close
-    // poles of a batch forest)
-    sec_eval(q, d, z, d[i], 0.5 * dd, i, g, f, psi, dpsi, phi, dphi);
-    o = (f >= 0.0) ? i : i + 1;
+    // origin = nearer pole, from the sign of f at the midpoint: from the FP32
+    // copies when f clears twice its error bound, else in FP64 (an FP32 sign
+    // taken without the bound picked the wrong half on close poles of a
+    // batch forest, and the root then lies outside the bracket)
+    float f32, e32;
+    sec_mid32(q, df, zf, df[i], (float)(0.5 * dd), g, f32, e32);
+    if (fabsf(f32) > 2.f * e32 && fabsf(f32) < INFINITY) {
+      o = (f32 >= 0.f) ? i : i + 1;
+    } else {
+      sec_eval(q, d, z, d[i], 0.5 * dd, i, g, f, psi, dpsi, phi, dphi);
+      o = (f >= 0.0) ? i : i + 1;
+    }
     const double dorg = d[o];
     if (o == i) { lo = 0.0; hi = 0.5 * dd; tau = 0.5 * dd; }
     else { lo = -0.5 * dd; hi = 0.0; tau = -0.5 * dd; }
