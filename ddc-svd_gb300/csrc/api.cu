@@ -696,6 +696,42 @@ static int bd_standalone(ddcsvd_context* h, int N, const double* dB1, const doub
   return check_status(h, dX ? "bdvec" : "bdsdc");
 }
 
+// ---- host-only planning of stage 2 (no device work): what the pipeline does
+// between the bidiagonal read-back and the D&C launch, for tests and tools
+int ddcsvd_split_plan(int N, double* a, double* b, double eps, int* starts, int* nstarts) {
+  t_last_error.clear();
+  if (N <= 0 || !a || !b || !starts || !nstarts || !(eps >= 0.0)) return DDCSVD_ERR_ARG;
+  std::vector<int> st, lo(N), hi(N);
+  split_bidiagonal(N, a, b, eps, st, lo.data(), hi.data());
+  for (size_t i = 0; i < st.size(); i++) starts[i] = st[i];
+  *nstarts = (int)st.size();
+  return DDCSVD_OK;
+}
+
+int ddcsvd_dc_plan(int N, int nstarts, const int* starts, int terms_per_lane, int* out, long long cap, int* meta) {
+  t_last_error.clear();
+  if (N <= 0 || nstarts < 2 || !starts || !meta || cap < 0 || (cap > 0 && !out)) return DDCSVD_ERR_ARG;
+  if (starts[0] != 0 || starts[nstarts - 1] != N) return DDCSVD_ERR_ARG;
+  for (int i = 0; i + 1 < nstarts; i++)
+    if (starts[i + 1] < starts[i]) return DDCSVD_ERR_ARG;
+  DcHost H;
+  dc_build_host(N, std::vector<int>(starts, starts + nstarts), H, terms_per_lane);
+  meta[0] = H.nnodes;
+  meta[1] = H.maxdepth;
+  meta[2] = H.ndm;
+  meta[3] = H.ntrees;
+  meta[4] = H.nseg;
+  meta[5] = H.maxtree;
+  meta[6] = (int)H.tree_off;
+  meta[7] = (int)H.ints.size();
+  if ((long long)H.ints.size() > cap) {
+    set_last_error("node table needs %zu ints", H.ints.size());
+    return DDCSVD_ERR_ARG;
+  }
+  for (size_t i = 0; i < H.ints.size(); i++) out[i] = H.ints[i];
+  return DDCSVD_OK;
+}
+
 int ddcsvd_bdsdc_sigma_device(ddcsvd_handle_t h, int N, const double* dB1, const double* dB2, double* dSigma) {
   if (!h || N <= 0 || !dB1 || !dB2 || !dSigma) return DDCSVD_ERR_ARG;
   std::lock_guard<std::mutex> g(h->mu);

@@ -35,6 +35,8 @@ _SIGS = {
     "ddcsvd_bidiag_f32_device": (c_int, [P, c_int, c_int, P, c_int, P, P, P, P, c_int]),
     "ddcsvd_bdsdc_sigma_device": (c_int, [P, c_int, P, P, P]),
     "ddcsvd_bdvec_device": (c_int, [P, c_int, P, P, P, P, P]),
+    "ddcsvd_split_plan": (c_int, [c_int, P, P, ctypes.c_double, P, P]),
+    "ddcsvd_dc_plan": (c_int, [c_int, c_int, P, c_int, P, ctypes.c_longlong, P]),
     "ddcsvd_svd_batched_f32_device": (c_int, [P, c_int, P, P, P, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f64_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),
     "ddcsvd_svd_backward_f32_device": (c_int, [P, c_int, c_int, c_int, P, P, P, P, P, P, P]),

@@ -140,6 +140,24 @@ int ddcsvd_bdsdc_sigma_device(ddcsvd_handle_t handle, int N, const double *dB1, 
 int ddcsvd_bdvec_device(ddcsvd_handle_t handle, int N, const double *dA, const double *dB,
                         const double *dSigma, float *dX, float *dY);
 
+/* Host-only planning of stage 2 (no GPU work; for tests and tools).
+ * ddcsvd_split_plan: splits the N x N bidiagonal a (N), b (N) at
+ * |b_i| <= 4 eps max|entry| as the pipeline does (b_i set to 0 there, b[N-1]
+ * too) and writes the block starts (ascending, first 0, last N; at most N+1)
+ * to starts, their count to nstarts.
+ * ddcsvd_dc_plan: the D&C forest the pipeline builds for those blocks
+ * (Calculations-Parallel.c:706-850: node N splits at K = N/2 into K and
+ * N-K-1, leaves N <= 2) and its schedule, as the packed int table uploaded
+ * to the GPU: per node r0, n, slot, K, child1, child2 (nodes ordered by
+ * depth), depth starts, merge starts, merge list, lanes per root by depth,
+ * then per tree: tree segment starts, segment node starts, segment merge
+ * ends, segment depths, segment lanes, nodes, trees by size.  meta[8] =
+ * {nodes, max depth, merges, trees, segments, largest tree, offset of the
+ * per-tree part, table length}; DDCSVD_ERR_ARG when cap is too small (meta
+ * is filled either way). */
+int ddcsvd_split_plan(int N, double *a, double *b, double eps, int *starts, int *nstarts);
+int ddcsvd_dc_plan(int N, int nstarts, const int *starts, int terms_per_lane, int *out, long long cap, int *meta);
+
 /* ---------------------------------------------------------------- batched */
 
 /* Many independent SVDs of uneven sizes in one launch sequence (device
