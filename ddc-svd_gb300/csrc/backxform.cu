@@ -5,10 +5,11 @@
 // wrong leading dimension for m != n; here the right reflectors are read with
 // their true layout.
 //
-// Blocked (BLOCKED modes): kWY consecutive reflectors are aggregated into
-// I - U T U^T (compact WY, T upper triangular) and applied with three GEMMs
-// per block, last block first:  W1 = U^T C,  W2 = T W1,  C -= U W2.
-// The GEMMs run on the back end of the mode (FP32 CUDA cores or tcgen05).
+// Blocked (BLOCKED modes): consecutive reflectors (kWY = 64 on the FP32 CUDA
+// cores, kWYT = 128 on tcgen05) are aggregated into I - U T U^T (compact WY,
+// T upper triangular) and applied per block, last block first:
+// W1 = U^T C, then C -= U (T W1) -- on tcgen05 as two products with U T
+// formed once per block.
 //
 // Plain (PLAIN_FP32): the reference's per-vector scheme -- every column of C
 // is transformed by the reflectors one at a time (a dot product and an axpy

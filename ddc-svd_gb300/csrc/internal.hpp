@@ -183,7 +183,7 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
                const double* sigma, const VecLayout* L, double* sigma_sorted, Arena& arena, bool plan_only);
 
 // ---------------------------------------------------------------- stage 5
-constexpr int kWY = 64;  // reflectors per WY block in the back-transformation
+constexpr int kWY = 64;  // reflectors per WY block of the FP32 (SIMT) back-transformation; tcgen05 blocks take 128
 // C (rows x ncols, ldc) := Q C with Q = H_0 ... H_{nref-1} (left reflectors in W columns).
 int apply_left_reflectors(ddcsvd_context* ctx, int m, int nref, const float* W, int ldw,
                           const float* tauq, float* C, int ldc, int ncols, GemmKind kind,
