@@ -114,8 +114,8 @@ __host__ __device__ inline long long ut_offset(int b, int rows_total) {
 //   wy_ut_kernel       grid (block, row chunk): UT = U T (row-major, ld NB)
 // so that applying the block is C -= UT (U^T C) (or, with T^T, the
 // transposed block of a QR factorisation).  A single CTA per block had cost
-// 1.3 ms for an 8192-row block.  NB = 64 (QR path) or 128 (back-transformation:
-// half the passes over C of 64-reflector blocks).
+// 1.3 ms for an 8192-row block.  NB = 32 (QR panels) or 128 (QR super-blocks
+// and the back-transformation: half the passes over C of 64-reflector blocks).
 constexpr int kPrepRows = 32;    // rows per shared-memory tile
 constexpr int kChunkRows = 512;  // rows per CTA of the chunked kernels (many blocks)
 constexpr int kChunkRowsFew = 128;  // the same when a call has at most two blocks (QR panels / super-blocks)
