@@ -356,8 +356,8 @@ __device__ void cl_refine(const TwParams& p, int k0, double* red) {
       }
     }
     const double rs = rsqrt((double)nb);
-    for (int q = t; q < c * nb; q += nt) {
-      const int j = q / nb, i = lo + q % nb;
+    for (long long q = t; q < (long long)c * nb; q += nt) {  // c * nb may pass 2^31 on huge blocks
+      const int j = (int)(q / nb), i = lo + (int)(q % nb);
       W[q] = p.Z[zc + j + (long long)(i - lo) * nb] * p.xinv[k0 + j] + cl_start(i, j) * rs;
     }
     __syncthreads();
