@@ -183,3 +183,18 @@ def test_split_plan_feeds_dc_plan(lib):
     b[rng.choice(N - 1, 25, replace=False)] = 0.0
     _, _, st = split_plan(L, a, b, EPS32)
     check_plan(dc_plan(L, N, st), N, st)
+
+
+@pytest.mark.parametrize("eps", [EPS64, EPS32])
+def test_split_plan_matches_oracle(lib, orc, eps):
+    """The library's host split and the oracle's (oracle/ddcsvd_oracle.c,
+    orc_bdsvd) zero exactly the same superdiagonal entries."""
+    L = lib.load()
+    rng = np.random.default_rng(int(eps * 1e20) % 1000)
+    for trial in range(20):
+        N = int(rng.integers(2, 400))
+        a = rng.uniform(-2, 2, N) * 10.0 ** rng.uniform(-8, 0, N)
+        b = rng.uniform(-2, 2, N) * 10.0 ** rng.uniform(-20, 0, N)
+        _, b_lib, _ = split_plan(L, a, b, eps)
+        _, _, b_orc = orc.bdsvd(a, b[: N - 1], eps)
+        assert np.array_equal(b_lib[: N - 1] == 0.0, b_orc == 0.0), trial
