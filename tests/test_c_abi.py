@@ -1,0 +1,38 @@
+"""CPU test of the boundary from C: tests/c/abi_check.c is compiled by a
+plain C compiler against include/ddcsvd.h (which checks the drop-ins'
+signatures against the reference's), linked to the built library and run.
+Without a GPU the drop-in must report failure (NaN singular values) rather
+than compute on the CPU; with one it must return the singular values."""
+import math
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_c_caller_compiles_links_and_runs(lib, tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    from ddcsvd import build as b
+    libdir = os.path.dirname(b.LIB_PATH)
+    exe = str(tmp_path / "abi_check")
+    cmd = [cc, "-std=c99", "-Wall", "-Werror", "-I", b.INCLUDE, os.path.join(HERE, "c", "abi_check.c"),
+           "-o", exe, f"-L{libdir}", f"-Wl,-rpath,{libdir}", "-lddcsvd"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = dict(l.split(" ", 1) for l in r.stdout.strip().splitlines())
+    s = [float(x) for x in lines["sigma"].split()]
+    import torch
+    if torch.cuda.is_available():
+        assert abs(s[0] - 2.0) < 1e-5 and abs(s[1] - 3.0) < 1e-5
+    else:
+        assert all(math.isnan(x) for x in s)
+        assert "svd_gpu:" in r.stderr  # one line says why
+    assert lines["split"].split() == ["0", "4", "0", "2", "3", "6"]
+    assert lines["plan"].split()[:1] == ["0"] and lines["plan"].split()[4] == "3"
+    assert lines["status"] == "ok"
