@@ -12,6 +12,9 @@
 // Four kernels per call: a batched tiled GEMM for J and K, an elementwise
 // kernel for M, the batched GEMM for U M (+ gU S^-1 as its C input) and for
 // (U M + gU S^-1) V^T.
+#include <cudaTypedefs.h>
+
+#include "ctx_cache.hpp"
 #include "internal.hpp"
 
 namespace ddcsvd {
@@ -105,6 +108,44 @@ static int bgemm(ddcsvd_context* ctx, int batch, int M, int N, int K, const T* A
   return DDCSVD_OK;
 }
 
+// The four launches of one adjoint on intermediates J, Kv, Mm (k x k per
+// problem) and P (m x k per problem).  Launch grids carry the batch in
+// gridDim.z / gridDim.y (at most 65535), so larger batches go in chunks.
+constexpr int kBatchChunk = 65535;
+
+template <typename T>
+static int adjoint_enqueue(ddcsvd_context* h, int batch, int m, int n, const T* U, const T* S, const T* V,
+                           const T* gU, const T* gS, const T* gV, T* gA, T* J, T* Kv, T* Mm, T* P) {
+  const int k = n;
+  const long long sU = (long long)m * k, sV = (long long)n * k, sK = (long long)k * k, sA = (long long)m * n;
+  for (int b0 = 0; b0 < batch; b0 += kBatchChunk) {
+    const int nb = std::min(kBatchChunk, batch - b0);
+    const T* Ub = U + b0 * sU;
+    const T* Vb = V + b0 * sV;
+    const T* Sb = S + b0 * (long long)k;
+    const T* gUb = gU ? gU + b0 * sU : nullptr;
+    const T* gVb = gV ? gV + b0 * sV : nullptr;
+    const T* gSb = gS ? gS + b0 * (long long)k : nullptr;
+    T* Jb = J + b0 * sK;
+    T* Kb = Kv + b0 * sK;
+    T* Mb = Mm + b0 * sK;
+    T* Pb = P + b0 * sU;
+    // J = U^T gU, K = V^T gV
+    if (gUb) DDC_TRY(bgemm<T>(h, nb, k, k, m, Ub, m, 1, sU, gUb, 1, m, sU, Jb, k, sK, T(1), T(0)));
+    if (gVb) DDC_TRY(bgemm<T>(h, nb, k, k, n, Vb, n, 1, sV, gVb, 1, n, sV, Kb, k, sK, T(1), T(0)));
+    dim3 g2(std::max(1, std::min(64, ceil_div(std::max(k * k, m * k), 256))), nb);
+    adjoint_core_kernel<T><<<g2, 256, 0, h->stream>>>(k, m, gUb ? Jb : nullptr, gVb ? Kb : nullptr, Sb, gSb, gUb,
+                                                      Mb, Pb);
+    count_launch();
+    DDC_CUDA_TRY(cudaGetLastError());
+    // P += U M
+    DDC_TRY(bgemm<T>(h, nb, m, k, k, Ub, 1, m, sU, Mb, 1, k, sK, Pb, m, sU, T(1), T(1)));
+    // gA = P V^T
+    DDC_TRY(bgemm<T>(h, nb, m, n, k, Pb, 1, m, sU, Vb, n, 1, sV, gA + b0 * sA, m, sA, T(1), T(0)));
+  }
+  return DDCSVD_OK;
+}
+
 template <typename T>
 static int svd_backward(ddcsvd_context* h, int batch, int m, int n, const T* U, const T* S, const T* V, const T* gU,
                         const T* gS, const T* gV, T* gA) {
@@ -127,17 +168,7 @@ static int svd_backward(ddcsvd_context* h, int batch, int m, int n, const T* U, 
   T* Mm = a.take<T>(kk);
   T* P = a.take<T>(mk);
   DDC_TRY(reset_status(h));
-  const long long sU = (long long)m * k, sV = (long long)n * k, sK = (long long)k * k;
-  // J = U^T gU, K = V^T gV
-  if (gU) DDC_TRY(bgemm<T>(h, batch, k, k, m, U, m, 1, sU, gU, 1, m, sU, J, k, sK, T(1), T(0)));
-  if (gV) DDC_TRY(bgemm<T>(h, batch, k, k, n, V, n, 1, sV, gV, 1, n, sV, Kv, k, sK, T(1), T(0)));
-  dim3 g2(std::max(1, std::min(64, ceil_div(std::max(k * k, m * k), 256))), batch);
-  adjoint_core_kernel<T><<<g2, 256, 0, h->stream>>>(k, m, gU ? J : nullptr, gV ? Kv : nullptr, S, gS, gU, Mm, P);
-  count_launch();
-  // P += U M
-  DDC_TRY(bgemm<T>(h, batch, m, k, k, U, 1, m, sU, Mm, 1, k, sK, P, m, sU, T(1), T(1)));
-  // gA = P V^T
-  DDC_TRY(bgemm<T>(h, batch, m, n, k, P, 1, m, sU, V, n, 1, sV, gA, m, (long long)m * n, T(1), T(0)));
+  DDC_TRY(adjoint_enqueue<T>(h, batch, m, n, U, S, V, gU, gS, gV, gA, J, Kv, Mm, P));
   return check_status(h, "svd_backward");
 }
 
@@ -152,54 +183,93 @@ static int svd_backward(ddcsvd_context* h, int batch, int m, int n, const T* U, 
 // workspace; it needs no handle either.
 constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB, held by every GPU that loads the library
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[128];  // device address of g_noalloc_scratch, per device
 
-// The array's host-side name is only a stand-in: its device address is looked
-// up once per device, with that device current.
-static int noalloc_scratch_address(int dev, char** out) {
-  if (dev < 0 || dev >= 128) return DDCSVD_ERR_ARG;
-  std::lock_guard<std::mutex> g(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+// The array's host-side name is only a stand-in: its device address is
+// looked up (cudaGetSymbolAddress, with the caller's context current) the
+// first time a context calls, and kept per context id.
+using CtxGetCurrentFn = PFN_cuCtxGetCurrent_v4000;
+using CtxGetIdFn = PFN_cuCtxGetId_v12000;
+static CtxValueCache<64> g_noalloc_addr;
+
+static int driver_fn(const char* name, void** fn) {
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !*fn) {
+    cudaGetLastError();
+    set_last_error("driver entry point %s unavailable", name);
+    return DDCSVD_ERR_CUDA;
+  }
+  return DDCSVD_OK;
+}
+
+static int lookup_scratch(void** p) {
+  const cudaError_t e = cudaGetSymbolAddress(p, g_noalloc_scratch);
+  if (e != cudaSuccess || !*p) {
+    cudaGetLastError();
+    set_last_error("cudaGetSymbolAddress of the adjoint scratch failed: %s", cudaGetErrorString(e));
+    return DDCSVD_ERR_CUDA;
+  }
+  return DDCSVD_OK;
+}
+
+static int noalloc_scratch_address(char** out) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current) DDC_TRY(driver_fn("cuCtxGetCurrent", reinterpret_cast<void**>(&get_current)));
+  if (!get_id) DDC_TRY(driver_fn("cuCtxGetId", reinterpret_cast<void**>(&get_id)));
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS) {
+    set_last_error("cuCtxGetCurrent failed");
+    return DDCSVD_ERR_CUDA;
+  }
+  if (!c) {
+    // no context current on this thread yet: the runtime's lookup makes the
+    // current device's primary context current
     void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_last_error("cudaGetSymbolAddress of the adjoint scratch failed: %s", cudaGetErrorString(e));
+    DDC_TRY(lookup_scratch(&p));
+    if (get_current(&c) != CUDA_SUCCESS || !c) {
+      set_last_error("no CUDA context is current");
       return DDCSVD_ERR_CUDA;
     }
-    g_noalloc_addr[dev] = p;
   }
-  *out = static_cast<char*>(g_noalloc_addr[dev]);
+  unsigned long long id = 0;
+  if (get_id(c, &id) != CUDA_SUCCESS) {
+    set_last_error("cuCtxGetId failed");
+    return DDCSVD_ERR_CUDA;
+  }
+  void* p = nullptr;
+  DDC_TRY(g_noalloc_addr.get(id, &p, lookup_scratch));
+  *out = static_cast<char*>(p);
   return DDCSVD_OK;
+}
+
+// Bytes of scratch one call takes: J, K and M (k x k per problem) and
+// P (m x k per problem), each region rounded up to 256 bytes.
+static size_t noalloc_bytes(int batch, int m, int n) {
+  const size_t kk = 8 * (size_t)n * n * batch, mk = 8 * (size_t)m * n * batch;
+  return 3 * (size_t)round_up((long long)kk, 256) + (size_t)round_up((long long)mk, 256);
 }
 
 static int svd_backward_f64_noalloc(cudaStream_t stream, int batch, int m, int n, const double* U, const double* S,
                                     const double* V, const double* gU, const double* gS, const double* gV,
                                     double* gA) {
   if (batch <= 0 || m <= 0 || n <= 0 || m < n || !U || !S || !V || !gA) return DDCSVD_ERR_ARG;
-  const int k = n;
-  // scratch layout: status word, J, K, M (k x k each), P (m x k), per problem
-  const size_t kk = (size_t)k * k * batch, mk = (size_t)m * k * batch;
-  Arena plan;
-  plan.take<DevStatus>(1);
-  plan.take<double>(kk);
-  plan.take<double>(kk);
-  plan.take<double>(kk);
-  plan.take<double>(mk);
-  if (plan.off > kNoAllocScratchBytes) {
+  const size_t need = noalloc_bytes(batch, m, n);
+  if (need > kNoAllocScratchBytes) {
     set_last_error("allocation-free adjoint needs %zu bytes of scratch; its fixed limit is %zu bytes "
-                   "(batch * (3 n^2 + m n) * 8 plus 256): split the batch",
-                   plan.off, kNoAllocScratchBytes);
+                   "(3 r(8 batch n^2) + r(8 batch m n), r = round up to 256): split the batch",
+                   need, kNoAllocScratchBytes);
     return DDCSVD_ERR_ARG;
   }
+  char* base = nullptr;
+  DDC_TRY(noalloc_scratch_address(&base));
   int dev = 0;
   DDC_CUDA_TRY(cudaGetDevice(&dev));
-  char* base = nullptr;
-  DDC_TRY(noalloc_scratch_address(dev, &base));
+  const int k = n;
+  const size_t kk = (size_t)k * k * batch, mk = (size_t)m * k * batch;
   Arena a;
   a.plan = false;
   a.base = base;
-  DevStatus* st = a.take<DevStatus>(1);
   double* J = a.take<double>(kk);
   double* Kv = a.take<double>(kk);
   double* Mm = a.take<double>(kk);
@@ -207,28 +277,13 @@ static int svd_backward_f64_noalloc(cudaStream_t stream, int batch, int m, int n
   ddcsvd_context ctx;  // stream only: nothing here allocates
   ctx.device = dev;
   ctx.stream = stream;
-  ctx.d_status = st;
-  // the array keeps the previous call's contents: the status word must start at zero
-  // (J, K, M and P are fully overwritten before they are read)
-  DDC_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevStatus), stream));
-  const long long sU = (long long)m * k, sV = (long long)n * k, sK = (long long)k * k;
-  if (gU) DDC_TRY(bgemm<double>(&ctx, batch, k, k, m, U, m, 1, sU, gU, 1, m, sU, J, k, sK, 1.0, 0.0));
-  if (gV) DDC_TRY(bgemm<double>(&ctx, batch, k, k, n, V, n, 1, sV, gV, 1, n, sV, Kv, k, sK, 1.0, 0.0));
-  dim3 g2(std::max(1, std::min(64, ceil_div(std::max(k * k, m * k), 256))), batch);
-  adjoint_core_kernel<double><<<g2, 256, 0, stream>>>(k, m, gU ? J : nullptr, gV ? Kv : nullptr, S, gS, gU, Mm, P);
-  count_launch();
-  DDC_TRY(bgemm<double>(&ctx, batch, m, k, k, U, 1, m, sU, Mm, 1, k, sK, P, m, sU, 1.0, 1.0));
-  DDC_TRY(bgemm<double>(&ctx, batch, m, n, k, P, 1, m, sU, V, n, 1, sV, gA, m, (long long)m * n, 1.0, 0.0));
-  DevStatus hs{0, 0};
-  DDC_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
-  DDC_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (hs.code != 0) {
-    set_last_error("svd_backward_noalloc: device status %d", hs.code);
-    return hs.code;
-  }
+  // The array keeps the previous call's contents; J, K, M and P are fully
+  // overwritten before they are read, so nothing needs clearing.  The call
+  // only enqueues: kernels of the same stream run in order, and a caller
+  // reads gA after synchronising the stream.
+  DDC_TRY(adjoint_enqueue<double>(&ctx, batch, m, n, U, S, V, gU, gS, gV, gA, J, Kv, Mm, P));
   return DDCSVD_OK;
 }
-
 }  // namespace ddcsvd
 
 using namespace ddcsvd;

@@ -65,6 +65,11 @@ void ktimer_collect(ddcsvd_context* ctx) {
 
 int ensure_workspace(ddcsvd_context* ctx, size_t bytes) {
   if (bytes <= ctx->ws_bytes) return DDCSVD_OK;
+  if (ctx->ws_cap && bytes > ctx->ws_cap) {
+    set_last_error("device workspace of %zu bytes exceeds the handle's workspace limit of %zu bytes", bytes,
+                   ctx->ws_cap);
+    return DDCSVD_ERR_ALLOC;
+  }
   if (ctx->ws) {
     DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->ws);
@@ -72,6 +77,7 @@ int ensure_workspace(ddcsvd_context* ctx, size_t bytes) {
     ctx->ws_bytes = 0;
   }
   size_t want = (size_t)round_up((long long)bytes, 1 << 21);
+  if (ctx->ws_cap) want = std::min(want, ctx->ws_cap);
   if (cudaMalloc(&ctx->ws, want) != cudaSuccess) {
     cudaGetLastError();
     set_last_error("device workspace of %zu bytes could not be allocated", want);
@@ -99,8 +105,16 @@ int ensure_pinned(ddcsvd_context* ctx, size_t bytes) {
   return DDCSVD_OK;
 }
 
+// Clears the error code and writes the handle's limits (kernel arguments, so
+// the host values may change right after the launch).
+__global__ void status_init_kernel(DevStatus* st, unsigned wait_us, unsigned extra) {
+  if (threadIdx.x == 0) *st = DevStatus{0, 0, wait_us, extra};
+}
+
 int reset_status(ddcsvd_context* ctx) {
-  DDC_CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, sizeof(DevStatus), ctx->stream));
+  status_init_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_status, ctx->wait_us, ctx->barrier_extra);
+  count_launch();
+  DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
 }
 
@@ -306,7 +320,9 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     DDC_CUDA_TRY(cudaMemcpyAsync(hd, pl.d, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (n > 1)
       DDC_CUDA_TRY(cudaMemcpyAsync(he, pl.e, sizeof(float) * (n - 1), cudaMemcpyDeviceToHost, ctx->stream));
-    DDC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    // the status word rides along: a stage-1 failure (non-finite input, a
+    // wait that ran out) ends the call here instead of feeding stages 2-5
+    DDC_TRY(check_status(ctx, "bidiagonalisation"));
     double* a64 = (double*)((char*)ctx->pinned + rb);
     double* b64 = a64 + n + 4;
     for (int i = 0; i < n; i++) {
@@ -569,6 +585,31 @@ int ddcsvd_release_workspace(ddcsvd_handle_t h) {
   if (h->ws) cudaFree(h->ws);
   h->ws = nullptr;
   h->ws_bytes = 0;
+  return DDCSVD_OK;
+}
+
+int ddcsvd_set_limits(ddcsvd_handle_t h, const long long* values, int count) {
+  if (!h || !values || count < 0) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  t_last_error.clear();
+  long long v[4] = {h->sec_maxit, (long long)h->wait_us, (long long)h->ws_cap, (long long)h->barrier_extra};
+  for (int k = 0; k < std::min(count, 4); k++) v[k] = values[k];
+  if (v[0] < 1 || v[0] > 80 || v[1] < 0 || v[1] > 4000000 || v[2] < 0 || v[3] < 0 || v[3] > 1024) {
+    set_last_error("limits out of range: iterations 1..80, wait 0..4000000 us, workspace >= 0, arrivals 0..1024");
+    return DDCSVD_ERR_ARG;
+  }
+  h->sec_maxit = (int)v[0];
+  h->wait_us = (unsigned)v[1];
+  h->ws_cap = (size_t)v[2];
+  h->barrier_extra = (unsigned)v[3];
+  return DDCSVD_OK;
+}
+
+int ddcsvd_get_limits(ddcsvd_handle_t h, long long* values, int count) {
+  if (!h || !values || count < 0) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  const long long v[4] = {h->sec_maxit, (long long)h->wait_us, (long long)h->ws_cap, (long long)h->barrier_extra};
+  for (int k = 0; k < std::min(count, 4); k++) values[k] = v[k];
   return DDCSVD_OK;
 }
 

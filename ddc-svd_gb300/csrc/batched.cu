@@ -535,6 +535,7 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   float* he = hd + Ntot + 8;
   DDC_CUDA_TRY(cudaMemcpyAsync(hd, d, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
   DDC_CUDA_TRY(cudaMemcpyAsync(he, e, sizeof(float) * Ntot, cudaMemcpyDeviceToHost, h->stream));
+  DDC_CUDA_TRY(cudaMemcpyAsync(h->h_status, h->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
   // while stage 1 runs: the D&C forest and vector layout for one block per
   // problem (a split inside a problem is rare; prep_build lays out anew then)
   Prep P;
@@ -550,6 +551,11 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
     DDC_TRY(prep_layout(h, gn, gout, starts0, pin + tb + rb + ab, blob, &P));
   }
   DDC_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (h->h_status->code != 0) {  // a stage-1 failure ends the call before stages 2-5
+    set_last_error("batched bidiagonalisation: device status %d (detail %d)", h->h_status->code,
+                   h->h_status->detail);
+    return h->h_status->code;
+  }
   double* a64 = (double*)(pin + tb + rb);
   double* b64 = a64 + Ntot + 8;
   for (int b = 0; b < batch; b++) {

@@ -24,10 +24,16 @@ namespace ddcsvd {
 // kernel returns promptly with a status instead of holding the GPU.
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;
 
-// Device status word layout: [0] = error code (0 = ok), [1] = detail.
-struct DevStatus {
+// Device status word: error code (0 = ok) and detail, written by kernels;
+// the two limits below are written by the host before each call
+// (ddcsvd_set_limits) and only read on the device.
+struct __align__(16) DevStatus {
   int code;
   int detail;
+  unsigned wait_us;  // wall-clock limit of one device-side wait in microseconds (0: kWaitLimitNs)
+  unsigned extra;    // fault injection: arrivals that the first grid barrier of a cooperative
+                     // launch waits for beyond its own CTAs (0 in normal use; > 0 makes that
+                     // barrier's waits run out, which tests the timeout path)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -44,6 +50,15 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 
 __device__ __forceinline__ int ld_volatile_int(const int* p) {
   return *reinterpret_cast<const volatile int*>(p);
+}
+
+__device__ __forceinline__ uint4 ld_status(const DevStatus* st) {
+  uint4 v;
+  asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(st)
+               : "memory");
+  return v;
 }
 
 __device__ __forceinline__ void set_error(DevStatus* st, int code, int detail) {
@@ -64,7 +79,8 @@ struct GridBarrier {
 
 // Grid-wide barrier for a cooperative launch of `nblocks` CTAs.  Returns
 // false (in every thread of the CTA) if the status word holds an error or
-// the wait exceeded kWaitLimitNs; callers then leave their loops.
+// the wait exceeded its limit (st->wait_us, else kWaitLimitNs); callers then
+// leave their loops.
 //
 // The arrival counter is never reset inside a launch: barrier k of the launch
 // is complete once it reaches (k + 1) * nblocks, and because no CTA can arrive
@@ -77,9 +93,12 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, De
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const int code = ld_volatile_int(&st->code);
+    const uint4 s = ld_status(st);
+    const int code = (int)s.x;
     const unsigned old = atom_add_acq_rel(&bar->count, 1u);
-    const unsigned target = (old / nblocks + 1u) * nblocks;
+    const unsigned round = old / nblocks;
+    const unsigned target = (round + 1u) * nblocks + (round == 0u ? s.w : 0u);
+    const unsigned long long limit = s.z ? 1000ull * s.z : kWaitLimitNs;
     int ok = code == 0;
     if (ok && old + 1u != target) {
       unsigned polls = 0;
@@ -93,7 +112,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, De
           const unsigned long long now = global_ns();
           if (t0 == 0) {
             t0 = now;
-          } else if (now - t0 > kWaitLimitNs) {
+          } else if (now - t0 > limit) {
             set_error(st, DDCSVD_ERR_TIMEOUT, where);
             ok = 0;
             break;

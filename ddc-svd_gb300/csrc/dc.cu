@@ -38,10 +38,10 @@
 namespace ddcsvd {
 
 constexpr int kDcThreads = 512;
-constexpr int kSecMaxIt = 80;
 
 struct DcParams {
   int N, nnodes, maxdepth, P;
+  int maxit;  // FP64 iterations per secular root (the handle's limit, 80 by default)
   const int* nd_r0;
   const int* nd_nn;
   const int* nd_slot;
@@ -453,7 +453,7 @@ __device__ __forceinline__ void sec_mid32(int q, const float* d, const float* z,
 }
 
 __device__ bool sec_root(int q, const double* d, const double* z, const float* df, const float* zf, double zz,
-                         int i, const LaneGroup& g, int* origin, double* tau_out, int* iters = nullptr) {
+                         int i, const LaneGroup& g, int maxit, int* origin, double* tau_out, int* iters = nullptr) {
   double f, psi, dpsi, phi, dphi;
   const bool last = (i == q - 1);
   int o;
@@ -501,7 +501,7 @@ __device__ bool sec_root(int q, const double* d, const double* z, const float* d
   // remaining error is far below FP64 resolution.
   bool conv = false;
   int it = 0;
-  for (; it < kSecMaxIt; it++) {
+  for (; it < maxit; it++) {
     sec_eval(q, d, z, dorg, tau, split, g, f, psi, dpsi, phi, dphi);
     const double prev = tau;
     if (sec_step<double>(last, f, psi, dpsi, phi, dphi, da0, db0, DBL_EPSILON, lo, hi, tau)) {
@@ -637,7 +637,8 @@ __global__ void __launch_bounds__(kDcThreads, 1) dc_kernel(DcParams p) {
       int o;
       double tau;
       int its = 0;
-      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau, &its);
+      bool ok = sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, p.maxit, &o,
+                         &tau, &its);
 #ifdef DDCSVD_PHASE_TRACE
       if (g.lg == 0 && d < 64) atomicAdd(&g_dc_iters[d * 84 + min(its, 80)], 1u);
 #else
@@ -810,7 +811,7 @@ __global__ void __launch_bounds__(kDcTreeThreads, 2) dc_tree_kernel(DcParams p, 
         int o;
         double tau;
         const bool ok =
-            sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, &o, &tau);
+            sec_root(q, p.dq + slot, p.zq + slot, p.dqf + slot, p.zqf + slot, p.zz[node], i, g, p.maxit, &o, &tau);
         if (g.lg == 0) {
           p.org[pos] = o;
           p.tau[pos] = tau;
@@ -1054,6 +1055,7 @@ int dc_sigma(ddcsvd_context* ctx, int N, const double* b1, const double* b2, dou
   const int nnodes = H->nnodes, md = H->maxdepth;
   DcParams p;
   p.N = N; p.nnodes = nnodes; p.maxdepth = md;
+  p.maxit = ctx->sec_maxit;
   size_t o = 0;
   p.nd_r0 = dints + o; o += nnodes;
   p.nd_nn = dints + o; o += nnodes;

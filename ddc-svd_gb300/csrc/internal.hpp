@@ -39,6 +39,14 @@ struct ddcsvd_context {
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
   int tune[8] = {16, 0, 512, 1, 8, 2, 1, 512};
+  // limits (ddcsvd_set_limits): FP64 secular iterations per root, the
+  // wall-clock limit of device waits (us, 0 = the built-in 4 s), the
+  // workspace budget (bytes, 0 = none), and the fault-injection count of
+  // missing grid-barrier arrivals
+  int sec_maxit = 80;
+  unsigned wait_us = 0;
+  size_t ws_cap = 0;
+  unsigned barrier_extra = 0;
   // set while an SVD of the R factor runs inside the tall-matrix path
   bool nested = false;
   std::mutex mu;

@@ -174,6 +174,25 @@ class Handle:
         buf = (ctypes.c_int * len(self.TUNING_KNOBS))(*[cur[k] for k in self.TUNING_KNOBS])
         check(load().ddcsvd_set_tuning(self._h, ctypes.addressof(buf), len(buf)), "set_tuning")
 
+    LIMITS = ("secular_iterations", "wait_us", "workspace_bytes", "barrier_extra_arrivals")
+
+    @property
+    def limits(self) -> dict:
+        """Limits of this handle (see ddcsvd_get_limits)."""
+        buf = (ctypes.c_longlong * len(self.LIMITS))()
+        check(load().ddcsvd_get_limits(self._h, ctypes.addressof(buf), len(buf)), "get_limits")
+        return dict(zip(self.LIMITS, (int(x) for x in buf)))
+
+    @limits.setter
+    def limits(self, values: dict) -> None:
+        cur = self.limits
+        cur.update(values)
+        buf = (ctypes.c_longlong * len(self.LIMITS))(*[cur[k] for k in self.LIMITS])
+        check(load().ddcsvd_set_limits(self._h, ctypes.addressof(buf), len(buf)), "set_limits")
+
+    def release_workspace(self) -> None:
+        check(load().ddcsvd_release_workspace(self._h), "release_workspace")
+
     def autotune_svd(self, m: int, n: int, mode="auto", reps: int = 2) -> dict:
         check(load().ddcsvd_autotune_svd(self._h, m, n, _mode(mode), reps), "autotune_svd")
         return self.tuning

@@ -48,6 +48,8 @@ _SIGS = {
     "ddcsvd_kernel_launch_count": (c_ll, []),
     "ddcsvd_set_stage_timing": (c_int, [P, c_int]),
     "ddcsvd_get_tuning": (c_int, [P, P, c_int]),
+    "ddcsvd_set_limits": (c_int, [P, P, c_int]),
+    "ddcsvd_get_limits": (c_int, [P, P, c_int]),
     "ddcsvd_set_tuning": (c_int, [P, P, c_int]),
     "ddcsvd_autotune_svd": (c_int, [P, c_int, c_int, c_int, c_int]),
     "ddcsvd_autotune_batched": (c_int, [P, c_int, P, P, c_int]),

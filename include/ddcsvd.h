@@ -178,7 +178,11 @@ int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t handle, int batch, const int *
  * Given dL/ds (gs), dL/dU (gU), dL/dV (gV) -- any may be NULL for zero --
  * writes dL/dA (gA, m x n):
  *   gA = U [diag(gs) + (F o (U^T gU - gU^T U)) S + S (F o (V^T gV - gV^T V))] V^T
- *        + (I - U U^T) gU S^-1 V^T,   F_ij = 1/(s_j^2 - s_i^2) (i != j), 0 on the diagonal. */
+ *        + (I - U U^T) gU S^-1 V^T,   F_ij = 1/(s_j^2 - s_i^2) (i != j), 0 on the diagonal.
+ * The derivative does not exist where two singular values coincide
+ * (s_i = s_j, i != j) or, with gU given, where one is zero: gA then holds
+ * Inf or NaN and the status is still DDCSVD_OK.  Any batch size is accepted
+ * (launches go in chunks of 65535 problems). */
 int ddcsvd_svd_backward_f64_device(ddcsvd_handle_t handle, int batch, int m, int n,
                                    const double *dU, const double *dS, const double *dV,
                                    const double *gU, const double *gS, const double *gV,
@@ -195,11 +199,14 @@ int ddcsvd_svd_backward_f32_device(ddcsvd_handle_t handle, int batch, int m, int
  * routine: its intermediates live in a 16 MiB array compiled into this
  * library, which every GPU that loads the library holds until the process
  * exits.  Inputs and outputs are caller-owned device buffers (same layout as
- * ddcsvd_svd_backward_f64_device); work goes to `stream` (a cudaStream_t,
- * NULL = legacy default stream) and the call returns after a stream
- * synchronisation.  Limit: batch * (3 n^2 + m n) * 8 + 256 bytes must not
- * exceed 16 MiB, else DDCSVD_ERR_ARG (split the batch).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * ddcsvd_svd_backward_f64_device).  The call only enqueues its kernels on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and returns; gA is
+ * ready once that stream has been synchronised.  Launch-configuration errors
+ * come back as DDCSVD_ERR_CUDA.  Limit: 3 r(8 batch n^2) + r(8 batch m n)
+ * bytes, r(x) = x rounded up to a multiple of 256, must not exceed 16 MiB
+ * (16777216), else DDCSVD_ERR_ARG (split the batch).  The first call in a
+ * CUDA context looks up the array's device address in that context
+ * (cudaGetSymbolAddress) and keeps it for the context's lifetime; make that
  * first call before any stream capture.  All calls share the one array:
  * calls whose GPU work overlaps (concurrent streams or threads) race and must
  * be serialised by the caller. */
@@ -241,6 +248,28 @@ int ddcsvd_set_tuning(ddcsvd_handle_t handle, const int *values, int count);
  * batched tuner [2], [3] and [4]. */
 int ddcsvd_autotune_svd(ddcsvd_handle_t handle, int m, int n, int mode, int reps);
 int ddcsvd_autotune_batched(ddcsvd_handle_t handle, int batch, const int *m, const int *n, int reps);
+
+/* ---------------------------------------------------------------- limits */
+
+/* No counterpart in the reference, which has no error path: it aborts the
+ * process on any failure (svd_gpu.c:85, cl-helper.h:47-55) and its secular
+ * bracket search `while (gamma_max < 0)` has no bound
+ * (Calculations-Parallel.c:208, 300).  Limits of a handle, in this order:
+ *   [0] FP64 iterations per secular root in stage 2 (1..80, default 80);
+ *       a root that has not converged by then gives DDCSVD_ERR_NOCONV
+ *   [1] wall-clock limit of one device-side wait of the cooperative kernels
+ *       (grid barriers) in microseconds (0..4000000; 0 = the built-in 4 s);
+ *       a wait that runs out gives DDCSVD_ERR_TIMEOUT and the kernel returns
+ *   [2] device workspace budget of the handle in bytes (0 = none); a call
+ *       whose workspace would exceed it gives DDCSVD_ERR_ALLOC
+ *   [3] fault injection for tests of the timeout path (0 in normal use):
+ *       the first grid barrier of every cooperative launch waits for this
+ *       many arrivals beyond its own CTAs, so its waits run out after limit
+ *       [1] and the call returns DDCSVD_ERR_TIMEOUT
+ * After any of these failures the handle stays usable.  get/set copy up to
+ * `count` limits; set checks the ranges (DDCSVD_ERR_ARG, nothing changed). */
+int ddcsvd_set_limits(ddcsvd_handle_t handle, const long long *values, int count);
+int ddcsvd_get_limits(ddcsvd_handle_t handle, long long *values, int count);
 
 /* ---------------------------------------------------------------- GEMM back ends */
 

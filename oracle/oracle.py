@@ -23,18 +23,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libddcsvd_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libddcsvd_ref.so")
-REF_SRC = "/root/reference"
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
 
-def build(with_ref: bool | None = None) -> None:
-    """Compile the oracle (always) and the reference build (when its sources exist)."""
+def build(with_ref: bool | None = None, ref_src: str | None = None) -> None:
+    """Compile the oracle (always) and the reference build from the reference's
+    sources in `ref_src` (else the DDCSVD_REF_SRC environment variable): when
+    with_ref is True, or None and that directory exists."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    src = ref_src or os.environ.get("DDCSVD_REF_SRC", "")
     if with_ref is None:
-        with_ref = os.path.isdir(REF_SRC)
+        with_ref = bool(src) and os.path.isdir(src)
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        if not (src and os.path.isdir(src)):
+            raise RuntimeError("the reference build needs its sources: pass ref_src or set DDCSVD_REF_SRC")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
 def _ptr(a: np.ndarray | None):

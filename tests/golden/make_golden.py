@@ -1,7 +1,8 @@
 """Generates tests/golden/*.npz from the reference's own host C code.
 
-Run in a container that has the reference sources (the build reads them in
-place through oracle/Makefile's `ref` target):
+Run on a machine that has the reference sources (the build reads them in
+place through oracle/Makefile's `ref` target; DDCSVD_REF_SRC names their
+directory):
 
     python tests/golden/make_golden.py
 
@@ -13,7 +14,13 @@ Each fixture stores the input matrix and the reference's outputs on it:
 Inputs are seeded numpy draws, except `svd_twsvd_*`, which reproduces
 test-whole-svd.c's own input: glibc rand() with its default seed 1,
 A[i] = 1 + 3 * rand() / (RAND_MAX + 1.0) in column-major order
-(test-whole-svd.c:18-23, 69-71).
+(test-whole-svd.c:18-23, 69-71), and `svd_cfg_512x256`, the plain
+single-matrix configuration exactly: default_rng(0).uniform(-1, 1,
+(512, 256)) rounded to FP32 (the reference runs on those FP32 values in
+FP64).  Its V is the reference's and wrong (multV's leading dimension for
+m != n); tests compare sigma and U only.
+
+    python tests/golden/make_golden.py --only svd_cfg_512x256   # one fixture
 """
 from __future__ import annotations
 
@@ -38,8 +45,11 @@ def glibc_rand_matrix(m: int, n: int) -> np.ndarray:
     return a.reshape((n, m)).T.copy(order="F")
 
 
-def main() -> None:
-    O.build(with_ref=True)
+REF_SRC = os.environ.get("DDCSVD_REF_SRC", "/root/reference")
+
+
+def main(only: list[str] | None = None) -> None:
+    O.build(with_ref=True, ref_src=REF_SRC)
     out = {}
     rng = np.random.default_rng(20121220)
     # bidiagonalisation goldens, including the m < n edge path (bidiag.c:133-160)
@@ -66,10 +76,20 @@ def main() -> None:
                                   V=r["V"].astype(np.float32), alpha=r["alpha"], beta=r["beta"],
                                   X=r["X"].astype(np.float32), Y=r["Y"].astype(np.float32),
                                   sigma_lapack=np.linalg.svd(A, compute_uv=False)[::-1].copy())
+    # the plain single-matrix configuration: 512 x 256, U[-1, 1] from default_rng(0), FP32 entries
+    A = np.random.default_rng(0).uniform(-1.0, 1.0, (512, 256)).astype(np.float32).astype(np.float64)
+    r = O.ref_svd(A)
+    out["svd_cfg_512x256"] = dict(A=A, sigma=r["sigma"], U=r["U"].astype(np.float32), V=r["V"].astype(np.float32),
+                                  alpha=r["alpha"], beta=r["beta"],
+                                  sigma_lapack=np.linalg.svd(A, compute_uv=False)[::-1].copy())
+    written = 0
     for name, d in out.items():
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
-    print(f"wrote {len(out)} fixtures to {HERE}")
+        written += 1
+    print(f"wrote {written} fixtures to {HERE}")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[sys.argv.index("--only") + 1:] if "--only" in sys.argv else None)

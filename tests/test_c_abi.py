@@ -36,3 +36,18 @@ def test_c_caller_compiles_links_and_runs(lib, tmp_path):
     assert lines["split"].split() == ["0", "4", "0", "2", "3", "6"]
     assert lines["plan"].split()[:1] == ["0"] and lines["plan"].split()[4] == "3"
     assert lines["status"] == "ok"
+
+
+def test_context_cache_logic(tmp_path):
+    """The allocation-free adjoint keeps its scratch address per CUDA context
+    id; the cache logic is host-only C++ and is checked here without a GPU."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    csrc = os.path.join(os.path.dirname(HERE), "ddc-svd_gb300", "csrc")
+    exe = str(tmp_path / "ctx_cache_check")
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-pthread", "-I", csrc,
+                    os.path.join(HERE, "c", "ctx_cache_check.cpp"), "-o", exe], check=True, capture_output=True,
+                   text=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr

@@ -7,7 +7,10 @@ takes no handle and keeps its intermediates in a fixed 16 MiB array inside
 the library.  These tests call it through the C ABI and compare it with the
 handle-based entry point, ddcsvd_svd_backward_f64_device, on two calls in a
 row (the second call finds the first call's data still in the shared array),
-and check that a call needing more than the fixed scratch is refused.
+check the size limit at exactly its documented value (accepted) and one
+problem beyond it (refused), and run a batch larger than one launch grid
+holds (more than 65535 problems).  The entry point only enqueues its work on
+the given stream; torch's own kernels on that stream run after it.
 """
 import ctypes
 
@@ -77,3 +80,44 @@ def test_noalloc_adjoint_refuses_more_than_its_scratch(lib, cuda):
     rc, _ = _noalloc(lib, torch, U, S, V, gU, gS, gV)
     assert rc == 1
     assert b"limit" in lib.load().ddcsvd_last_error()
+
+
+def _limit_bytes(B, m, n):
+    r = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    return 3 * r(8 * B * n * n) + r(8 * B * m * n)
+
+
+def test_noalloc_adjoint_limit_is_exact(lib, cuda):
+    """m = n = 64: each problem takes 128 KiB, so 128 problems fill the 16 MiB exactly."""
+    torch = cuda
+    m = n = 64
+    assert _limit_bytes(128, m, n) == 16 << 20 and _limit_bytes(129, m, n) > 16 << 20
+    U, S, V, gU, gS, gV = _problem(torch, 15, 129, m, n)
+    rc, got = _noalloc(lib, torch, U[:128], S[:128], V[:128], gU[:128], gS[:128], gV[:128])
+    assert rc == 0, lib.load().ddcsvd_last_error()
+    ref = lib.svd_backward_device(U[:128], S[:128], V[:128], gU[:128], gS[:128], gV[:128])
+    assert float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref)) <= 1e-12
+    rc, _ = _noalloc(lib, torch, U, S, V, gU, gS, gV)
+    assert rc == 1
+
+
+def test_noalloc_adjoint_batch_beyond_one_launch_grid(lib, cuda):
+    torch = cuda
+    B, m, n = 70000, 3, 2
+    U, S, V, gU, gS, gV = _problem(torch, 16, B, m, n)
+    rc, got = _noalloc(lib, torch, U, S, V, gU, gS, gV)
+    assert rc == 0, lib.load().ddcsvd_last_error()
+    ref = lib.svd_backward_device(U, S, V, gU, gS, gV)
+    assert float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref)) <= 1e-12
+    # the last chunk (problems 65535..69999) against a direct evaluation
+    k = slice(65535, B)
+    Ui, Si, Vi, gUi, gSi, gVi = U[k], S[k], V[k], gU[k], gS[k], gV[k]
+    F = Si[:, None, :] ** 2 - Si[:, :, None] ** 2
+    F = torch.where(F == 0, torch.full_like(F, float("inf")), F).reciprocal()
+    J = Ui.transpose(1, 2) @ gUi
+    K = Vi.transpose(1, 2) @ gVi
+    Mi = torch.diag_embed(gSi) + (F * (J - J.transpose(1, 2))) * Si[:, None, :] + \
+        Si[:, :, None] * (F * (K - K.transpose(1, 2)))
+    proj = gUi - Ui @ (Ui.transpose(1, 2) @ gUi)
+    direct = Ui @ Mi @ Vi.transpose(1, 2) + (proj / Si[:, None, :]) @ Vi.transpose(1, 2)
+    assert float(torch.linalg.norm(got[k] - direct) / torch.linalg.norm(direct)) <= 1e-12
