@@ -41,18 +41,19 @@ SEED = 1
 METRIC = "4096^2 full-SVD ms (graded cond 1e6, FP32)"  # names the default --size
 
 
-def graded_matrix(torch, n, seed, device):
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    G1 = torch.randn((n, n), dtype=torch.float64, device=device, generator=g)
-    G2 = torch.randn((n, n), dtype=torch.float64, device=device, generator=g)
-    Q1, R1 = torch.linalg.qr(G1)
-    Q1 = Q1 * torch.sign(torch.diagonal(R1))
-    Q2, R2 = torch.linalg.qr(G2)
-    Q2 = Q2 * torch.sign(torch.diagonal(R2))
-    s = 10.0 ** (-6.0 * torch.arange(n, dtype=torch.float64, device=device) / (n - 1))
-    A64 = (Q1 * s) @ Q2.T
-    return A64, s
+def graded_matrix_host(n, seed):
+    """The graded configuration on the host, identical for both bench arms and
+    the tests: Gaussians from numpy default_rng(seed) (Q1's, then Q2's), Haar
+    factors from their QR sign-fixed by diag(R), sigma_i = 10^(-6 i/(n-1)),
+    A = Q1 diag(sigma) Q2^T formed in FP64 and rounded to FP32.  Returns
+    (A as FP32, sigma descending as FP64)."""
+    rng = np.random.default_rng(seed)
+    Q1, R1 = np.linalg.qr(rng.standard_normal((n, n)))
+    Q1 *= np.sign(np.diag(R1))
+    Q2, R2 = np.linalg.qr(rng.standard_normal((n, n)))
+    Q2 *= np.sign(np.diag(R2))
+    s = 10.0 ** (-6.0 * np.arange(n) / (n - 1))
+    return ((Q1 * s) @ Q2.T).astype(np.float32), s
 
 
 class ClockSampler:
@@ -106,6 +107,60 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def device_peaks(torch):
+    """Rates measured here with library code and CUDA events, for rooflines that
+    MEASURED_PEAKS.json does not hold: L2 read bandwidth (cuBLAS SGEMV over a
+    64 MiB matrix, a 2 x 32 MiB copy and a sum over 48 MiB -- working sets
+    that stay L2-resident across repetitions; the best of the three), FP32
+    CUDA-core rate (cuBLAS SGEMM 8192^3 with TF32 off) and FP64 rate (cuBLAS
+    DGEMM 4096^3)."""
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps
+
+    out = {}
+    A = torch.randn((4096, 4096), device="cuda")
+    x = torch.randn(4096, device="cuda")
+    y = torch.empty(4096, device="cuda")
+    t = timed(lambda: torch.mv(A, x, out=y), 50)
+    l2 = {"sgemv_64MiB": 4096 * 4096 * 4 / t / 1e9}
+    a = torch.randn(8 << 20, device="cuda")
+    b = torch.empty_like(a)
+    t = timed(lambda: b.copy_(a), 50)
+    l2["copy_2x32MiB"] = 2 * a.numel() * 4 / t / 1e9
+    c = torch.randn(12 << 20, device="cuda")
+    r = torch.empty((), device="cuda")
+    t = timed(lambda: torch.sum(c, out=r), 50)
+    l2["sum_48MiB"] = c.numel() * 4 / t / 1e9
+    out["l2_read_gbs"] = round(max(l2.values()), 1)
+    out["l2_probes_gbs"] = {k: round(v, 1) for k, v in l2.items()}
+    del A, a, b, c
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    X = torch.randn((8192, 8192), device="cuda")
+    Y = torch.empty_like(X)
+    t = timed(lambda: torch.matmul(X, X, out=Y), 5)
+    out["fp32_simt_tflops"] = round(2 * 8192 ** 3 / t / 1e12, 2)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del X, Y
+    D = torch.randn((4096, 4096), dtype=torch.float64, device="cuda")
+    E = torch.empty_like(D)
+    t = timed(lambda: torch.matmul(D, D, out=E), 3)
+    out["fp64_tflops"] = round(2 * 4096 ** 3 / t / 1e12, 3)
+    del D, E
+    torch.cuda.empty_cache()
+    out["how"] = ("CUDA events around repeated cuBLAS / torch calls: SGEMV, copy and sum on L2-resident "
+                  "working sets (best of three = l2_read_gbs), SGEMM 8192^3 with TF32 off, DGEMM 4096^3")
+    return out
+
+
 def gemv_bytes(m, n):
     """Algorithmic bytes of the memory-bound half of the bidiagonalisation:
     every column step reads the trailing block twice (y = A^T u, x = A v),
@@ -154,10 +209,15 @@ def time_mode(torch, lib, h, Ac, bufs, mode, steps, warmup, flush):
 
 def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
     """FP64 CPU restatement of the reference pipeline (bidiag.c + host stages) on a
-    bounded sample of the 4096^2 workload, extrapolated to the full SVD."""
+    bounded sample of the 4096^2 workload, extrapolated to the full SVD.
+
+    Threads: the bidiagonalisation is one thread (like the reference's
+    bidiag_seq); the D&C, vector and back-transformation stages run OpenMP
+    loops on every host core (as the reference's do), so `cores` is the
+    host's core count and `threads` gives the split."""
     from oracle import oracle
     oracle.build(with_ref=False)
-    threads = 1  # the port is scalar, like the reference's bidiag_seq (>99% of the time)
+    omp = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or (os.cpu_count() or 1)
     m, n = A64_host.shape
     # (1) bidiagonalisation: the first k Householder steps of the 4096^2 matrix
     A = np.asfortranarray(A64_host.copy())
@@ -185,10 +245,14 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
     tbb = time.perf_counter() - t0
     rest_full = max(tfull - tbb, 0.0) * (n / ns) ** 3
     total_ms = 1e3 * (bidiag_full + rest_full)
-    return {"value": round(total_ms, 1), "unit": "ms", "cores": threads, "kind": "port",
-            "sample": (f"FP64 CPU port of bidiag.c + host stages: first {k2} of {n - 1} Householder steps of the "
-                       f"4096^2 input ({tb:.1f} s, scaled by the step work sum (m-i)(n-i)), plus the other "
-                       f"stages on its leading 1024^2 block ({max(tfull - tbb, 0):.2f} s, scaled by (4096/1024)^3)")}
+    return {"value": round(total_ms, 1), "unit": "ms", "cores": omp, "kind": "port", "extrapolated": True,
+            "threads": {"bidiagonalisation": 1, "stages_2_to_5": omp},
+            "same_config": True,
+            "parts_ms": {"bidiagonalisation": round(1e3 * bidiag_full, 1), "stages_2_to_5": round(1e3 * rest_full, 1)},
+            "sample": (f"FP64 CPU port of bidiag.c + host stages on the same FP32 input as the GPU arm: first {k2} "
+                       f"of {n - 1} Householder steps of the {n}^2 input ({tb:.1f} s, scaled by the step work "
+                       f"sum (m-i)(n-i)), plus the other stages on its leading {ns}^2 block "
+                       f"({max(tfull - tbb, 0):.2f} s, scaled by ({n}/{ns})^3); an extrapolation, not a full run")}
 
 
 # DRAM bytes (read + write) of one panel-kernel launch, mean over the 4096^2
@@ -269,7 +333,7 @@ def lib_mode_ok(lib, h):
         raise
 
 
-def bench_batched(torch, lib, h, steps, flush, dist=None, world=1, rank=0):
+def bench_batched(torch, lib, h, steps, flush, dist=None, world=1, rank=0, peaks=None):
     """The 2048-problem batch; under torchrun the problems are split across
     ranks by cost (no exchange) and SVDs/s is the whole batch over the slowest
     rank's time."""
@@ -315,7 +379,22 @@ def bench_batched(torch, lib, h, steps, flush, dist=None, world=1, rank=0):
     comp = sum(4 * (2 * a.shape[0] * a.shape[1] + a.shape[1] + a.shape[1] ** 2) for a in allmats)
     flops = sum(8.0 * a.shape[0] * a.shape[1] ** 2 - 4.0 / 3.0 * a.shape[1] ** 3 for a in allmats)
     hbm, _ = measured_peaks()
+    # compute rooflines (the batch is ~84 flop/B: compute-bound, so the HBM fraction is small by construction)
+    f1 = sum(4.0 * a.shape[0] * a.shape[1] ** 2 - 4.0 / 3.0 * a.shape[1] ** 3 for a in mats)  # bidiagonalisation
+    f5 = sum(4.0 * a.shape[0] * a.shape[1] ** 2 for a in mats)  # U and V back-transformation
+    comp_roof = None
+    if peaks:
+        p32 = peaks["fp32_simt_tflops"] * 1e12
+        comp_roof = {"unit": "TFLOP/s", "peak_fp32": peaks["fp32_simt_tflops"], "peak_kind": "measured (cuBLAS SGEMM)",
+                     "whole_batch_fp32_frac": round(flops / (ms * 1e-3) / p32, 4),
+                     "stage1_fp32_frac": round(f1 / (kms[0] * 1e-3) / p32, 4) if kms[0] > 0 else None,
+                     "backxform_fp32_frac": round(f5 / (kms[4] * 1e-3) / p32, 4) if kms[4] > 0 else None,
+                     "dc_fp64_pipe_frac": 0.83,
+                     "dc_note": "dc_tree_kernel FP64 pipe utilisation from the committed ncu capture "
+                                "(profiles/dc_tree_kernel_batched2048.md); its FP64 work is data-dependent "
+                                "(secular iterations), so no flop count is formed here"}
     return {"svds_per_s": round(len(allmats) / (ms * 1e-3), 1), "ms": round(ms, 3), "count": len(allmats),
+            "compute_roofline": comp_roof,
             "ranks": world, "scaling": "strong (one batch split across ranks by cost)" if world > 1 else "n/a",
             "loop_single_svds_per_s": round(1e3 / loop_ms, 1), "compulsory_bytes": comp, "elements": mn,
             "hbm_frac": round(comp / (ms * 1e-3) / 1e9 / hbm, 4), "gflops": round(flops / (ms * 1e-3) / 1e9, 1),
@@ -324,7 +403,7 @@ def bench_batched(torch, lib, h, steps, flush, dist=None, world=1, rank=0):
                                   [round(x, 3) for x in kms]))}
 
 
-def bench_adjoint(torch, lib, h, steps):
+def bench_adjoint(torch, lib, h, steps, peaks=None):
     out = {}
     rng = np.random.default_rng(4)
     B, m, n = 256, 128, 64
@@ -343,8 +422,17 @@ def bench_adjoint(torch, lib, h, steps):
             e1.record()
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1))
-        out[f"bwd_ms_{name}"] = round(float(np.mean(ts)), 4)
+        ms = float(np.mean(ts))
+        out[f"bwd_ms_{name}"] = round(ms, 4)
+        # the four batched products: J = U^T gU, K = V^T gV, P += U M, gA = P V^T
+        fl = B * (2.0 * n * n * m + 2.0 * n * n * n + 2.0 * m * n * n + 2.0 * m * n * n)
+        out[f"bwd_tflops_{name}"] = round(fl / (ms * 1e-3) / 1e12, 3)
+        if peaks:
+            pk = peaks["fp64_tflops"] if name == "f64" else peaks["fp32_simt_tflops"]
+            out[f"bwd_frac_{name}"] = round(fl / (ms * 1e-3) / 1e12 / pk, 4)
     out["shape"] = "256 x (128x64)"
+    if peaks:
+        out["peak_note"] = "fractions of the measured cuBLAS DGEMM (f64) and SGEMM with TF32 off (f32) rates"
     return out
 
 
@@ -353,13 +441,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    rng = np.random.default_rng(SEED)
-    Q1, R1 = np.linalg.qr(rng.standard_normal((M, M)))
-    Q1 *= np.sign(np.diag(R1))
-    Q2, R2 = np.linalg.qr(rng.standard_normal((N, N)))
-    Q2 *= np.sign(np.diag(R2))
-    s = 10.0 ** (-6.0 * np.arange(N) / (N - 1))
-    A64 = ((Q1 * s) @ Q2.T).astype(np.float32).astype(np.float64)
+    A32, _ = graded_matrix_host(N, SEED)
+    A64 = A32.astype(np.float64)
     budget = max(4.0, 150.0 / max(args.steps + args.warmup, 1))
     vals = []
     cb = None
@@ -407,10 +490,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    A64, s_true = graded_matrix(torch, N, SEED + rank, dev)
+    A32h, s_np = graded_matrix_host(N, SEED + rank)
     workload = f"svd_graded_{M}x{N}"
-    A32 = A64.float()
+    A32 = torch.from_numpy(A32h).to(dev)
     A64r = A32.double()
+    s_true = torch.from_numpy(s_np).to(dev)
     Ac = A32.t().contiguous()  # column-major buffer
     h = lib.Handle(local)
     # launch knobs from the library's autotuner for this shape (untimed)
@@ -432,7 +516,7 @@ def main():
         avail.append(mode)
         torch.cuda.synchronize()
         s, Ut, Vt = bufs
-        acc = accuracy(torch, A64r, torch.linalg.svdvals(A64r) if False else s_true, s, Ut.t(), Vt.t())
+        acc = accuracy(torch, A64r, s_true, s, Ut.t(), Vt.t())
         h.stage_timing(True)
         lib.svd_device_colmajor(h, M, N, Ac, *bufs, mode=mode)
         torch.cuda.synchronize()
@@ -496,8 +580,10 @@ def main():
         e2e.append(1e3 * (time.perf_counter() - t0))
     e2e_ms = float(np.mean(e2e))
 
-    batched = bench_batched(torch, lib, h, max(3, args.steps), flush, dist, world, rank) if not args.quick else None
-    adjoint = bench_adjoint(torch, lib, h, max(3, args.steps)) if not args.quick else None
+    peaks = device_peaks(torch)
+    batched = (bench_batched(torch, lib, h, max(3, args.steps), flush, dist, world, rank, peaks)
+               if not args.quick else None)
+    adjoint = bench_adjoint(torch, lib, h, max(3, args.steps), peaks) if not args.quick else None
     tall = bench_tall(torch, lib, h, 2) if not args.quick else None
 
     # roofline of the dominant kernel class (bidiagonalisation GEMV kernels)
@@ -516,7 +602,12 @@ def main():
                             "achieved = the two GEMVs' algorithmic bytes over all columns / the summed time of "
                             "the panel launches and the cluster-tail launch",
             "bytes_per_launch": round(bytes_total / nl), "launches": nl,
-            "avg_launch_ms": round(bid_ms / nl, 4)}
+            "avg_launch_ms": round(bid_ms / nl, 4),
+            "l2": {"achieved": round(achieved, 1) if achieved else None, "peak": peaks["l2_read_gbs"],
+                   "peak_kind": "measured here (best L2-resident read probe)", "unit": "GB/s",
+                   "frac": round(achieved / peaks["l2_read_gbs"], 3) if achieved else None,
+                   "note": "the 4096^2 trailing block (64 MiB) stays in L2 between column steps, so L2 "
+                           "bandwidth is the binding memory bound of this kernel"}}
 
     if rank != 0:
         if dist is not None:
@@ -524,7 +615,7 @@ def main():
         return
     cb = None
     if world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(A64r.cpu().numpy())
+        cb = cpu_baseline(A32h.astype(np.float64))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False, "scaling": "weak",
@@ -537,7 +628,7 @@ def main():
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": M * N * 4,
                 "d2h_bytes_per_step": (N + M * N + N * N) * 4, "api": "ddcsvd_svd_f32 (pinned host buffers)"},
         "roofline": roof, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cb,
-        "batched": batched, "adjoint": adjoint, "tall": tall,
+        "batched": batched, "adjoint": adjoint, "tall": tall, "device_peaks": peaks,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -69,8 +69,10 @@ def test_config_plain_512x256_vs_reference_outputs(lib, cuda, orc):
     gaps = np.diff(g["sigma_lapack"])
     gap = np.minimum(np.r_[np.inf, gaps], np.r_[gaps, np.inf]) / smax
     Ur = g["U"].astype(np.float64)
-    sep = [k for k in range(256) if gap[k] > 1e-2]
-    assert len(sep) > 100
+    # columns whose sigma is separated by more than 5e-4 sigma_max (244 of 256 here): the
+    # reference's U agrees with the FP64 oracle there to 2e-9 in 1 - |cos|
+    sep = [k for k in range(256) if gap[k] > 5e-4]
+    assert len(sep) >= 200
     runs = {"svd_gpu": lib.svd_gpu(A)}
     for mode in _modes(lib, cuda):
         s, U, V = lib.svd_device(torch.from_numpy(A.astype(np.float32)).cuda(), mode=mode)
@@ -82,7 +84,7 @@ def test_config_plain_512x256_vs_reference_outputs(lib, cuda, orc):
         met = orc.metrics(A, s, U, V, g["sigma_lapack"])
         assert met["resid"] <= TOL and met["orth_u"] <= TOL and met["orth_v"] <= TOL, (name, met)
         for k in sep:
-            assert abs(abs(U[:, k] @ Ur[:, k]) / np.linalg.norm(Ur[:, k]) - 1) < 1e-3, (name, k)
+            assert abs(abs(U[:, k] @ Ur[:, k]) / np.linalg.norm(Ur[:, k]) - 1) < 1e-4, (name, k)
 
 
 # ------------------------------------------------------------------ 4096^2 graded
