@@ -21,48 +21,71 @@ namespace ddcsvd {
 
 // C[b] (M x N, col-major, ldc) = beta * C[b] + alpha * A[b] B[b], element
 // (r, k) of A[b] at A + b*as + r*ars + k*acs, element (k, c) of B[b] at
-// B + b*bs + k*brs + c*bcs.  32 x 32 tiles, 16 x 16 threads, 2 x 2 outputs each.
+// B + b*bs + k*brs + c*bcs.  64 x 64 tiles, 256 threads with 4 x 4 outputs
+// each (rows ty + 16 a, columns tx + 16 c), K in slabs of 16.  Tile loads
+// walk the operand's unit-stride index fastest, so either layout of A and B
+// (the adjoint reads U, V transposed and not) is read in coalesced segments.
+constexpr int kBgTile = 64, kBgK = 16;
+
 template <typename T>
-__global__ void bgemm_kernel(int M, int N, int K, const T* __restrict__ A, long long ars, long long acs,
-                             long long as, const T* __restrict__ B, long long brs, long long bcs, long long bs,
-                             T* C, int ldc, long long cs, T alpha, T beta) {
-  __shared__ T At[32][33];
-  __shared__ T Bt[32][33];
+__device__ __forceinline__ void bgemm_load(T (*dst)[kBgTile + 1], const T* __restrict__ src, long long s_mn,
+                                           long long s_k, int mn0, int MN, int k0, int K) {
+  // dst[kk][i] = element (mn0 + i, k0 + kk); the index with stride 1 varies fastest across threads
+  const bool k_fast = (s_k == 1 && s_mn != 1);
+  for (int idx = threadIdx.x; idx < kBgTile * kBgK; idx += blockDim.x) {
+    int i, kk;
+    if (k_fast) { kk = idx % kBgK; i = idx / kBgK; }
+    else { i = idx % kBgTile; kk = idx / kBgTile; }
+    const int r = mn0 + i, k = k0 + kk;
+    dst[kk][i] = (r < MN && k < K) ? src[r * s_mn + k * s_k] : T(0);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, const T* __restrict__ A, long long ars,
+                                                    long long acs, long long as, const T* __restrict__ B,
+                                                    long long brs, long long bcs, long long bs, T* C, int ldc,
+                                                    long long cs, T alpha, T beta) {
+  __shared__ T At[kBgK][kBgTile + 1];
+  __shared__ T Bt[kBgK][kBgTile + 1];
   const int b = blockIdx.z;
-  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int r0 = blockIdx.x * kBgTile, c0 = blockIdx.y * kBgTile;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const T* Ab = A + b * as;
   const T* Bb = B + b * bs;
-  T acc[2][2] = {{0, 0}, {0, 0}};
-  for (int k0 = 0; k0 < K; k0 += 32) {
-    for (int idx = ty * 16 + tx; idx < 32 * 32; idx += 256) {
-      const int i = idx % 32, kk = idx / 32;
-      const int r = r0 + i, k = k0 + kk;
-      At[kk][i] = (r < M && k < K) ? Ab[r * ars + k * acs] : T(0);
-      const int c = c0 + i;
-      Bt[kk][i] = (c < N && k < K) ? Bb[k * brs + c * bcs] : T(0);
-    }
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[a][c] = T(0);
+  for (int k0 = 0; k0 < K; k0 += kBgK) {
+    bgemm_load<T>(At, Ab, ars, acs, r0, M, k0, K);
+    bgemm_load<T>(Bt, Bb, bcs, brs, c0, N, k0, K);
     __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < 32; kk++) {
-      const T a0 = At[kk][ty], a1 = At[kk][ty + 16];
-      const T b0 = Bt[kk][tx], b1 = Bt[kk][tx + 16];
-      acc[0][0] += a0 * b0;
-      acc[0][1] += a0 * b1;
-      acc[1][0] += a1 * b0;
-      acc[1][1] += a1 * b1;
+#pragma unroll
+    for (int kk = 0; kk < kBgK; kk++) {
+      T x[4], y[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        x[a] = At[kk][ty + 16 * a];
+        y[a] = Bt[kk][tx + 16 * a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[a][c] += x[a] * y[c];
     }
     __syncthreads();
   }
   T* Cb = C + b * cs;
 #pragma unroll
-  for (int i = 0; i < 2; i++)
+  for (int a = 0; a < 4; a++)
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-      const int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
-      if (r < M && c < N) {
-        T* p = Cb + r + (size_t)c * ldc;
-        *p = (beta == T(0) ? T(0) : beta * *p) + alpha * acc[i][j];
+    for (int c = 0; c < 4; c++) {
+      const int r = r0 + ty + 16 * a, cc = c0 + tx + 16 * c;
+      if (r < M && cc < N) {
+        T* p = Cb + r + (size_t)cc * ldc;
+        *p = (beta == T(0) ? T(0) : beta * *p) + alpha * acc[a][c];
       }
     }
 }
@@ -100,9 +123,9 @@ template <typename T>
 static int bgemm(ddcsvd_context* ctx, int batch, int M, int N, int K, const T* A, long long ars, long long acs,
                  long long as, const T* B, long long brs, long long bcs, long long bs, T* C, int ldc, long long cs,
                  T alpha, T beta) {
-  dim3 grid(ceil_div(M, 32), ceil_div(N, 32), batch);
-  bgemm_kernel<T><<<grid, dim3(16, 16), 0, ctx->stream>>>(M, N, K, A, ars, acs, as, B, brs, bcs, bs, C, ldc, cs,
-                                                          alpha, beta);
+  dim3 grid(ceil_div(M, kBgTile), ceil_div(N, kBgTile), batch);
+  bgemm_kernel<T><<<grid, 256, 0, ctx->stream>>>(M, N, K, A, ars, acs, as, B, brs, bcs, bs, C, ldc, cs, alpha,
+                                                 beta);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;

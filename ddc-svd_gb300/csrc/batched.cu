@@ -39,8 +39,11 @@ constexpr int kBatchBidiagThreads = 512;  // bidiagonalisation CTAs (one per SM,
 
 __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 
-// Compensated CTA-wide sum; every thread gets the same value (warps are
-// added in warp order).  `red` holds 2 * (blockDim.x / 32) floats.
+// Compensated CTA-wide sum; every thread gets the same value.  The warp
+// partials are added as a fixed pairwise tree (depth log2 of the warp
+// count instead of a chain through all of them: every thread forms the
+// total, so its latency sits on each column step), the same tree in every
+// thread.  `red` holds 2 * (blockDim.x / 32) floats; blockDim.x / 32 <= 16.
 __device__ __forceinline__ FF cta_sum_ff(FF v, float* red) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   v = warp_sum_ff(v);
@@ -50,9 +53,15 @@ __device__ __forceinline__ FF cta_sum_ff(FF v, float* red) {
     red[2 * wid + 1] = v.lo;
   }
   __syncthreads();
-  FF r{0.f, 0.f};
-  for (int k = 0; k < nw; k++) r = ff_add(r, FF{red[2 * k], red[2 * k + 1]});
-  return r;
+  auto ld = [&](int k) { return k < nw ? FF{red[2 * k], red[2 * k + 1]} : FF{0.f, 0.f}; };
+  FF w[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) w[k] = ff_add(ld(k), ld(k + 8));
+#pragma unroll
+  for (int h = 4; h > 0; h >>= 1)
+#pragma unroll
+    for (int k = 0; k < h; k++) w[k] = ff_add(w[k], w[k + h]);
+  return w[0];
 }
 
 constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m - i <= 256)

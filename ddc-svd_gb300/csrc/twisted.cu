@@ -432,21 +432,76 @@ __device__ void cl_refine(const TwParams& p, int k0, double* red) {
   }
 }
 
-// rank of sigma_k among the sigmas of its group (ascending, stable).
-__global__ void tw_rank_kernel(int N, const double* __restrict__ sigma, VecLayout L, int* rank,
-                               double* sorted) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+// rank of sigma_k among the sigmas of its group (ascending, stable):
+// rank_k = #{j in group : s_j < s_k or (s_j == s_k and j < k)}.  The count
+// is split over slot segments (grid y) so that a single large group (one SVD:
+// N^2 comparisons) spreads over the whole GPU; each CTA stages the part of
+// its segment that its threads' groups touch in shared memory, and adds its
+// partial counts with integer atomics (rank zeroed beforehand), so the
+// result is exact and independent of the order.
+constexpr int kRankThreads = 256;
+constexpr int kRankTile = 1024;
+
+__global__ void __launch_bounds__(kRankThreads) tw_rank_count_kernel(int N, const double* __restrict__ sigma,
+                                                                   VecLayout L, int* rank, int seg) {
+  __shared__ double tile[kRankTile];
+  __shared__ int s_lo, s_hi;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int glo = N, ghi = 0;
+  double v = 0.0;
+  if (k < N) {
     const int g = L.grp[k];
-    const int g0 = L.g_lo[g], gn = L.g_n[g];
-    const double v = sigma[k];
-    int r = 0;
-    for (int j = g0; j < g0 + gn; j++) {
-      const double u = sigma[j];
-      r += (u < v) || (u == v && j < k);
-    }
-    rank[k] = r;
-    if (sorted) sorted[g0 + r] = v;
+    glo = L.g_lo[g];
+    ghi = glo + L.g_n[g];
+    v = sigma[k];
   }
+  if (threadIdx.x == 0) {
+    s_lo = N;
+    s_hi = 0;
+  }
+  __syncthreads();
+  if (k < N) {
+    atomicMin(&s_lo, glo);
+    atomicMax(&s_hi, ghi);
+  }
+  __syncthreads();
+  const int j0 = max(blockIdx.y * seg, s_lo), j1 = min(min(N, (blockIdx.y + 1) * seg), s_hi);
+  int cnt = 0;
+  for (int t0 = j0; t0 < j1; t0 += kRankTile) {
+    const int t1 = min(j1, t0 + kRankTile);
+    for (int j = t0 + threadIdx.x; j < t1; j += blockDim.x) tile[j - t0] = sigma[j];
+    __syncthreads();
+    const int a = max(t0, glo), b = min(t1, ghi);
+    for (int j = a; j < b; j++) {
+      const double u = tile[j - t0];
+      cnt += (u < v) || (u == v && j < k);
+    }
+    __syncthreads();
+  }
+  if (k < N && cnt) atomicAdd(&rank[k], cnt);
+}
+
+__global__ void tw_rank_place_kernel(int N, const double* __restrict__ sigma, VecLayout L, const int* rank,
+                                     double* sorted) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
+    sorted[L.g_lo[L.grp[k]] + rank[k]] = sigma[k];
+}
+
+static int rank_values(ddcsvd_context* ctx, int N, const double* sigma, const VecLayout& L, int* rank,
+                       double* sorted) {
+  DDC_CUDA_TRY(cudaMemsetAsync(rank, 0, sizeof(int) * (size_t)N, ctx->stream));
+  const int nseg = std::max(1, std::min(16, ceil_div(N, 512)));
+  const int seg = ceil_div(N, nseg);
+  tw_rank_count_kernel<<<dim3(ceil_div(N, kRankThreads), nseg), kRankThreads, 0, ctx->stream>>>(N, sigma, L, rank,
+                                                                                                  seg);
+  count_launch();
+  if (sorted) {
+    tw_rank_place_kernel<<<std::min(ceil_div(N, 256), 8 * ctx->num_sms), 256, 0, ctx->stream>>>(N, sigma, L, rank,
+                                                                                                sorted);
+    count_launch();
+  }
+  DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
 }
 
 // One 32 x 32 tile (vectors k0.., rows i0.. of a block) per CTA:
@@ -497,10 +552,7 @@ __global__ void tw_zero_outside_kernel(int N, TwParams p) {
 
 int sort_values(ddcsvd_context* ctx, int N, const double* in, double* out, const VecLayout* L, Arena& a) {
   int* rank = a.take<int>(N + 8);
-  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, in, *L, rank, out);
-  count_launch();
-  DDC_CUDA_TRY(cudaGetLastError());
-  return DDCSVD_OK;
+  return rank_values(ctx, N, in, *L, rank, out);
 }
 
 void split_bidiagonal(int N, double* a, double* b, double eps, std::vector<int>& starts, int* blk_lo,
@@ -559,8 +611,7 @@ int bd_vectors(ddcsvd_context* ctx, int N, long long store, const double* a, con
   count_launch();
   tw_cluster_kernel<<<std::min(ceil_div(N, kClThreads), 2 * ctx->num_sms), kClThreads, 0, ctx->stream>>>(p);
   count_launch();
-  tw_rank_kernel<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, sigma, p.L, rank, sigma_sorted);
-  count_launch();
+  DDC_TRY(rank_values(ctx, N, sigma, p.L, rank, sigma_sorted));
   tw_finalize_kernel<<<L->ntiles, dim3(32, 8), 0, ctx->stream>>>(p);
   count_launch();
   tw_zero_outside_kernel<<<std::min(N, 16 * ctx->num_sms), 128, 0, ctx->stream>>>(N, p);
