@@ -255,12 +255,14 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
 
 
 # DRAM bytes (read + write) of one panel-kernel launch, mean over the 4096^2
-# factorisation, from an ncu capture of `python -m ddcsvd.profile --size 4096
-# --mode tf32x6 --reps 1 --kind uniform` (metrics dram__bytes_read.sum and
-# dram__bytes_write.sum, all 112 panel launches; the last 512 columns run in
-# one cluster-tail launch).  Far below the algorithmic GEMV bytes: the
-# trailing block is re-read from L2, not HBM.
-PANEL_DRAM_BYTES_PER_LAUNCH = 26006530
+# factorisation: ncu (metrics dram__bytes_read.sum and dram__bytes_write.sum)
+# on six sampled launches of `python -m ddcsvd.profile --size 4096 --mode
+# tf32x6 --reps 1 --kind uniform` (k0 = 0, 32, 1760, 1792, 3488, 3520), each
+# one DRAM read of its trailing block plus 0.44 MB on average, scaled over the
+# 112 panel launches (the last 512 columns run in one cluster-tail launch).
+# Far below the algorithmic GEMV bytes: the trailing block is re-read from
+# L2, not HBM.
+PANEL_DRAM_BYTES_PER_LAUNCH = 26247568
 
 
 def bench_tall(torch, lib, h, steps):
@@ -596,8 +598,9 @@ def main():
             "achieved": round(achieved, 1) if achieved else None,
             "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / hbm, 3) if achieved else None, "traffic": PANEL_DRAM_BYTES_PER_LAUNCH,
-            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per panel launch, mean over the 112 "
-                            "panel launches of a 4096^2 factorisation (L2 flushed before each launch by ncu); "
+            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per panel launch: six sampled "
+                            "launches (early, middle, late) scaled over the 112 panel launches of a 4096^2 "
+                            "factorisation (L2 flushed before each launch by ncu); "
                             "achieved = the two GEMVs' algorithmic bytes over all columns / the summed time of "
                             "the panel launches and the cluster-tail launch",
             "bytes_per_launch": round(bytes_total / nl), "launches": nl,

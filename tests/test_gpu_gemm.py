@@ -49,3 +49,24 @@ def test_gemm_narrow_output(lib, cuda, mode):
     ref = A.double() @ B.double().T
     C = lib.gemm_nt_device(A, B, mode=mode)
     assert float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref)) <= 5e-6
+
+
+@pytest.mark.parametrize("mode", ["tf32x6", "tf32x3"])
+@pytest.mark.parametrize("M,N,K,beta", [(3000, 1700, 96, 0.0), (3000, 1700, 96, 1.0), (2900, 64, 2048, 0.0),
+                                        (1500, 300, 200, 0.5)])
+def test_gemm_persistent_tiles(lib, cuda, mode, M, N, K, beta):
+    """More tiles (or K slices) than SMs, so every persistent CTA runs several
+    in a row: the stage ring and the accumulator pair carry on across tiles, and
+    the chunked TMA epilogue (beta 0 store, beta 1 reduce-add), the split-K
+    partials (narrow N, long K) and the per-thread update (other beta) all see
+    a CTA's second and later tiles.  Ragged M, N, K."""
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(M + N + K)
+    A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
+    B = torch.rand((N, K), device="cuda", generator=g) * 2 - 1
+    C0 = torch.rand((M, N), device="cuda", generator=g) * 2 - 1
+    ref = beta * C0.double() - (A.double() @ B.double().T)
+    C = lib.gemm_nt_device(A, B, mode=mode, C=C0.clone(), alpha=-1.0, beta=beta)
+    torch.cuda.synchronize()
+    err = float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref))
+    assert err <= (3e-6 if mode == "tf32x6" else 6e-6), err
