@@ -12,23 +12,27 @@
 //                          h*h' + h*m' + m*h' + m*m' + h*l' + l*h'  below FP32
 // (smallest products are issued first).
 //
-// One CTA computes a 128 x BN tile (BN = 128, 64 or 32), 6 warps:
+// A persistent CTA (one per SM) computes 128 x BN tiles (BN = 128, 64 or 32)
+// one after another, 10 warps:
 //   warp 0      TMA producer: raw FP32 K-slabs (32 wide, 128-byte swizzle)
 //               of A and B into a shared-memory ring (3 stages for two
 //               parts, 2 for three);
-//   warps 2-5   split each landed slab in place into its TF32 parts (part 0
+//   warps 2-9   split each landed slab in place into its TF32 parts (part 0
 //               overwrites the raw copy), then release it to the MMA;
 //   warp 1      TMEM allocation and the single MMA-issuing thread:
 //               tcgen05.mma.kind::tf32 over 4 K-steps x (3 or 6) products
 //               per slab into one of two TMEM slab accumulators (fresh per
 //               slab); tcgen05.commit frees the stage and the accumulator;
-//   warps 2-5   drain each slab accumulator with tcgen05.ld (lane = row)
+//   warps 2-9   drain each slab accumulator with tcgen05.ld (lane = row;
+//               two warps per TMEM lane quarter, each half of the columns)
 //               into FP32 registers with round-to-nearest adds -- the tensor
 //               core's own accumulation over many MMAs loses ~2-3 bits
 //               against FP32 FMA chains -- and finally update C (coalesced
-//               along columns of col-major C).
-// Split-K over blockIdx.z writes FP32 partials that a second kernel reduces
-// in a fixed order (deterministic).
+//               along columns of col-major C, or 32-column chunks through
+//               shared memory and one TMA store / reduce-add each).
+// The stage ring and the accumulator pair run on across tiles, so one tile's
+// epilogue overlaps the next tile's loads.  Split-K slices write FP32
+// partials that a second kernel reduces in a fixed order (deterministic).
 //
 // Every mbarrier wait is bounded by wall-clock time; on expiry the CTA
 // records DDCSVD_ERR_TIMEOUT, skips its stores, waits (bounded) for its own
@@ -49,13 +53,13 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BK = 32;  // FP32 elements per slab row: 128 bytes = one swizzle span
-constexpr int THREADS = 192;
-// K slabs accumulated in one TMEM buffer before the epilogue warps drain it
-// into FP32 registers: the tensor core's own accumulation error grows with
-// the number of MMAs it chains (measured: ~linear in K; draining every 4
-// slabs raised the 4096^2 SVD residual from 1.3e-6 to 3.7e-6), so each
-// 32-wide slab is drained and added in FP32 round-to-nearest.
-constexpr int kGroup = 1;
+constexpr int THREADS = 320;  // producer warp, MMA warp, 8 split / drain / epilogue warps
+constexpr int kWorkers = THREADS - 64;
+// Each 32-wide K slab is accumulated in a fresh TMEM buffer and drained by
+// the epilogue warps into FP32 registers: the tensor core's own accumulation
+// error grows with the number of MMAs it chains (measured: ~linear in K;
+// draining every 4 slabs raised the 4096^2 SVD residual from 1.3e-6 to
+// 3.7e-6), so every slab is drained and added in FP32 round-to-nearest.
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 // Bounded wait for the phase of the given parity.  Returns false when the CTA
@@ -146,26 +150,54 @@ struct TcParams {
   int M, N;
   int a_koff, b_koff;  // K coordinate of the first slab in the A / B maps
   int nslab;           // slabs of 32 along K in total
-  int per_split;       // slabs per blockIdx.z
+  int per_split;       // slabs per K slice
+  int ksplit;          // K slices
+  int tiles_m, tiles_n;
   float* C;
   int ldc;
   float alpha, beta;
-  float* partial;  // split-K partials (M x N per split, ld M) or null
+  float* partial;  // split-K partials (M x N per slice, ld M) or null
   int trans;       // store C transposed: element (r, c) at C[c + r * ldc]
   int tma_epi;     // 0: per-thread C update; 1: TMA store (beta 0); 2: TMA reduce-add (beta 1)
   DevStatus* st;
 };
 
+// Shared memory: the stage ring, then two epilogue chunk buffers of BM x 32
+// FP32, then the barriers.
 template <int BN, int NP>
 struct Layout {
   static constexpr int A_BYTES = BM * BK * 4;
   static constexpr int B_BYTES = BN * BK * 4;
   static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
   static constexpr int STAGES = (NP == 2) ? 3 : 2;
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;  // + alignment and barriers
-  static constexpr int TMEM_COLS = 2 * BN;  // two slab accumulators
+  static constexpr int EPI_CHUNK = 32;                  // columns per epilogue chunk
+  static constexpr int EPI_BYTES = BM * EPI_CHUNK * 4;  // one chunk buffer
+  static constexpr int EPI_OFF = STAGES * STAGE;
+  static constexpr int BAR_OFF = EPI_OFF + 2 * EPI_BYTES;
+  static constexpr int SMEM = BAR_OFF + 1024 + 256;     // + alignment and barriers
+  static constexpr int TMEM_COLS = 2 * BN;              // two slab accumulators
 };
 
+// AND of `v` over the 256 threads of warps 2-9 (named barrier 2); every one of
+// them must call it.
+__device__ __forceinline__ bool epi_vote(bool v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.b32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 2, 256, p;\n\t"
+      "selp.s32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((int)v)
+      : "memory");
+  return r != 0;
+}
+
+// Persistent: each CTA takes work items (K slice, N tile, M tile; M fastest)
+// blockIdx.x, blockIdx.x + gridDim.x, ...  The stage ring and the two slab
+// accumulators continue across items, indexed by this CTA's running slab
+// count, so the producer and the MMA issuer run ahead into the next item
+// while the split/epilogue warps write the previous one out.
 template <int BN, int NP>
 __global__ void __launch_bounds__(THREADS, 1)
     tc_gemm_split_tf32_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -174,7 +206,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   constexpr int STAGES = L::STAGES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(round_up(reinterpret_cast<uintptr_t>(smem_raw), 1024));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::STAGE);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
   uint64_t* full = bars;
   uint64_t* conv = bars + STAGES;
   uint64_t* empty = bars + 2 * STAGES;
@@ -187,12 +219,12 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&conv[s], 128);
+      mbar_init(&conv[s], kWorkers);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 128);
+      mbar_init(&acce[b], kWorkers);
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -208,159 +240,215 @@ __global__ void __launch_bounds__(THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-  const int s_begin = blockIdx.z * p.per_split;
-  const int s_end = min(p.nslab, s_begin + p.per_split);
-  const int nsl = max(0, s_end - s_begin);
+  const int items = p.tiles_m * p.tiles_n * p.ksplit;
+  // work item w: m tile, n tile, K slice, first slab and slab count
+  auto item = [&](int w, int& m0, int& n0, int& z, int& s_begin, int& nsl) {
+    const int mt = w % p.tiles_m, rest = w / p.tiles_m;
+    const int nt = rest % p.tiles_n;
+    z = rest / p.tiles_n;
+    m0 = mt * BM;
+    n0 = nt * BN;
+    s_begin = z * p.per_split;
+    nsl = max(0, min(p.nslab, s_begin + p.per_split) - s_begin);
+  };
   // stage layout: A parts 0..NP-1, then B parts 0..NP-1 (part 0 = raw -> hi)
   auto a_part = [&](int s, int k) { return smem + s * L::STAGE + k * L::A_BYTES; };
   auto b_part = [&](int s, int k) { return smem + s * L::STAGE + NP * L::A_BYTES + k * L::B_BYTES; };
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
-      for (int i = 0; i < nsl; i++) {
-        const int s = i % STAGES;
-        if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1, abort_flag, p.st, 901)) break;
-        mbar_arrive_expect_tx(&full[s], L::A_BYTES + L::B_BYTES);
-        const int sl = s_begin + i;
-        tma_load_2d(a_part(s, 0), &tmA, p.a_koff + sl * BK, m0, &full[s]);
-        tma_load_2d(b_part(s, 0), &tmB, p.b_koff + sl * BK, n0, &full[s]);
-        issued = i + 1;
+      int gi = 0;  // this CTA's running slab count
+      bool go = true;
+      for (int w = blockIdx.x; w < items && go; w += gridDim.x) {
+        int m0, n0, z, s_begin, nsl;
+        item(w, m0, n0, z, s_begin, nsl);
+        for (int i = 0; i < nsl; i++, gi++) {
+          const int s = gi % STAGES;
+          if (gi >= STAGES && !mbar_wait(&empty[s], ((gi / STAGES) - 1) & 1, abort_flag, p.st, 901)) {
+            go = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], L::A_BYTES + L::B_BYTES);
+          const int sl = s_begin + i;
+          tma_load_2d(a_part(s, 0), &tmA, p.a_koff + sl * BK, m0, &full[s]);
+          tma_load_2d(b_part(s, 0), &tmB, p.b_koff + sl * BK, n0, &full[s]);
+        }
       }
       // make sure no copy of ours is still landing before the CTA may exit
-      for (int i = max(0, issued - STAGES); i < issued; i++) {
-        const int s = i % STAGES;
+      for (int j = max(0, gi - STAGES); j < gi; j++) {
+        const int s = j % STAGES;
         const unsigned long long t0 = global_ns();
-        while (!mbar_try_wait(&full[s], (i / STAGES) & 1) && global_ns() - t0 < kTcWaitNs) {
+        while (!mbar_try_wait(&full[s], (j / STAGES) & 1) && global_ns() - t0 < kTcWaitNs) {
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BM, BN);
-      for (int i = 0; i < nsl; i++) {
-        const int s = i % STAGES, g = i / kGroup, b = g & 1;
-        const bool gfirst = (i % kGroup) == 0;
-        const bool glast = (i % kGroup) == kGroup - 1 || i == nsl - 1;
-        if (!mbar_wait(&conv[s], (i / STAGES) & 1, abort_flag, p.st, 902)) break;
-        if (gfirst && g >= 2 && !mbar_wait(&acce[b], ((g >> 1) - 1) & 1, abort_flag, p.st, 905)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + (uint32_t)(b * BN);
-#pragma unroll
-        for (int kk = 0; kk < BK / 8; kk++) {
-          const uint32_t off = kk * 32;  // 8 TF32 elements = 32 bytes along K
-          uint64_t da[NP], db[NP];
-#pragma unroll
-          for (int k = 0; k < NP; k++) {
-            da[k] = smem_desc_sw128(smem_u32(a_part(s, k)) + off);
-            db[k] = smem_desc_sw128(smem_u32(b_part(s, k)) + off);
+      int gi = 0;
+      bool go = true;
+      for (int w = blockIdx.x; w < items && go; w += gridDim.x) {
+        int m0, n0, z, s_begin, nsl;
+        item(w, m0, n0, z, s_begin, nsl);
+        for (int i = 0; i < nsl; i++, gi++) {
+          const int s = gi % STAGES, b = gi & 1;
+          if (!mbar_wait(&conv[s], (gi / STAGES) & 1, abort_flag, p.st, 902) ||
+              (gi >= 2 && !mbar_wait(&acce[b], ((gi >> 1) - 1) & 1, abort_flag, p.st, 905))) {
+            go = false;
+            break;
           }
-          const uint32_t first = (kk > 0 || !gfirst) ? 1u : 0u;  // each slab group starts a fresh partial sum
-          if (NP == 3) {  // l*h, h*l, m*m, m*h, h*m, h*h
-            mma_tf32(d, da[2], db[0], idesc, first);
-            mma_tf32(d, da[0], db[2], idesc, 1u);
-            mma_tf32(d, da[1], db[1], idesc, 1u);
-            mma_tf32(d, da[1], db[0], idesc, 1u);
-            mma_tf32(d, da[0], db[1], idesc, 1u);
-            mma_tf32(d, da[0], db[0], idesc, 1u);
-          } else {  // l*h, h*l, h*h
-            mma_tf32(d, da[1], db[0], idesc, first);
-            mma_tf32(d, da[0], db[1], idesc, 1u);
-            mma_tf32(d, da[0], db[0], idesc, 1u);
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(b * BN);
+#pragma unroll
+          for (int kk = 0; kk < BK / 8; kk++) {
+            const uint32_t off = kk * 32;  // 8 TF32 elements = 32 bytes along K
+            uint64_t da[NP], db[NP];
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+              da[k] = smem_desc_sw128(smem_u32(a_part(s, k)) + off);
+              db[k] = smem_desc_sw128(smem_u32(b_part(s, k)) + off);
+            }
+            const uint32_t first = kk > 0 ? 1u : 0u;  // each slab starts a fresh partial sum
+            if (NP == 3) {  // l*h, h*l, m*m, m*h, h*m, h*h
+              mma_tf32(d, da[2], db[0], idesc, first);
+              mma_tf32(d, da[0], db[2], idesc, 1u);
+              mma_tf32(d, da[1], db[1], idesc, 1u);
+              mma_tf32(d, da[1], db[0], idesc, 1u);
+              mma_tf32(d, da[0], db[1], idesc, 1u);
+              mma_tf32(d, da[0], db[0], idesc, 1u);
+            } else {  // l*h, h*l, h*h
+              mma_tf32(d, da[1], db[0], idesc, first);
+              mma_tf32(d, da[0], db[1], idesc, 1u);
+              mma_tf32(d, da[0], db[0], idesc, 1u);
+            }
           }
+          mma_commit(&empty[s]);
+          mma_commit(&accf[b]);
         }
-        mma_commit(&empty[s]);
-        if (glast) mma_commit(&accf[b]);
       }
     }
   } else {
-    // warps 2-5: split landed slabs; drain each slab's partial sum from TMEM
+    // warps 2-9: split landed slabs; drain each slab's partial sum from TMEM
     // into round-to-nearest FP32 registers (the tensor core's own accumulation
-    // across many MMAs is less accurate than FP32 FMA chains)
+    // across many MMAs is less accurate than FP32 FMA chains); write each
+    // finished item out.  Two warps share each TMEM lane quarter (warp % 4):
+    // warps 2-5 hold the tile's first BN/2 columns, warps 6-9 the others.
+    constexpr int HALF = BN / 2;
     const int ct = threadIdx.x - 64;
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int q = warp & 3;         // TMEM lane quarter this warp may access
+    const int h = (warp - 2) >> 2;  // column half
     const uint32_t lane_base = (uint32_t)(q * 32) << 16;
-    float acc[BN];
-#pragma unroll
-    for (int c = 0; c < BN; c++) acc[c] = 0.f;
+    const int rl = q * 32 + lane;  // row of the tile this thread holds
+    float acc[HALF];
     bool ok = true;
-    auto drain = [&](int j) {  // slab group j
-      const int b = j & 1;
-      if (!mbar_wait(&accf[b], (j >> 1) & 1, abort_flag, p.st, 904)) {
+    int gi = 0;
+    // Every decision below is made alike by all 256 threads: tcgen05.ld is
+    // warp-collective and the epilogue's named barriers count all eight warps,
+    // so a wait that one lane gave up on is given up by its whole warp
+    // (__all_sync), and each item's epilogue starts only after a vote of the
+    // eight warps (bar.red.and on barrier 2).
+    auto drain = [&](int g) {  // slab g of this CTA
+      const int b = g & 1;
+      if (!__all_sync(0xffffffffu, mbar_wait(&accf[b], (g >> 1) & 1, abort_flag, p.st, 904))) {
         ok = false;
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 16) {
+      for (int c0 = 0; c0 < HALF; c0 += 16) {
         uint32_t r[16];
-        tmem_ld16(tmem + lane_base + (uint32_t)(b * BN + c0), r);
+        tmem_ld16(tmem + lane_base + (uint32_t)(b * BN + h * HALF + c0), r);
 #pragma unroll
         for (int jj = 0; jj < 16; jj++) acc[c0 + jj] += __uint_as_float(r[jj]);
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(&acce[b]);
     };
-    for (int i = 0; i < nsl && ok; i++) {
-      const int s = i % STAGES;
-      if (!mbar_wait(&full[s], (i / STAGES) & 1, abort_flag, p.st, 903)) {
-        ok = false;
-        break;
+    for (int w = blockIdx.x; w < items && ok; w += gridDim.x) {
+      int m0, n0, z, s_begin, nsl;
+      item(w, m0, n0, z, s_begin, nsl);
+#pragma unroll
+      for (int c = 0; c < HALF; c++) acc[c] = 0.f;
+      for (int i = 0; i < nsl && ok; i++, gi++) {
+        const int s = gi % STAGES;
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (gi / STAGES) & 1, abort_flag, p.st, 903))) {
+          ok = false;
+          break;
+        }
+        split_tile<NP>(reinterpret_cast<float4*>(a_part(s, 0)), reinterpret_cast<float4*>(a_part(s, 1)),
+                       reinterpret_cast<float4*>(a_part(s, NP - 1)), L::A_BYTES / 16, ct, kWorkers);
+        split_tile<NP>(reinterpret_cast<float4*>(b_part(s, 0)), reinterpret_cast<float4*>(b_part(s, 1)),
+                       reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, kWorkers);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&conv[s]);
+        if (i >= 1) drain(gi - 1);
       }
-      split_tile<NP>(reinterpret_cast<float4*>(a_part(s, 0)), reinterpret_cast<float4*>(a_part(s, 1)),
-                     reinterpret_cast<float4*>(a_part(s, NP - 1)), L::A_BYTES / 16, ct, 128);
-      split_tile<NP>(reinterpret_cast<float4*>(b_part(s, 0)), reinterpret_cast<float4*>(b_part(s, 1)),
-                     reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, 128);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&conv[s]);
-      if (i >= kGroup && (i % kGroup) == 0) drain(i / kGroup - 1);
-    }
-    if (ok && nsl >= 1) drain((nsl - 1) / kGroup);
-    // ---------------- epilogue: registers -> C
-    ok = ok && !*abort_flag && nsl > 0;
-    const int row = m0 + q * 32 + lane;
-    if (p.tma_epi && !p.partial) {
-      // alpha * acc -> shared tile [BN cols][BM rows] (the stage buffers are
-      // free: every MMA has completed and every TMA load has landed), then one
-      // thread stores or reduce-adds the tile into C with a single TMA op
-      float* tile = reinterpret_cast<float*>(smem);
-      const int rl = q * 32 + lane;
+      if (ok && nsl >= 1) drain(gi - 1);
+      ok = epi_vote(ok && !*abort_flag);
+      if (!ok) break;
+      if (nsl < 1) continue;
+      // ---------------- epilogue of this item: registers -> C
+      const int row = m0 + rl;
+      const int ch0 = n0 + h * HALF;  // first column this thread holds
+      if (p.tma_epi && !p.partial) {
+        // alpha * acc through the two shared-memory chunk buffers of BM x 32 and
+        // one TMA store or reduce-add per chunk: with BN >= 64 each half fills
+        // its own buffer with 32 of its columns per round; with BN = 32 the
+        // halves share buffer 0.  A round refills the buffers only after the
+        // previous round's copies have read them.
+        constexpr bool OWN = HALF >= L::EPI_CHUNK;
+        constexpr int ROUNDS = OWN ? HALF / L::EPI_CHUNK : 1;
+        constexpr int COLS = OWN ? L::EPI_CHUNK : HALF;  // columns per thread per round
+        float* buf = reinterpret_cast<float*>(smem + L::EPI_OFF + (OWN ? h : 0) * L::EPI_BYTES);
+        const int cofs = OWN ? 0 : h * HALF;  // column offset inside a shared buffer
 #pragma unroll
-      for (int c = 0; c < BN; c++) tile[c * BM + rl] = p.alpha * acc[c];
-      fence_proxy_async_smem();
-      asm volatile("bar.sync 1, 128;" ::: "memory");
-      if (ct == 0 && ok) {
-        if (p.tma_epi == 2) tma_reduce_add_2d(&tmC, tile, m0, n0);
-        else tma_store_2d(&tmC, tile, m0, n0);
-        bulk_commit_and_wait();
-      }
-    } else if (ok && row < p.M) {
+        for (int r = 0; r < ROUNDS; r++) {
+          if (ct == 0) bulk_wait_read_0();
+          asm volatile("bar.sync 1, 256;" ::: "memory");
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        if (p.partial) {
-#pragma unroll
-          for (int jj = 0; jj < 16; jj++) {
-            const int col = n0 + c0 + jj;
-            if (col < p.N) p.partial[(size_t)blockIdx.z * p.M * p.N + row + (size_t)col * p.M] = acc[c0 + jj];
+          for (int c = 0; c < COLS; c++) buf[(cofs + c) * BM + rl] = p.alpha * acc[r * COLS + c];
+          fence_proxy_async_smem();
+          asm volatile("bar.sync 1, 256;" ::: "memory");
+          if (ct == 0) {
+            for (int hb = 0; hb < (OWN ? 2 : 1); hb++) {
+              const int col = n0 + (OWN ? hb * HALF + r * L::EPI_CHUNK : 0);
+              if (col >= p.N) continue;
+              const float* src = reinterpret_cast<const float*>(smem + L::EPI_OFF + hb * L::EPI_BYTES);
+              if (p.tma_epi == 2) tma_reduce_add_2d(&tmC, src, m0, col);
+              else tma_store_2d(&tmC, src, m0, col);
+            }
+            bulk_commit();
           }
-        } else {
-          // 16 independent loads of C in flight, then the 16 updates
-          const size_t rs = p.trans ? (size_t)p.ldc : 1, cs = p.trans ? 1 : (size_t)p.ldc;
-          float old[16];
+        }
+      } else if (row < p.M) {
 #pragma unroll
-          for (int jj = 0; jj < 16; jj++) {
-            const int col = n0 + c0 + jj;
-            old[jj] = (p.beta != 0.f && col < p.N) ? p.C[row * rs + col * cs] : 0.f;
-          }
+        for (int c0 = 0; c0 < HALF; c0 += 16) {
+          if (p.partial) {
 #pragma unroll
-          for (int jj = 0; jj < 16; jj++) {
-            const int col = n0 + c0 + jj;
-            if (col < p.N) p.C[row * rs + col * cs] = p.beta * old[jj] + p.alpha * acc[c0 + jj];
+            for (int jj = 0; jj < 16; jj++) {
+              const int col = ch0 + c0 + jj;
+              if (col < p.N) p.partial[(size_t)z * p.M * p.N + row + (size_t)col * p.M] = acc[c0 + jj];
+            }
+          } else {
+            // 16 independent loads of C in flight, then the 16 updates
+            const size_t rs = p.trans ? (size_t)p.ldc : 1, cs = p.trans ? 1 : (size_t)p.ldc;
+            float old[16];
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+              const int col = ch0 + c0 + jj;
+              old[jj] = (p.beta != 0.f && col < p.N) ? p.C[row * rs + col * cs] : 0.f;
+            }
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+              const int col = ch0 + c0 + jj;
+              if (col < p.N) p.C[row * rs + col * cs] = p.beta * old[jj] + p.alpha * acc[c0 + jj];
+            }
           }
         }
       }
     }
+    // every TMA store / reduce-add of this CTA completes before its shared memory goes away
+    if (ct == 0) bulk_wait_all();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -440,6 +528,7 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   CUtensorMap ma, mb;
   DDC_TRY(make_map(&ma, A, (long long)a_koff + K, M, lda, BM));
   DDC_TRY(make_map(&mb, B, (long long)b_koff + K, N, ldb, BN));
+  static_assert(L::SMEM <= 232448, "tensor-core GEMM shared memory exceeds the opt-in limit");
   static bool attr_set = false;
   if (!attr_set) {
     DDC_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_split_tf32_kernel<BN, NP>,
@@ -467,15 +556,20 @@ static int launch(ddcsvd_context* ctx, int M, int N, int K, const float* A, long
   }
   p.per_split = ceil_div(p.nslab, ksplit);
   ksplit = ceil_div(p.nslab, p.per_split);
+  p.ksplit = ksplit;
+  p.tiles_m = ceil_div(M, BM);
+  p.tiles_n = ceil_div(N, BN);
   p.partial = (ksplit > 1) ? reinterpret_cast<float*>(scratch->base) : nullptr;
-  // C update through one TMA store (beta 0) or reduce-add (beta 1) per tile
+  // C update through TMA stores (beta 0) or reduce-adds (beta 1) of 32-column chunks
   CUtensorMap mc;
   memset(&mc, 0, sizeof(mc));
   p.tma_epi = 0;
   if (!trans && ksplit == 1 && (beta == 0.f || beta == 1.f) && (reinterpret_cast<uintptr_t>(C) & 15) == 0 &&
-      (ldc % 4) == 0 && make_map_c(&mc, C, M, N, ldc, BN) == DDCSVD_OK)
+      (ldc % 4) == 0 && make_map_c(&mc, C, M, N, ldc, L::EPI_CHUNK) == DDCSVD_OK)
     p.tma_epi = (beta == 0.f) ? 1 : 2;
-  dim3 grid(ceil_div(M, BM), ceil_div(N, BN), ksplit);
+  // persistent: one CTA per SM (the shared-memory footprint allows no more), items spread over them
+  const int items = p.tiles_m * p.tiles_n * ksplit;
+  const int grid = std::max(1, std::min(items, ctx->num_sms));
   tc_gemm_split_tf32_kernel<BN, NP><<<grid, THREADS, L::SMEM, ctx->stream>>>(ma, mb, mc, p);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
