@@ -53,13 +53,14 @@ def test_gemm_narrow_output(lib, cuda, mode):
 
 @pytest.mark.parametrize("mode", ["tf32x6", "tf32x3"])
 @pytest.mark.parametrize("M,N,K,beta", [(3000, 1700, 96, 0.0), (3000, 1700, 96, 1.0), (2900, 64, 2048, 0.0),
-                                        (1500, 300, 200, 0.5)])
+                                        (1500, 300, 200, 0.5), (20000, 24, 96, 0.0), (20000, 24, 96, 1.0)])
 def test_gemm_persistent_tiles(lib, cuda, mode, M, N, K, beta):
     """More tiles (or K slices) than SMs, so every persistent CTA runs several
     in a row: the stage ring and the accumulator pair carry on across tiles, and
     the chunked TMA epilogue (beta 0 store, beta 1 reduce-add), the split-K
-    partials (narrow N, long K) and the per-thread update (other beta) all see
-    a CTA's second and later tiles.  Ragged M, N, K."""
+    partials (narrow N, long K), the per-thread update (other beta) and the
+    32-wide tiles (N = 24: 157 tiles of 128 x 32) all see a CTA's second and
+    later tiles.  Ragged M, N, K."""
     torch = cuda
     g = torch.Generator(device="cuda").manual_seed(M + N + K)
     A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
