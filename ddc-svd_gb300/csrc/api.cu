@@ -842,10 +842,15 @@ static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda
     if (at) cudaFreeAsync(at, h->stream);
     if (rc != DDCSVD_OK) break;
     if (cudaMemcpyAsync(S, dS, sizeof(float) * k, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-    if (cudaMemcpy2DAsync(U, sizeof(float) * ldu, dU, sizeof(float) * m, sizeof(float) * m, k,
-                          cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-    if (cudaMemcpy2DAsync(V, sizeof(float) * ldv, dV, sizeof(float) * n, sizeof(float) * n, k,
-                          cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    // packed host layouts leave as one contiguous copy each, strided ones row block by row block
+    auto out2d = [&](float* dst, int ld, const float* src, int rows) {
+      return ld == rows
+                 ? cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)rows * k, cudaMemcpyDeviceToHost, h->stream)
+                 : cudaMemcpy2DAsync(dst, sizeof(float) * ld, src, sizeof(float) * rows, sizeof(float) * rows, k,
+                                     cudaMemcpyDeviceToHost, h->stream);
+    };
+    if (out2d(U, ldu, dU, m) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    if (out2d(V, ldv, dV, n) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
   } while (0);
   cudaFreeAsync(dA, h->stream);

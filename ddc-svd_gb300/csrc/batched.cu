@@ -44,10 +44,12 @@ __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 // count instead of a chain through all of them: every thread forms the
 // total, so its latency sits on each column step), the same tree in every
 // thread.  `red` holds 2 * (blockDim.x / 32) floats; blockDim.x / 32 <= 16.
+// No thread may still read `red` from an earlier sum when this one starts:
+// the caller alternates two buffers with CTA barriers between their uses, so
+// the partials are written without a barrier first.
 __device__ __forceinline__ FF cta_sum_ff(FF v, float* red) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   v = warp_sum_ff(v);
-  __syncthreads();
   if (lane == 0) {
     red[2 * wid] = v.hi;
     red[2 * wid + 1] = v.lo;
@@ -87,13 +89,17 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
     if (t == 0) {
       d[i] = alpha;
       tq[i] = tauq;
-      M[i + (size_t)i * ld] = 1.f;
     }
-    for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
-    __syncthreads();
-    if (i == n - 1) break;
+    if (i == n - 1) {  // last column: no update, only the reflector form
+      if (t == 0) M[i + (size_t)i * ld] = 1.f;
+      for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
+      break;
+    }
     // ---- left update of columns > i (left_dotprods + left_update_mat):
-    // four columns per warp at a time against the reflector held in registers
+    // four columns per warp at a time against the reflector held in registers.
+    // The reflector is formed from the stored column as u_i = 1, u_r = sq x_r
+    // (the same products the stored form would hold); column i is rewritten
+    // in that form only after the update, so no barrier precedes it.
     if (tauq != 0.f) {
       const float* uc = M + (size_t)i * ld;
       if (m - i <= 32 * kColRegs) {
@@ -101,7 +107,7 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
 #pragma unroll
         for (int k = 0; k < kColRegs; k++) {
           const int r = i + lane + 32 * k;
-          u[k] = (r < m) ? uc[r] : 0.f;
+          u[k] = (r < m) ? (r == i ? 1.f : uc[r] * sq) : 0.f;
         }
         for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
           float w[4];
@@ -138,18 +144,21 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
         for (int c = i + 1 + wid; c < n; c += nw) {
           float* col = M + (size_t)c * ld;
           float w = 0.f;
-          for (int r = i + lane; r < m; r += 32) w += uc[r] * col[r];
+          for (int r = i + lane; r < m; r += 32) w += (r == i ? 1.f : uc[r] * sq) * col[r];
           w = warp_sum(w) * tauq;
-          for (int r = i + lane; r < m; r += 32) col[r] -= w * uc[r];
+          for (int r = i + lane; r < m; r += 32) col[r] -= w * (r == i ? 1.f : uc[r] * sq);
         }
       }
     }
     __syncthreads();
+    // column i in reflector form (no later step of this problem reads it)
+    if (t == 0) M[i + (size_t)i * ld] = 1.f;
+    for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
     // ---- right reflector from row i
     const float y0 = M[i + (size_t)(i + 1) * ld];
     FF r2{0.f, 0.f};
     for (int c = i + 2 + t; c < n; c += blockDim.x) r2 = ff_add_sq(r2, M[i + (size_t)c * ld]);
-    r2 = cta_sum_ff(r2, red);
+    r2 = cta_sum_ff(r2, red + 32);
     float beta, taup, sp;
     if (i < n - 2) {
       householder_ff(y0, r2, &beta, &taup, &sp);
