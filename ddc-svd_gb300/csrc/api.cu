@@ -227,7 +227,7 @@ static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda,
                 : svd_core_impl(ctx, m, n, dA, lda, dS, dU, ldu, dV, ldv, mode, check_finite);
   const int lu = (int)round_up(m, 4), lv = (int)round_up(n, 4);
   float* buf = nullptr;
-  DDC_CUDA_TRY(cudaMallocAsync((void**)&buf, sizeof(float) * ((size_t)lu * n + (size_t)lv * n + 64), ctx->stream));
+  DDC_CUDA_TRY(pool_alloc(ctx, &buf, sizeof(float) * ((size_t)lu * n + (size_t)lv * n + 64)));
   float* Ui = buf;
   float* Vi = buf + (size_t)lu * n + 32;
   int rc = tall ? svd_tall_qr(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite)
@@ -393,9 +393,9 @@ static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int l
   QrWork qw;
   plan_qr(plan, m, n, P, kind, &qw);
   char* buf = nullptr;
-  if (cudaMallocAsync((void**)&buf, plan.off + 4096, ctx->stream) != cudaSuccess) {
+  if (pool_alloc(ctx, &buf, plan.off + 4096) != cudaSuccess) {
     cudaGetLastError();
-    set_last_error("cudaMallocAsync of %zu bytes for the QR path failed", plan.off + 4096);
+    set_last_error("device allocation of %zu bytes for the QR path failed", plan.off + 4096);
     return DDCSVD_ERR_ALLOC;
   }
   Arena a;
@@ -504,6 +504,15 @@ static int create_ctx(ddcsvd_context** out, int device) {
   c->smem_optin = prop.sharedMemPerBlockOptin;
   DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->own_stream = true;
+  {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    DDC_CUDA_TRY(cudaMemPoolCreate(&c->pool, &props));
+    unsigned long long keep = ~0ull;
+    DDC_CUDA_TRY(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   DDC_CUDA_TRY(cudaMalloc(&c->d_status, sizeof(DevStatus)));
   DDC_CUDA_TRY(cudaMallocHost(&c->h_status, sizeof(DevStatus)));
   for (int k = 0; k < 5; k++) DDC_CUDA_TRY(cudaEventCreate(&c->ev[k]));
@@ -561,6 +570,7 @@ int ddcsvd_destroy(ddcsvd_handle_t h) {
   if (h->h_status) cudaFreeHost(h->h_status);
   for (int k = 0; k < 5; k++) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
   if (h->own_stream) cudaStreamDestroy(h->stream);
+  if (h->pool) cudaMemPoolDestroy(h->pool);
   delete h;
   return DDCSVD_OK;
 }
@@ -585,6 +595,7 @@ int ddcsvd_release_workspace(ddcsvd_handle_t h) {
   if (h->ws) cudaFree(h->ws);
   h->ws = nullptr;
   h->ws_bytes = 0;
+  if (h->pool) cudaMemPoolTrimTo(h->pool, 0);
   return DDCSVD_OK;
 }
 
@@ -644,7 +655,7 @@ int ddcsvd_svd_f32_device(ddcsvd_handle_t h, int m, int n, const float* dA, int 
   float* at = nullptr;
   if (m < n) {
     // A^T scratch lives in its own allocation so the pipeline workspace stays intact
-    DDC_CUDA_TRY(cudaMallocAsync((void**)&at, sizeof(float) * (size_t)m * n, h->stream));
+    DDC_CUDA_TRY(pool_alloc(h, &at, sizeof(float) * (size_t)m * n));
   }
   int rc = svd_device(h, m, n, dA, lda, dSigma, dU, ldu, dV, ldv, mode, at);
   if (at) cudaFreeAsync(at, h->stream);
@@ -786,7 +797,7 @@ int ddcsvd_bdvec_device(ddcsvd_handle_t h, int N, const double* dA, const double
   std::lock_guard<std::mutex> g(h->mu);
   DDC_CUDA_TRY(cudaSetDevice(h->device));
   double* scratch_sorted = nullptr;
-  DDC_CUDA_TRY(cudaMallocAsync((void**)&scratch_sorted, sizeof(double) * N, h->stream));
+  DDC_CUDA_TRY(pool_alloc(h, &scratch_sorted, sizeof(double) * N));
   int rc = bd_standalone(h, N, dA, dB, true, dSigma, scratch_sorted, dX, dY);
   cudaFreeAsync(scratch_sorted, h->stream);
   return rc;
@@ -824,7 +835,7 @@ static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda
   const int k = std::min(m, n);
   float *dA = nullptr, *dS = nullptr, *dU = nullptr, *dV = nullptr;
   const size_t na = (size_t)m * n, nu = (size_t)m * k, nv = (size_t)n * k;
-  DDC_CUDA_TRY(cudaMallocAsync((void**)&dA, sizeof(float) * (na + k + nu + nv + 64), h->stream));
+  DDC_CUDA_TRY(pool_alloc(h, &dA, sizeof(float) * (na + k + nu + nv + 64)));
   dS = dA + na;
   dU = dS + k;
   dV = dU + nu;
@@ -837,7 +848,7 @@ static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda
                             cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
     }
     float* at = nullptr;
-    if (m < n && cudaMallocAsync((void**)&at, sizeof(float) * na, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+    if (m < n && pool_alloc(h, &at, sizeof(float) * na) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
     rc = svd_device(h, m, n, dA, m, dS, dU, m, dV, n, mode, at);
     if (at) cudaFreeAsync(at, h->stream);
     if (rc != DDCSVD_OK) break;
@@ -928,8 +939,8 @@ void bidiag_par(int m, int n, double* A, double* alpha, double* beta) {
     float* dW = nullptr;
     double* dOut = nullptr;
     do {
-      if (cudaMallocAsync((void**)&dW, sizeof(float) * ((size_t)ldw * nc + 4 * (size_t)nc + 64), h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
-      if (cudaMallocAsync((void**)&dOut, sizeof(double) * na, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+      if (pool_alloc(h, &dW, sizeof(float) * ((size_t)ldw * nc + 4 * (size_t)nc + 64)) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
+      if (pool_alloc(h, &dOut, sizeof(double) * na) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
       float* dd = dW + (size_t)ldw * nc;
       float* de = dd + nc;
       float* tq = de + nc;
@@ -991,8 +1002,8 @@ static int form_factor_host(int m, int n, const double* A_mod, double* Q, bool l
   const size_t na = (size_t)m * n, nq = (size_t)rows * rows, ns = left ? 0 : (size_t)n * n;
   double* buf = nullptr;
   int rc = DDCSVD_OK;
-  if (cudaMallocAsync((void**)&buf, sizeof(double) * (na + nq + ns + 16), h->stream) != cudaSuccess) {
-    set_last_error("cudaMallocAsync of %zu bytes failed", sizeof(double) * (na + nq + ns + 16));
+  if (pool_alloc(h, &buf, sizeof(double) * (na + nq + ns + 16)) != cudaSuccess) {
+    set_last_error("device allocation of %zu bytes failed", sizeof(double) * (na + nq + ns + 16));
     return DDCSVD_ERR_ALLOC;
   }
   double* dA = buf;

@@ -77,6 +77,10 @@ struct PanelParams {
   int rpt4;
   float* xpart;
   int ldxp;
+  // two-GEMV form with more rows than shared memory holds next to the panel
+  // blocks: y = A^T u reads the column from xcol (global, L2-resident)
+  // instead of a staged copy, and the staging buffer holds only the row
+  int ucol_global;
 };
 
 __device__ __forceinline__ float sgn_ref(float x) { return x < 0.f ? -1.f : 1.f; }
@@ -101,14 +105,19 @@ __device__ __forceinline__ void householder(float x0, double t2, float* alpha, f
 // sum_{r in [r0, r1)} col[r] * xs[r]; col in global (16B-aligned base), xs in
 // shared memory indexed absolutely.  Warp-cooperative, result in all lanes.
 // Eight 16-byte loads per lane are kept in flight.
+// kGlobalX: xs is in global memory, written by other CTAs since this kernel
+// started (read through L2, bypassing L1); otherwise shared memory.
+template <bool kGlobalX = false>
 __device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, const float* xs, int r0,
                                               int r1, int lane) {
   float acc = 0.f;
   if (r1 <= r0) return 0.f;
   int a0 = min(r1, (r0 + 3) & ~3);
   int a1 = max(a0, r1 & ~3);
-  if (lane < a0 - r0) acc += __ldcg(col + r0 + lane) * xs[r0 + lane];
-  if (lane < r1 - a1) acc += __ldcg(col + a1 + lane) * xs[a1 + lane];
+  auto xl = [&](int r) { return kGlobalX ? __ldcg(xs + r) : xs[r]; };
+  auto xl4 = [&](const float4* v) { return kGlobalX ? __ldcg(v) : *v; };
+  if (lane < a0 - r0) acc += __ldcg(col + r0 + lane) * xl(r0 + lane);
+  if (lane < r1 - a1) acc += __ldcg(col + a1 + lane) * xl(a1 + lane);
   const float4* c4 = reinterpret_cast<const float4*>(col + a0);
   const float4* x4 = reinterpret_cast<const float4*>(xs + a0);
   const int nq = (a1 - a0) >> 2;
@@ -119,13 +128,13 @@ __device__ __forceinline__ float warp_dot_col(const float* __restrict__ col, con
     for (int u = 0; u < 8; u++) w[u] = __ldcg(c4 + q + 32 * u);
 #pragma unroll
     for (int u = 0; u < 8; u++) {
-      const float4 v = x4[q + 32 * u];
+      const float4 v = xl4(x4 + q + 32 * u);
       acc += w[u].x * v.x + w[u].y * v.y + w[u].z * v.z + w[u].w * v.w;
     }
   }
   for (; q < nq; q += 32) {
     float4 w0 = __ldcg(c4 + q);
-    float4 v0 = x4[q];
+    float4 v0 = xl4(x4 + q);
     acc += w0.x * v0.x + w0.y * v0.y + w0.z * v0.z + w0.w * v0.w;
   }
   return warp_sum(acc);
@@ -489,8 +498,8 @@ __device__ PanelSmem carve(float* smem, int bigsz, int rc, int cc, int P, bool f
   return s;
 }
 
-size_t panel_smem_bytes(int m, int n, int rc, int cc, int threads, int P, bool fused) {
-  size_t f = round_up(std::max(m, n) + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
+size_t panel_smem_bytes(int bigsz, int rc, int cc, int threads, int P, bool fused) {
+  size_t f = round_up(bigsz + 4, 4) + 4 * threads + round_up(rc + 4, 4) + round_up(cc + 4, 4) +
              round_up(cc * 8 + 4, 4) + 2 * (size_t)rc * kLD + 2 * (size_t)cc * kLD +
              round_up(std::max(rc, cc) + 4, 4) + 8 + 8 * (kPanel + 4) + kPS + 4 + 4 +
              64 + 8 + (size_t)(threads / 32) * (kPS + 4) + 4;
@@ -507,7 +516,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
   const int m = p.m, n = p.n, k0 = p.k0, ldw = p.ldw, ldn = p.ldn;
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
   constexpr bool fx = kRpt4 > 0;
-  PanelSmem S = carve(smem, max(m, n), p.rc, p.cc, p.P, fx);
+  PanelSmem S = carve(smem, p.ucol_global ? n : max(m, n), p.rc, p.cc, p.P, fx);
   float* W = p.W;
   float *X = p.X, *Y = p.Y, *VT = p.VT;
   // static partitions for this panel
@@ -584,7 +593,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
       }
       if (t == 64) x0v = __ldcg(p.xcol + i);
       const bool stage = i < n - 1;
-      const int sa = (i + 1) & ~3, snv = stage ? (m - sa + 3) >> 2 : 0;
+      const int sa = (i + 1) & ~3, snv = (stage && !p.ucol_global) ? (m - sa + 3) >> 2 : 0;
       const float4* src4 = reinterpret_cast<const float4*>(p.xcol + sa);
       float4* dst4 = reinterpret_cast<float4*>(S.big + sa);
       const int nt = blockDim.x;
@@ -683,7 +692,8 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         for (int item = wid; item < ncol * segs; item += nw) {
           const int cl = item / segs, sg = item % segs;
           const int r0 = i + 1 + sg * seglen, r1 = min(m, r0 + seglen);
-          float v = warp_dot_col(W + (size_t)(c_s + cl) * ldw, S.big, r0, r1, lane);
+          float v = p.ucol_global ? warp_dot_col<true>(W + (size_t)(c_s + cl) * ldw, p.xcol, r0, r1, lane)
+                                  : warp_dot_col(W + (size_t)(c_s + cl) * ldw, S.big, r0, r1, lane);
           if (lane == 0) S.ypart[cl * 8 + sg] = v;
         }
         __syncthreads();
@@ -1275,8 +1285,18 @@ int bidiag_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* 
       pp.xpart = w.xpart;
       pp.ldxp = w.ldxp;
     }
+    size_t smem = panel_smem_bytes(std::max(m, n), pp.rc, pp.cc, kBidiagThreads, P, pp.rpt4 > 0);
+    pp.ucol_global = 0;
+    if (smem > ctx->smem_optin && pp.rpt4 == 0) {
+      pp.ucol_global = 1;
+      smem = panel_smem_bytes(n, pp.rc, pp.cc, kBidiagThreads, P, false);
+    }
+    if (smem > ctx->smem_optin) {
+      set_last_error("bidiagonalisation panel of %d x %d needs %zu bytes of shared memory per CTA (limit %zu): "
+                     "too many rows for the direct path", m - k0, n - k0, smem, ctx->smem_optin);
+      return DDCSVD_ERR_ARG;
+    }
     DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
-    const size_t smem = panel_smem_bytes(m, n, pp.rc, pp.cc, kBidiagThreads, P, pp.rpt4 > 0);
     ktimer_begin(ctx, KC_BIDIAG);
     const void* kfn = pp.rpt4 == 1   ? (const void*)bidiag_panel_kernel<1>
                       : pp.rpt4 == 2 ? (const void*)bidiag_panel_kernel<2>
@@ -1331,6 +1351,11 @@ int bidiag_plain(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* d,
   DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
   size_t smem = (round_up(std::max(m, n) + 4, 4) + 4 * kBidiagThreads + round_up(pp.rc + 4, 4) +
                  round_up(pp.cc + 4, 4) + 4 + 64 + 16) * sizeof(float) + 64;
+  if (smem > ctx->smem_optin) {
+    set_last_error("the plain FP32 path stages a %d-entry column in shared memory (%zu bytes, limit %zu): "
+                   "too many rows", std::max(m, n), smem, ctx->smem_optin);
+    return DDCSVD_ERR_ARG;
+  }
   ktimer_begin(ctx, KC_BIDIAG);
   int rc = launch_coop((const void*)bidiag_plain_kernel, w.P, kBidiagThreads, smem, &pp, ctx->stream);
   ktimer_end(ctx);
@@ -1394,8 +1419,13 @@ int qr_blocked(ddcsvd_context* ctx, int m, int n, float* W, int ldw, float* tau,
       q.rc = (int)round_up(ceil_div(m - (k0 & ~3), w.P), 4);
       q.W = W; q.tau = tau; q.Vp = w.Vp + off + (size_t)off * w.ldv; q.ldv = w.ldv;
       q.part = w.part; q.rowi = w.rowi; q.bar = w.bar; q.st = ctx->d_status;
-      DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
       ktimer_begin(ctx, KC_QR);
+      if (qr_smem_bytes(q.rc, kBidiagThreads) > ctx->smem_optin) {
+        set_last_error("QR panel of %d rows needs %zu bytes of shared memory per CTA (limit %zu): too many rows",
+                       m - k0, qr_smem_bytes(q.rc, kBidiagThreads), ctx->smem_optin);
+        return DDCSVD_ERR_ARG;
+      }
+      DDC_CUDA_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), ctx->stream));
       DDC_TRY(launch_coop((const void*)qr_panel_kernel, w.P, kBidiagThreads, qr_smem_bytes(q.rc, kBidiagThreads), &q,
                           ctx->stream));
       ktimer_end(ctx);

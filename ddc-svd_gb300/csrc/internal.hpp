@@ -39,6 +39,11 @@ struct ddcsvd_context {
   // of them changes the arithmetic beyond the summation order of split-K and
   // of the D&C lane groups
   int tune[8] = {16, 0, 512, 1, 8, 2, 1, 512};
+  // the handle's own stream-ordered memory pool (per-call buffers: host-API
+  // staging, QR-path blocks, aligned U/V copies); it keeps what it reserved
+  // between calls (release threshold unlimited), so a repeated call maps no
+  // new pages; ddcsvd_release_workspace trims it
+  cudaMemPool_t pool = nullptr;
   // limits (ddcsvd_set_limits): FP64 secular iterations per root, the
   // wall-clock limit of device waits (us, 0 = the built-in 4 s), the
   // workspace budget (bytes, 0 = none), and the fault-injection count of
@@ -53,6 +58,13 @@ struct ddcsvd_context {
 };
 
 namespace ddcsvd {
+// A per-call device buffer from the handle's pool, ordered on its stream
+// (released with cudaFreeAsync on the same stream).
+template <typename T>
+inline cudaError_t pool_alloc(ddcsvd_context* c, T** p, size_t bytes) {
+  return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, c->pool, c->stream);
+}
+
 enum TuneKnob {
   TK_SPLITK_MAX = 0,     // cap on split-K pieces of the GEMMs (1 = no split)
   TK_TC_BN = 1,          // tensor-core tile width: 0 = by N (64 if N <= 64 else 128), 64 = always 64

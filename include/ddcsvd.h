@@ -102,15 +102,18 @@ int ddcsvd_svd_f32(int m, int n, const float *A, int lda, float *sigma, float *U
 
 /* ---------------------------------------------------------------- handles and device API */
 
-/* A handle owns a CUDA stream, a device workspace and pinned staging memory
- * on one device.  Calls on one handle are serialised; use one handle per
+/* A handle owns a CUDA stream, a device workspace, a stream-ordered memory
+ * pool and pinned staging memory on one device.  Calls on one handle are serialised; use one handle per
  * host thread for concurrency.  device < 0 selects the current device. */
 int ddcsvd_create(ddcsvd_handle_t *handle, int device);
 int ddcsvd_destroy(ddcsvd_handle_t handle);
 /* Work of this handle goes to `stream` (a cudaStream_t; NULL = the legacy default stream).
  * A new handle starts on a private non-blocking stream. */
 int ddcsvd_set_stream(ddcsvd_handle_t handle, void *stream);
-/* Frees the cached device workspace (it regrows on the next call). */
+/* Frees the cached device workspace and returns the memory that the
+ * handle's own stream-ordered pool keeps between calls (per-call buffers of
+ * the host API, the QR path and aligned output copies); both regrow on the
+ * next call. */
 int ddcsvd_release_workspace(ddcsvd_handle_t handle);
 
 /* Full SVD, device pointers (FP32).  The call is asynchronous on the

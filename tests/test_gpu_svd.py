@@ -187,12 +187,14 @@ def test_svd_large_shapes(lib, cuda, orc, m, n):
 
 
 @pytest.mark.parametrize("m,n,kind", [(600, 256, "uniform"), (1200, 200, "graded"), (256, 700, "uniform"),
-                                      (2048, 130, "rank_deficient"), (1001, 300, "uniform"), (4100, 1030, "graded")])
+                                      (2048, 130, "rank_deficient"), (1001, 300, "uniform"), (4100, 1030, "graded"),
+                                      (40000, 160, "uniform")])
 def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
     """m >= 2n (or n >= 2m) in the tensor-core modes goes through Householder
     QR, the SVD of R and U = Q [U_R; 0].  QR works in 128-column super-blocks
     of 32-column panels: 200, 300 and 1030 columns end in partial super-blocks
-    and partial panels; 1001 rows are not a multiple of 4."""
+    and partial panels; 1001 rows are not a multiple of 4; 40000 rows put 264
+    rows in each CTA of the panel kernel."""
     if not _mode_available(lib, "tf32x6"):
         pytest.skip("tf32x6 unavailable")
     rng = np.random.default_rng(m + 7 * n)
@@ -210,12 +212,16 @@ def test_svd_tall_qr_path(lib, cuda, orc, m, n, kind):
 
 
 @pytest.mark.parametrize("fused", [0, 1])
-@pytest.mark.parametrize("m,n", [(1023, 517), (2050, 2050), (8200, 100)])
+@pytest.mark.parametrize("m,n", [(1023, 517), (2050, 2050), (8200, 100), (40001, 96)])
 def test_panel_one_pass_and_two_gemv_forms(lib, cuda, orc, fused, m, n):
     """The panel kernel's one-read form (knob panel_fused = 1, the default up to
     8192 rows) and its two-GEMV form meet the same bounds.  Row counts that are
     not multiples of 4 exercise the ragged last float4; with 8200 rows the first
-    panel runs the two-GEMV form and the later ones the one-read form."""
+    panel runs the two-GEMV form and the later ones the one-read form.  With
+    40001 rows the staged column no longer fits shared memory beside the panel
+    blocks, and y = A^T u reads it from global memory (both knob settings)."""
+    if fused == 0 and m > 10000:
+        pytest.skip("the same two-GEMV form as the fused setting at this size")
     mode = "tf32x6" if _mode_available(lib, "tf32x6") else "blocked"
     rng = np.random.default_rng(m * 13 + n + fused)
     A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
@@ -537,3 +543,28 @@ def test_host_f32_api(lib, cuda, orc):
     A = rng.uniform(-1, 1, (150, 90)).astype(np.float32)
     s, U, V = lib.svd(A)
     check_metrics(orc, A, s.astype(np.float64), U.astype(np.float64), V.astype(np.float64))
+
+
+@pytest.mark.parametrize("mode,m,n,tall_qr", [("plain", 60000, 8, 0), ("tf32x6", 262144, 128, 1),
+                                              ("tf32x6", 262144, 128, 0)])
+def test_row_limits_report_arg(lib, cuda, mode, m, n, tall_qr):
+    """Beyond the rows that the panel kernels hold in shared memory (plain
+    FP32 path: the whole column, ~56K rows; QR and direct panels: a 1/152
+    slice of the rows times 33 floats, ~250K rows) a call fails with
+    DDCSVD_ERR_ARG and a message naming the limit, and the handle still
+    gives correct results afterwards."""
+    if mode == "tf32x6" and not _mode_available(lib, mode):
+        pytest.skip("tf32x6 unavailable")
+    A = cuda.zeros((m, n), dtype=cuda.float32, device="cuda")
+    A[:n, :n] = cuda.eye(n, device="cuda")
+    h = lib.Handle()
+    h.tuning = {"tall_qr": tall_qr}
+    with pytest.raises(lib.DdcsvdError) as ei:
+        lib.svd_device(A, mode=mode, handle=h)
+    assert ei.value.status == 1
+    assert "too many rows" in str(ei.value)
+    cuda.cuda.synchronize()
+    B = np.random.default_rng(9).uniform(-1, 1, (300, 200)).astype(np.float32)
+    s, U, V = lib.svd_device(cuda.from_numpy(B).cuda(), mode=mode, handle=h)
+    st = np.sort(np.linalg.svd(B.astype(np.float64), compute_uv=False))
+    assert np.max(np.abs(s.double().cpu().numpy() - st)) <= TOL * st[-1]
