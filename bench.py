@@ -265,11 +265,15 @@ def cpu_baseline(A64_host: np.ndarray, budget_s: float = 20.0):
 PANEL_DRAM_BYTES_PER_LAUNCH = 26247568
 
 
-def bench_tall(torch, lib, h, steps):
+def bench_tall(torch, lib, steps):
     """Thin SVD of the tall configuration: 16384 x 8192 FP32, entries N(0, 1)
     from a seeded generator (rng(2)); residual and orthogonality in FP32 on
-    the GPU (no FP64 reference of this size is formed)."""
+    the GPU (no FP64 reference of this size is formed).  Its own handle,
+    with the launch knobs the library's autotuner picks for this shape
+    (untimed), as a user tuning per shape would have."""
     m, n = 16384, 8192
+    h = lib.Handle()
+    tuning = h.autotune_svd(m, n, mode="tf32x6", reps=1)
     rng = np.random.default_rng(2)
     A = torch.from_numpy(rng.standard_normal((n, m), dtype=np.float32)).cuda()  # column-major m x n
     bufs = (torch.empty(n, device="cuda"), torch.empty((n, m), device="cuda"), torch.empty((n, n), device="cuda"))
@@ -299,7 +303,8 @@ def bench_tall(torch, lib, h, steps):
     ms = float(np.mean(ts))
     del A, bufs
     torch.cuda.empty_cache()
-    return {"m": m, "n": n, "mode": "tf32x6", "ms": round(ms, 2),
+    h.close()
+    return {"m": m, "n": n, "mode": "tf32x6", "ms": round(ms, 2), "tuning": tuning,
             "gflops": round(svd_flops(m, n) / (ms * 1e-3) / 1e9, 1),
             "kernel_ms": dict(zip(["bidiag_kernels", "trailing_gemm", "dc", "vectors", "backxform", "qr"],
                                   [round(x, 3) for x in kms])),
@@ -585,7 +590,7 @@ def main():
     batched = (bench_batched(torch, lib, h, max(3, args.steps), flush, dist, world, rank, peaks)
                if not args.quick else None)
     adjoint = bench_adjoint(torch, lib, h, max(3, args.steps), peaks) if not args.quick else None
-    tall = bench_tall(torch, lib, h, 2) if not args.quick else None
+    tall = bench_tall(torch, lib, 2) if not args.quick else None
 
     # roofline of the dominant kernel class (bidiagonalisation GEMV kernels)
     hbm, peak_kind = measured_peaks()

@@ -614,6 +614,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
         return v;
       };
       reduce_partials(p.colpart, p.P, 2 * j + 1, S.redp, S.tot, S.nrm, [&]() {
+        PMARK(14);
         if (t < j) {
           S.Wi[t] = wi;
           S.Xi[t] = xi;
@@ -781,6 +782,7 @@ __global__ void __launch_bounds__(kBidiagThreads, 1) bidiag_panel_kernel(PanelPa
 #pragma unroll
       for (int u = 0; u < kXR; u++) xv[u] = (t + u * nt < nxi) ? xload(t + u * nt) : make_float4(0.f, 0.f, 0.f, 0.f);
       reduce_partials(p.rowpart, p.P, 2 * j + 2, S.redp, S.tot, S.nrm, [&]() {
+        PMARK(15);
         if (t == 64) S.misc[1] = x1v;
         if (t >= 96 && t < 96 + j + 1) S.Yi[t - 96] = yiv;
         if (t >= 160 && t < 160 + j) S.VTi[t - 160] = vtv;

@@ -178,6 +178,19 @@ struct Layout {
   static constexpr int TMEM_COLS = 2 * BN;              // two slab accumulators
 };
 
+// phase marks (trace builds): CTA 0, one row per slab of the CTA (first 128)
+#ifdef DDCSVD_PHASE_TRACE
+__device__ unsigned long long g_gemm_trace[128 * 16];
+#define GMARK(cond, g, slot)                                                        \
+  do {                                                                              \
+    if ((cond) && blockIdx.x == 0 && (g) < 128) g_gemm_trace[(g) * 16 + (slot)] = global_ns(); \
+  } while (0)
+#else
+#define GMARK(cond, g, slot) \
+  do {                       \
+  } while (0)
+#endif
+
 // AND of `v` over the 256 threads of warps 2-9 (named barrier 2); every one of
 // them must call it.
 __device__ __forceinline__ bool epi_vote(bool v) {
@@ -268,6 +281,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             go = false;
             break;
           }
+          GMARK(true, gi, 0);
           mbar_arrive_expect_tx(&full[s], L::A_BYTES + L::B_BYTES);
           const int sl = s_begin + i;
           tma_load_2d(a_part(s, 0), &tmA, p.a_koff + sl * BK, m0, &full[s]);
@@ -298,6 +312,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          GMARK(true, gi, 3);
           const uint32_t d = tmem + (uint32_t)(b * BN);
 #pragma unroll
           for (int kk = 0; kk < BK / 8; kk++) {
@@ -324,6 +339,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           mma_commit(&empty[s]);
           mma_commit(&accf[b]);
+          GMARK(true, gi, 4);
         }
       }
     }
@@ -354,6 +370,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      GMARK(ct == 0, g, 5);
 #pragma unroll
       for (int c0 = 0; c0 < HALF; c0 += 16) {
         uint32_t r[16];
@@ -363,6 +380,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(&acce[b]);
+      GMARK(ct == 0, g, 6);
     };
     for (int w = blockIdx.x; w < items && ok; w += gridDim.x) {
       int m0, n0, z, s_begin, nsl;
@@ -375,12 +393,14 @@ __global__ void __launch_bounds__(THREADS, 1)
           ok = false;
           break;
         }
+        GMARK(ct == 0, gi, 1);
         split_tile<NP>(reinterpret_cast<float4*>(a_part(s, 0)), reinterpret_cast<float4*>(a_part(s, 1)),
                        reinterpret_cast<float4*>(a_part(s, NP - 1)), L::A_BYTES / 16, ct, kWorkers);
         split_tile<NP>(reinterpret_cast<float4*>(b_part(s, 0)), reinterpret_cast<float4*>(b_part(s, 1)),
                        reinterpret_cast<float4*>(b_part(s, NP - 1)), L::B_BYTES / 16, ct, kWorkers);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&conv[s]);
+        GMARK(ct == 0, gi, 2);
         if (i >= 1) drain(gi - 1);
       }
       if (ok && nsl >= 1) drain(gi - 1);
@@ -388,6 +408,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok) break;
       if (nsl < 1) continue;
       // ---------------- epilogue of this item: registers -> C
+      GMARK(ct == 0, gi - 1, 7);
       const int row = m0 + rl;
       const int ch0 = n0 + h * HALF;  // first column this thread holds
       if (p.tma_epi && !p.partial) {
@@ -446,6 +467,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
       }
+      GMARK(ct == 0, gi - 1, 8);
     }
     // every TMA store / reduce-add of this CTA completes before its shared memory goes away
     if (ct == 0) bulk_wait_all();
@@ -647,3 +669,9 @@ int gemm_tc(ddcsvd_context* ctx, GemmKind kind, int M, int N, int K1, Mat A1, Ma
 }
 
 }  // namespace ddcsvd
+
+#ifdef DDCSVD_PHASE_TRACE
+extern "C" int ddcsvd_gemm_trace_read(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, ddcsvd::tc::g_gemm_trace, sizeof(ddcsvd::tc::g_gemm_trace));
+}
+#endif
