@@ -39,33 +39,6 @@ constexpr int kBatchBidiagThreads = 512;  // bidiagonalisation CTAs (one per SM,
 
 __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 
-// Compensated CTA-wide sum; every thread gets the same value.  The warp
-// partials are added as a fixed pairwise tree (depth log2 of the warp
-// count instead of a chain through all of them: every thread forms the
-// total, so its latency sits on each column step), the same tree in every
-// thread.  `red` holds 2 * (blockDim.x / 32) floats; blockDim.x / 32 <= 16.
-// No thread may still read `red` from an earlier sum when this one starts:
-// the caller alternates two buffers with CTA barriers between their uses, so
-// the partials are written without a barrier first.
-__device__ __forceinline__ FF cta_sum_ff(FF v, float* red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = warp_sum_ff(v);
-  if (lane == 0) {
-    red[2 * wid] = v.hi;
-    red[2 * wid + 1] = v.lo;
-  }
-  __syncthreads();
-  auto ld = [&](int k) { return k < nw ? FF{red[2 * k], red[2 * k + 1]} : FF{0.f, 0.f}; };
-  FF w[8];
-#pragma unroll
-  for (int k = 0; k < 8; k++) w[k] = ff_add(ld(k), ld(k + 8));
-#pragma unroll
-  for (int h = 4; h > 0; h >>= 1)
-#pragma unroll
-    for (int k = 0; k < h; k++) w[k] = ff_add(w[k], w[k + h]);
-  return w[0];
-}
-
 constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m - i <= 256)
 
 // Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA
@@ -73,23 +46,32 @@ constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m 
 // rank-1 update, then right reflector and rank-1 update, per column).
 // Reflectors stay in M in LAPACK form (unit leading entry stored).  Norms are
 // compensated FP32 sums and the reflector scalars FP32 (the caller keeps
-// max|M| in [2^-40, 2^40]); every thread forms them from the same reduced
-// value, so no broadcast round is needed.
+// max|M| in [2^-40, 2^40]).  A problem has at most 256 rows, so warp 0 alone
+// forms each reflector (norm, scalars, and for the right one the scaled row)
+// and hands the scalars to the other warps through `sh` across the barrier
+// that the update needs anyway: four CTA barriers per column, and the
+// reduction and the scalar arithmetic run once instead of in every warp.
 __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, float* tq, float* tp,
-                           float* vrow, float* red, int iend) {
+                           float* vrow, float* sh, int iend) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
   for (int i = 0; i < iend; i++) {
-    // ---- left reflector from column i
-    const float x0 = M[i + (size_t)i * ld];
-    FF s2{0.f, 0.f};
-    for (int r = i + 1 + t; r < m; r += blockDim.x) s2 = ff_add_sq(s2, M[r + (size_t)i * ld]);
-    s2 = cta_sum_ff(s2, red);
-    float alpha, tauq, sq;
-    householder_ff(x0, s2, &alpha, &tauq, &sq);
-    if (t == 0) {
-      d[i] = alpha;
-      tq[i] = tauq;
+    // ---- left reflector from column i (warp 0)
+    if (wid == 0) {
+      const float x0 = M[i + (size_t)i * ld];
+      FF s2{0.f, 0.f};
+      for (int r = i + 1 + lane; r < m; r += 32) s2 = ff_add_sq(s2, M[r + (size_t)i * ld]);
+      s2 = warp_sum_ff(s2);
+      float alpha, tauq, sq;
+      householder_ff(x0, s2, &alpha, &tauq, &sq);
+      if (lane == 0) {
+        d[i] = alpha;
+        tq[i] = tauq;
+        sh[0] = tauq;
+        sh[1] = sq;
+      }
     }
+    __syncthreads();
+    const float tauq = sh[0], sq = sh[1];
     if (i == n - 1) {  // last column: no update, only the reflector form
       if (t == 0) M[i + (size_t)i * ld] = 1.f;
       for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
@@ -151,34 +133,36 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
       }
     }
     __syncthreads();
-    // column i in reflector form (no later step of this problem reads it)
+    // column i in reflector form (no later step of this problem reads it);
+    // warp 0 meanwhile forms the right reflector from row i (disjoint entries)
     if (t == 0) M[i + (size_t)i * ld] = 1.f;
     for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
-    // ---- right reflector from row i
-    const float y0 = M[i + (size_t)(i + 1) * ld];
-    FF r2{0.f, 0.f};
-    for (int c = i + 2 + t; c < n; c += blockDim.x) r2 = ff_add_sq(r2, M[i + (size_t)c * ld]);
-    r2 = cta_sum_ff(r2, red + 32);
-    float beta, taup, sp;
-    if (i < n - 2) {
-      householder_ff(y0, r2, &beta, &taup, &sp);
-    } else {  // one element left: no reflection (bidiag.c:125-129)
-      beta = y0;
-      taup = 0.f;
-      sp = 0.f;
-    }
-    if (t == 0) {
-      e[i] = beta;
-      tp[i] = taup;
-    }
-    for (int c = i + 1 + t; c < n; c += blockDim.x) {
-      float v;
-      if (c == i + 1) v = (taup != 0.f) ? 1.f : 0.f;
-      else v = M[i + (size_t)c * ld] * sp;
-      M[i + (size_t)c * ld] = v;
-      vrow[c] = v;
+    if (wid == 0) {
+      const float y0 = M[i + (size_t)(i + 1) * ld];
+      FF r2{0.f, 0.f};
+      for (int c = i + 2 + lane; c < n; c += 32) r2 = ff_add_sq(r2, M[i + (size_t)c * ld]);
+      r2 = warp_sum_ff(r2);
+      float beta, taup, sp;
+      if (i < n - 2) {
+        householder_ff(y0, r2, &beta, &taup, &sp);
+      } else {  // one element left: no reflection (bidiag.c:125-129)
+        beta = y0;
+        taup = 0.f;
+        sp = 0.f;
+      }
+      if (lane == 0) {
+        e[i] = beta;
+        tp[i] = taup;
+        sh[2] = taup;
+      }
+      for (int c = i + 1 + lane; c < n; c += 32) {
+        const float v = (c == i + 1) ? ((taup != 0.f) ? 1.f : 0.f) : M[i + (size_t)c * ld] * sp;
+        M[i + (size_t)c * ld] = v;
+        vrow[c] = v;
+      }
     }
     __syncthreads();
+    const float taup = sh[2];
     // ---- right update of rows > i (right_dotprods + right_update_mat):
     // two threads per row (alternate columns, partial dots joined by one
     // shuffle) while the rows fit, so every thread works (more threads per
@@ -214,7 +198,7 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
                                                                      float* tp, int smem_floats, int maxn) {
   extern __shared__ __align__(16) float sm[];
   __shared__ int s_task;
-  __shared__ float red[64];
+  __shared__ float red[4];  // reflector scalars handed from warp 0 to the CTA
   __shared__ unsigned s_amax;
   float* vrow = sm;                 // maxn
   float* Ms = sm + ((maxn + 3) & ~3);  // problem copy when it fits
