@@ -41,20 +41,49 @@ __device__ __forceinline__ float bsgn(float x) { return x < 0.f ? -1.f : 1.f; }
 
 constexpr int kColRegs = 8;  // rows per lane of the register-held reflector (m - i <= 256)
 
+// phase marks (trace builds): CTA 0; rows 0-63 the first 64 columns of its
+// first problem (slots 0-4: column start, after each of the four barriers),
+// rows 64-127 its problems in turn (slot 0 start, 1 end, 2 m, 3 n)
+#ifdef DDCSVD_PHASE_TRACE
+__device__ unsigned long long g_batch_trace[128 * 16];
+#define BMARK(row, slot, val)                                                         \
+  do {                                                                                \
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (row) < 128) g_batch_trace[(row) * 16 + (slot)] = (val); \
+  } while (0)
+#else
+#define BMARK(row, slot, val) \
+  do {                        \
+  } while (0)
+#endif
+
 // Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA
 // (the reference's bidiag_seq order, bidiag.c:33-186: left reflector and
 // rank-1 update, then right reflector and rank-1 update, per column).
 // Reflectors stay in M in LAPACK form (unit leading entry stored).  Norms are
 // compensated FP32 sums and the reflector scalars FP32 (the caller keeps
-// max|M| in [2^-40, 2^40]).  A problem has at most 256 rows, so warp 0 alone
-// forms each reflector (norm, scalars, and for the right one the scaled row)
-// and hands the scalars to the other warps through `sh` across the barrier
-// that the update needs anyway: four CTA barriers per column, and the
-// reduction and the scalar arithmetic run once instead of in every warp.
+// max|M| in [2^-40, 2^40]).  Warp 0 alone forms each reflector (norm,
+// scalars, and for the right one the scaled row) and hands the scalars to
+// the other warps through `sh` across the barrier that the update needs
+// anyway: four CTA barriers per column.
+//
+// While the trailing rows fit the warps' registers (m - i <= 256) the left
+// update and the right reflector's products share one pass over the block:
+// a warp holds four columns of it in registers, updates them, and with the
+// new row-i values w_c (c >= i + 2) accumulates sum_c a'_rc w_c for its
+// rows; the right update then forms z_r = a'_{r,i+1} + sp * sum_c a'_rc w_c
+// (v_{i+1} = 1, v_c = sp w_c) instead of a second pass of dot products.
+// `zs` holds the warps' partial sums (blockDim.x / 32 rows of 256) and their
+// totals (256 more).
 __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, float* tq, float* tp,
-                           float* vrow, float* sh, int iend) {
+                           float* vrow, float* zs, float* sh, int iend, bool trace = false) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
+  constexpr int kZRows = 32 * kColRegs;
+  float* zsum = zs + nw * kZRows;
+  (void)trace;
   for (int i = 0; i < iend; i++) {
+    const bool tr = trace && i < 64;
+    (void)tr;
+    BMARK(tr ? i : 999, 0, global_ns());
     // ---- left reflector from column i (warp 0)
     if (wid == 0) {
       const float x0 = M[i + (size_t)i * ld];
@@ -71,40 +100,44 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
       }
     }
     __syncthreads();
+    BMARK(tr ? i : 999, 1, global_ns());
     const float tauq = sh[0], sq = sh[1];
     if (i == n - 1) {  // last column: no update, only the reflector form
       if (t == 0) M[i + (size_t)i * ld] = 1.f;
       for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
       break;
     }
-    // ---- left update of columns > i (left_dotprods + left_update_mat):
-    // four columns per warp at a time against the reflector held in registers.
+    // ---- left update of columns > i (left_dotprods + left_update_mat).
     // The reflector is formed from the stored column as u_i = 1, u_r = sq x_r
     // (the same products the stored form would hold); column i is rewritten
     // in that form only after the update, so no barrier precedes it.
-    if (tauq != 0.f) {
-      const float* uc = M + (size_t)i * ld;
-      if (m - i <= 32 * kColRegs) {
-        float u[kColRegs];
+    const bool merged = m - i <= kZRows;
+    const float* uc = M + (size_t)i * ld;
+    if (merged) {
+      float u[kColRegs], zp[kColRegs];
 #pragma unroll
-        for (int k = 0; k < kColRegs; k++) {
-          const int r = i + lane + 32 * k;
-          u[k] = (r < m) ? (r == i ? 1.f : uc[r] * sq) : 0.f;
-        }
-        for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
+      for (int k = 0; k < kColRegs; k++) {
+        const int r = i + lane + 32 * k;
+        u[k] = (r < m) ? (r == i ? 1.f : uc[r] * sq) : 0.f;
+        zp[k] = 0.f;
+      }
+      for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
+        float a[4][kColRegs];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+          for (int k = 0; k < kColRegs; k++) {
+            const int r = i + lane + 32 * k;
+            a[q][k] = (c0 + q < n && r < m) ? M[r + (size_t)(c0 + q) * ld] : 0.f;
+          }
+        if (tauq != 0.f) {
           float w[4];
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            float a = 0.f;
-            if (c0 + q < n) {
-              const float* col = M + (size_t)(c0 + q) * ld;
+            float s = 0.f;
 #pragma unroll
-              for (int k = 0; k < kColRegs; k++) {
-                const int r = i + lane + 32 * k;
-                if (r < m) a += u[k] * col[r];
-              }
-            }
-            w[q] = a;
+            for (int k = 0; k < kColRegs; k++) s += u[k] * a[q][k];
+            w[q] = s;
           }
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1)
@@ -112,31 +145,51 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
             for (int q = 0; q < 4; q++) w[q] += __shfl_xor_sync(0xffffffffu, w[q], o);
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            if (c0 + q >= n) continue;
-            float* col = M + (size_t)(c0 + q) * ld;
             const float f = w[q] * tauq;
 #pragma unroll
-            for (int k = 0; k < kColRegs; k++) {
-              const int r = i + lane + 32 * k;
-              if (r < m) col[r] -= f * u[k];
+            for (int k = 0; k < kColRegs; k++) a[q][k] -= f * u[k];
+            if (c0 + q < n) {
+              float* col = M + (size_t)(c0 + q) * ld;
+#pragma unroll
+              for (int k = 0; k < kColRegs; k++) {
+                const int r = i + lane + 32 * k;
+                if (r < m) col[r] = a[q][k];
+              }
             }
           }
         }
-      } else {
-        for (int c = i + 1 + wid; c < n; c += nw) {
-          float* col = M + (size_t)c * ld;
-          float w = 0.f;
-          for (int r = i + lane; r < m; r += 32) w += (r == i ? 1.f : uc[r] * sq) * col[r];
-          w = warp_sum(w) * tauq;
-          for (int r = i + lane; r < m; r += 32) col[r] -= w * (r == i ? 1.f : uc[r] * sq);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float wc = __shfl_sync(0xffffffffu, a[q][0], 0);  // new a_{i,c}
+          if (c0 + q >= i + 2 && c0 + q < n)
+#pragma unroll
+            for (int k = 0; k < kColRegs; k++) zp[k] += a[q][k] * wc;
         }
+      }
+#pragma unroll
+      for (int k = 0; k < kColRegs; k++) zs[wid * kZRows + lane + 32 * k] = zp[k];
+    } else if (tauq != 0.f) {
+      for (int c = i + 1 + wid; c < n; c += nw) {
+        float* col = M + (size_t)c * ld;
+        float w = 0.f;
+        for (int r = i + lane; r < m; r += 32) w += (r == i ? 1.f : uc[r] * sq) * col[r];
+        w = warp_sum(w) * tauq;
+        for (int r = i + lane; r < m; r += 32) col[r] -= w * (r == i ? 1.f : uc[r] * sq);
       }
     }
     __syncthreads();
+    BMARK(tr ? i : 999, 2, global_ns());
     // column i in reflector form (no later step of this problem reads it);
-    // warp 0 meanwhile forms the right reflector from row i (disjoint entries)
+    // warp 0 meanwhile forms the right reflector from row i (disjoint
+    // entries), and every thread adds the warps' partial products of its rows
     if (t == 0) M[i + (size_t)i * ld] = 1.f;
     for (int r = i + 1 + t; r < m; r += blockDim.x) M[r + (size_t)i * ld] *= sq;
+    if (merged)
+      for (int rr = 1 + t; rr < m - i; rr += blockDim.x) {
+        float z = 0.f;
+        for (int w = 0; w < nw; w++) z += zs[w * kZRows + rr];
+        zsum[rr] = z;
+      }
     if (wid == 0) {
       const float y0 = M[i + (size_t)(i + 1) * ld];
       FF r2{0.f, 0.f};
@@ -154,6 +207,7 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
         e[i] = beta;
         tp[i] = taup;
         sh[2] = taup;
+        sh[3] = sp;
       }
       for (int c = i + 1 + lane; c < n; c += 32) {
         const float v = (c == i + 1) ? ((taup != 0.f) ? 1.f : 0.f) : M[i + (size_t)c * ld] * sp;
@@ -162,32 +216,43 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
       }
     }
     __syncthreads();
-    const float taup = sh[2];
+    BMARK(tr ? i : 999, 3, global_ns());
+    const float taup = sh[2], sp = sh[3];
     // ---- right update of rows > i (right_dotprods + right_update_mat):
-    // two threads per row (alternate columns, partial dots joined by one
-    // shuffle) while the rows fit, so every thread works (more threads per
-    // row measured slower: shuffles and shared-memory bank conflicts)
+    // two threads per row (alternate columns) while the rows fit, so every
+    // thread works (more threads per row measured slower: shuffles and
+    // shared-memory bank conflicts)
     if (taup != 0.f) {
       if (2 * (m - i - 1) <= (int)blockDim.x) {
         const int r = i + 1 + (t >> 1), h = t & 1;
         const bool act = r < m;
         float z = 0.f;
-        if (act)
-          for (int c = i + 1 + h; c < n; c += 2) z += M[r + (size_t)c * ld] * vrow[c];
-        z += __shfl_xor_sync(0xffffffffu, z, 1);
+        if (merged) {
+          if (act) z = M[r + (size_t)(i + 1) * ld] + sp * zsum[r - i];
+          __syncwarp();  // both threads of the row read a_{r,i+1} before it changes
+        } else {
+          if (act)
+            for (int c = i + 1 + h; c < n; c += 2) z += M[r + (size_t)c * ld] * vrow[c];
+          z += __shfl_xor_sync(0xffffffffu, z, 1);
+        }
         z *= taup;
         if (act)
           for (int c = i + 1 + h; c < n; c += 2) M[r + (size_t)c * ld] -= z * vrow[c];
       } else {
         for (int r = i + 1 + t; r < m; r += blockDim.x) {
           float z = 0.f;
-          for (int c = i + 1; c < n; c++) z += M[r + (size_t)c * ld] * vrow[c];
+          if (merged) {
+            z = M[r + (size_t)(i + 1) * ld] + sp * zsum[r - i];
+          } else {
+            for (int c = i + 1; c < n; c++) z += M[r + (size_t)c * ld] * vrow[c];
+          }
           z *= taup;
           for (int c = i + 1; c < n; c++) M[r + (size_t)c * ld] -= z * vrow[c];
         }
       }
     }
     __syncthreads();
+    BMARK(tr ? i : 999, 4, global_ns());
   }
 }
 
@@ -200,8 +265,12 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
   __shared__ int s_task;
   __shared__ float red[4];  // reflector scalars handed from warp 0 to the CTA
   __shared__ unsigned s_amax;
-  float* vrow = sm;                 // maxn
-  float* Ms = sm + ((maxn + 3) & ~3);  // problem copy when it fits
+  float* vrow = sm;                                   // maxn
+  float* zs = sm + ((maxn + 3) & ~3);  // right products: warps x 256 partials + 256 totals
+  float* Ms = zs + ((blockDim.x >> 5) + 1) * 32 * kColRegs;  // problem copy when it fits
+#ifdef DDCSVD_PHASE_TRACE
+  int pcount = 0;
+#endif
   while (true) {
     if (threadIdx.x == 0) s_task = atomicAdd(counter, 1);
     __syncthreads();
@@ -210,6 +279,15 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
     if (q >= ntask) break;
     const BatchTask T = tasks[order[q]];
     const int m = T.m, n = T.n, ld = m;
+#ifdef DDCSVD_PHASE_TRACE
+    const int prow = 64 + pcount;
+    const bool first = pcount == 0;
+    BMARK(prow, 0, global_ns());
+    BMARK(prow, 2, (unsigned long long)m);
+    BMARK(prow, 3, (unsigned long long)n);
+#else
+    const bool first = false;
+#endif
     const bool fits = (long long)m * n <= smem_floats;
     // a problem beyond the shared memory: columns [0, k0) run in global memory
     // until the trailing block fits (k0 = n: none fits)
@@ -238,18 +316,18 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
       for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) M[(idx % m) + (size_t)(idx / m) * ld] *= sc;
     __syncthreads();
     if (fits || k0 >= n) {
-      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, n);
+      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, zs, red, n, first);
     } else {
       // the first k0 columns in global memory, then the (m - k0) x (n - k0)
       // trailing block (the only part later columns touch) in shared memory
-      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, red, k0);
+      cta_bidiag(M, ld, m, n, d + T.offD, e + T.offD, tq + T.offD, tp + T.offD, vrow, zs, red, k0);
       __syncthreads();
       const int mt = m - k0, nt = n - k0;
       for (int idx = threadIdx.x; idx < mt * nt; idx += blockDim.x)
         Ms[idx] = Wg[(k0 + idx % mt) + (size_t)(k0 + idx / mt) * ld];
       __syncthreads();
-      cta_bidiag(Ms, mt, mt, nt, d + T.offD + k0, e + T.offD + k0, tq + T.offD + k0, tp + T.offD + k0, vrow, red,
-                 nt);
+      cta_bidiag(Ms, mt, mt, nt, d + T.offD + k0, e + T.offD + k0, tq + T.offD + k0, tp + T.offD + k0, vrow, zs,
+                 red, nt);
       __syncthreads();
       for (int idx = threadIdx.x; idx < mt * nt; idx += blockDim.x)
         Wg[(k0 + idx % mt) + (size_t)(k0 + idx / mt) * ld] = Ms[idx];
@@ -265,6 +343,10 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
     if (fits)
       for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) Wg[idx] = M[idx];
     __syncthreads();
+#ifdef DDCSVD_PHASE_TRACE
+    BMARK(prow, 1, global_ns());
+    pcount++;
+#endif
   }
 }
 
@@ -516,11 +598,11 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   const int smem_floats = 24 * 1024;
   int max_optin = 0;
   DDC_CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-  const int vrow_floats = (int)((maxn + 3) & ~3);
+  const int bthreads = (h->tune[TK_BATCH_THREADS] == 256) ? 256 : kBatchBidiagThreads;
+  const int vrow_floats = (int)((maxn + 3) & ~3) + (bthreads / 32 + 1) * 32 * kColRegs;
   const int bidiag_floats = h->tune[TK_BATCH_SMEM_FULL]
                                 ? std::max(1024, (max_optin - 2048) / (int)sizeof(float) - vrow_floats)
                                 : smem_floats;
-  const int bthreads = (h->tune[TK_BATCH_THREADS] == 256) ? 256 : kBatchBidiagThreads;
   const size_t smem = sizeof(float) * ((size_t)vrow_floats + bidiag_floats);
   DDC_CUDA_TRY(cudaFuncSetAttribute(batch_bidiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
@@ -594,3 +676,9 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   if (h->timing && rc == DDCSVD_OK) ktimer_collect(h);
   return rc;
 }
+
+#ifdef DDCSVD_PHASE_TRACE
+extern "C" int ddcsvd_batch_trace_read(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, ddcsvd::g_batch_trace, sizeof(ddcsvd::g_batch_trace));
+}
+#endif
