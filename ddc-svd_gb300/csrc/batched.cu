@@ -351,19 +351,24 @@ __global__ void __launch_bounds__(kBatchBidiagThreads) batch_bidiag_kernel(const
 }
 
 // Applies reflectors j = jhi-1 ... 0 to kCW columns held in registers (lane
-// owns rows lane + 32 k).  Reflector j is the vector v(r) = vec(j, r) for
-// rows r >= j + shift (unit leading entry stored), zero above.
-constexpr int kRowsPerLane = 8;  // register-resident columns: rows <= 256
-constexpr int kCW = 8;           // columns per warp at a time
-template <typename VecFn>
-__device__ __forceinline__ void apply_reflectors_regs(float (&c)[kCW][kRowsPerLane], int rows, int jhi, int shift,
+// owns rows lane + 32 k, k < KR).  Reflector j is the vector v(r) = vec(j, r)
+// for rows r >= j + shift (unit leading entry stored), zero above.  KR is the
+// problem's row count in 32-row slices (1, 2, 4 or 8), so small problems do
+// not multiply zeros.  The kCW dot products of a reflector are summed over
+// the warp by a reduce-scatter (4 + 2 + 1 shuffles leave each lane a partial
+// of one column over 8 lanes, 2 more complete it) and a gather of the 8
+// sums (17 shuffles instead of 5 per column).
+constexpr int kCW = 8;  // columns per warp at a time
+template <int KR, typename VecFn>
+__device__ __forceinline__ void apply_reflectors_regs(float (&c)[kCW][KR], int rows, int jhi, int shift,
                                                       const float* __restrict__ tau, VecFn vec, int lane) {
+  const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
   for (int j = jhi - 1; j >= 0; j--) {
     const float t = tau[j];
     if (t == 0.f) continue;
-    float u[kRowsPerLane];
+    float u[KR];
 #pragma unroll
-    for (int k = 0; k < kRowsPerLane; k++) {
+    for (int k = 0; k < KR; k++) {
       const int r = lane + 32 * k;
       u[k] = (r >= j + shift && r < rows) ? vec(j, r) : 0.f;
     }
@@ -372,36 +377,101 @@ __device__ __forceinline__ void apply_reflectors_regs(float (&c)[kCW][kRowsPerLa
     for (int q = 0; q < kCW; q++) {
       float a = 0.f;
 #pragma unroll
-      for (int k = 0; k < kRowsPerLane; k++) a += u[k] * c[q][k];
+      for (int k = 0; k < KR; k++) a += u[k] * c[q][k];
       d[q] = a;
     }
+    float e4[4], e2[2];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < 4; q++)
+      e4[q] = (b16 ? d[q + 4] : d[q]) + __shfl_xor_sync(0xffffffffu, b16 ? d[q] : d[q + 4], 16);
 #pragma unroll
-      for (int q = 0; q < kCW; q++) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
+    for (int q = 0; q < 2; q++)
+      e2[q] = (b8 ? e4[q + 2] : e4[q]) + __shfl_xor_sync(0xffffffffu, b8 ? e4[q] : e4[q + 2], 8);
+    float g = (b4 ? e2[1] : e2[0]) + __shfl_xor_sync(0xffffffffu, b4 ? e2[0] : e2[1], 4);
+    g += __shfl_xor_sync(0xffffffffu, g, 2);
+    g += __shfl_xor_sync(0xffffffffu, g, 1);
+    // lane l now holds the sum of column 4 b16 + 2 b8 + b4
 #pragma unroll
     for (int q = 0; q < kCW; q++) {
-      const float f = t * d[q];
+      const float f = t * __shfl_sync(0xffffffffu, g, ((q >> 2) & 1) * 16 + ((q >> 1) & 1) * 8 + (q & 1) * 4);
 #pragma unroll
-      for (int k = 0; k < kRowsPerLane; k++) c[q][k] -= f * u[k];
+      for (int k = 0; k < KR; k++) c[q][k] -= f * u[k];
     }
   }
 }
 
+// Left side of one problem up to 256 rows: U_core = Q [Y; 0], kCW columns per
+// warp at a time in registers, left reflectors n-1 .. 0 (column j of R).
+template <int KR>
+__device__ void bx_left(float* Uc, int m, int n, const float* R, const float* tauq, int lane, int wid, int nw) {
+  for (int c0 = wid * kCW; c0 < n; c0 += nw * kCW) {
+    float c[kCW][KR];
+#pragma unroll
+    for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = lane + 32 * k, col = c0 + qq;
+        c[qq][k] = (col < n && r < n) ? Uc[r + (size_t)col * m] : 0.f;
+      }
+    apply_reflectors_regs<KR>(c, m, n, 0, tauq, [&](int j, int r) { return R[r + (size_t)j * m]; }, lane);
+#pragma unroll
+    for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = lane + 32 * k, col = c0 + qq;
+        if (col < n && r < m) Uc[r + (size_t)col * m] = c[qq][k];
+      }
+  }
+}
+
+// Right side: V_core = P X, right reflectors n-3 .. 0 (row j of R from column j+1).
+template <int KR>
+__device__ void bx_right(float* Vc, int m, int n, const float* R, const float* taup, int lane, int wid, int nw) {
+  for (int c0 = wid * kCW; c0 < n; c0 += nw * kCW) {
+    float c[kCW][KR];
+#pragma unroll
+    for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = lane + 32 * k, col = c0 + qq;
+        c[qq][k] = (col < n && r < n) ? Vc[r + (size_t)col * n] : 0.f;
+      }
+    apply_reflectors_regs<KR>(c, n, n - 2, 1, taup, [&](int j, int k) { return R[j + (size_t)k * m]; }, lane);
+#pragma unroll
+    for (int qq = 0; qq < kCW; qq++)
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = lane + 32 * k, col = c0 + qq;
+        if (col < n && r < n) Vc[r + (size_t)col * n] = c[qq][k];
+      }
+  }
+}
+
+__device__ __forceinline__ int row_slices(int rows) { return rows <= 32 ? 1 : rows <= 64 ? 2 : rows <= 128 ? 4 : 8; }
+
 // U_core = Q [Y; 0], V_core = P X for one problem per CTA (multU / multV).
-// Problems up to 256 rows keep kCW columns per warp in registers and read the
-// reflectors from shared memory (or L1): one warp-wide reduction per
-// reflector for kCW columns at once.  Larger problems use the plain column
-// loop (one column per warp, in global memory).
+// Persistent CTAs take problems largest first from an atomic counter over the
+// size-sorted order (a static round robin left the largest problems to the
+// last wave).  Problems up to 256 rows keep kCW columns per warp in
+// registers, sized to the problem's rows, and read the reflectors from
+// shared memory (or L1): one warp-wide reduction per reflector for kCW
+// columns at once.  Larger problems use the plain column loop (one column
+// per warp, in global memory).
 __global__ void __launch_bounds__(kBatchThreads) batch_backxform_kernel(const BatchTask* __restrict__ tasks,
-                                                                        int ntask, const float* __restrict__ W,
+                                                                        const int* __restrict__ order, int ntask,
+                                                                        int* counter, const float* __restrict__ W,
                                                                         const float* __restrict__ tq,
                                                                         const float* __restrict__ tp, float* U,
                                                                         float* V, int smem_floats) {
   extern __shared__ __align__(16) float sm[];
+  __shared__ int s_task;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int q = blockIdx.x; q < ntask; q += gridDim.x) {
-    const BatchTask T = tasks[q];
+  while (true) {
+    if (threadIdx.x == 0) s_task = atomicAdd(counter, 1);
+    __syncthreads();
+    const int qi = s_task;
+    if (qi >= ntask) break;
+    const BatchTask T = tasks[order[qi]];
     const int m = T.m, n = T.n;
     const bool fits = (long long)m * n <= smem_floats;
     const float* Wg = W + T.offW;
@@ -414,41 +484,18 @@ __global__ void __launch_bounds__(kBatchThreads) batch_backxform_kernel(const Ba
     __syncthreads();
     const float* tauq = tq + T.offD;
     const float* taup = tp + T.offD;
-    if (m <= 32 * kRowsPerLane) {
-      for (int c0 = wid * kCW; c0 < n; c0 += nw * kCW) {
-        float c[kCW][kRowsPerLane];
-        // U: columns of [Y; 0] (rows >= n are zero), left reflectors n-1 .. 0
-#pragma unroll
-        for (int qq = 0; qq < kCW; qq++)
-#pragma unroll
-          for (int k = 0; k < kRowsPerLane; k++) {
-            const int r = lane + 32 * k, col = c0 + qq;
-            c[qq][k] = (col < n && r < n) ? Uc[r + (size_t)col * m] : 0.f;
-          }
-        apply_reflectors_regs(c, m, n, 0, tauq, [&](int j, int r) { return R[r + (size_t)j * m]; }, lane);
-#pragma unroll
-        for (int qq = 0; qq < kCW; qq++)
-#pragma unroll
-          for (int k = 0; k < kRowsPerLane; k++) {
-            const int r = lane + 32 * k, col = c0 + qq;
-            if (col < n && r < m) Uc[r + (size_t)col * m] = c[qq][k];
-          }
-        // V: columns of X, right reflectors n-3 .. 0 (row j of R from column j+1)
-#pragma unroll
-        for (int qq = 0; qq < kCW; qq++)
-#pragma unroll
-          for (int k = 0; k < kRowsPerLane; k++) {
-            const int r = lane + 32 * k, col = c0 + qq;
-            c[qq][k] = (col < n && r < n) ? Vc[r + (size_t)col * n] : 0.f;
-          }
-        apply_reflectors_regs(c, n, n - 2, 1, taup, [&](int j, int k) { return R[j + (size_t)k * m]; }, lane);
-#pragma unroll
-        for (int qq = 0; qq < kCW; qq++)
-#pragma unroll
-          for (int k = 0; k < kRowsPerLane; k++) {
-            const int r = lane + 32 * k, col = c0 + qq;
-            if (col < n && r < n) Vc[r + (size_t)col * n] = c[qq][k];
-          }
+    if (m <= 256) {
+      switch (row_slices(m)) {
+        case 1: bx_left<1>(Uc, m, n, R, tauq, lane, wid, nw); break;
+        case 2: bx_left<2>(Uc, m, n, R, tauq, lane, wid, nw); break;
+        case 4: bx_left<4>(Uc, m, n, R, tauq, lane, wid, nw); break;
+        default: bx_left<8>(Uc, m, n, R, tauq, lane, wid, nw); break;
+      }
+      switch (row_slices(n)) {
+        case 1: bx_right<1>(Vc, m, n, R, taup, lane, wid, nw); break;
+        case 2: bx_right<2>(Vc, m, n, R, taup, lane, wid, nw); break;
+        case 4: bx_right<4>(Vc, m, n, R, taup, lane, wid, nw); break;
+        default: bx_right<8>(Vc, m, n, R, taup, lane, wid, nw); break;
       }
     } else {
       // rows n..m-1 of [Y; 0]
@@ -590,7 +637,7 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   DDC_CUDA_TRY(cudaMemcpyAsync(dt, pin, sizeof(BatchTask) * batch, cudaMemcpyHostToDevice, h->stream));
   DDC_CUDA_TRY(cudaMemcpyAsync(dord, pin + sizeof(BatchTask) * batch, sizeof(int) * batch, cudaMemcpyHostToDevice,
                                h->stream));
-  DDC_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), h->stream));
+  DDC_CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(int), h->stream));  // stage 1 and stage 5 work counters
   // ---- stage 1: persistent CTAs over the size-sorted work list
   // stage 1 keeps a problem in shared memory when it fits the SM's opt-in
   // maximum (up to ~56K entries: all but the largest 256 x 2xx problems);
@@ -665,8 +712,11 @@ extern "C" int ddcsvd_svd_batched_f32_device(ddcsvd_handle_t h, int batch, const
   DDC_CUDA_TRY(cudaFuncSetAttribute(batch_backxform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)std::max<size_t>(smem5, 16)));
   ktimer_begin(h, KC_BACKXFORM);
-  batch_backxform_kernel<<<std::min(batch, 8 * h->num_sms), kBatchThreads, smem5, h->stream>>>(dt, batch, W, tq, tp,
-                                                                                             dU, dV, smem_floats);
+  int occ5 = 1;
+  DDC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ5, batch_backxform_kernel, kBatchThreads,
+                                                            std::max<size_t>(smem5, 16)));
+  batch_backxform_kernel<<<std::min(batch, h->num_sms * std::max(occ5, 1)), kBatchThreads, smem5, h->stream>>>(
+      dt, dord, batch, counter + 1, W, tq, tp, dU, dV, smem_floats);
   count_launch();
   ktimer_end(h);
   batch_sigma_out_kernel<<<std::min(batch, 1024), 128, 0, h->stream>>>(dt, batch, sig, dSigma);
