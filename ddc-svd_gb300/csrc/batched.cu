@@ -56,6 +56,82 @@ __device__ unsigned long long g_batch_trace[128 * 16];
   } while (0)
 #endif
 
+__device__ __forceinline__ int row_slices(int rows) { return rows <= 32 ? 1 : rows <= 64 ? 2 : rows <= 128 ? 4 : 8; }
+
+// One pass of the batched column step over the trailing block (rows i.., at
+// most 32 KR of them): a warp holds four columns in registers, forms their
+// left dot products with u (u_i = 1, u_r = sq x_r), applies the left update,
+// and with the new row-i values w_c (c >= i + 2) accumulates the partial
+// right products sum_c a'_rc w_c of its rows into zs (its row of 256).  The
+// four dot products are summed over the warp by a reduce-scatter (2 + 1
+// shuffles leave each lane a partial of one column over 8 lanes, 3 more
+// complete it) and a gather: 10 shuffles instead of 20.
+template <int KR>
+__device__ __forceinline__ void left_pass(float* M, int ld, int m, int n, int i, float tauq, float sq, float* zs,
+                                          int lane, int wid, int nw) {
+  const float* uc = M + (size_t)i * ld;
+  const bool b16 = lane & 16, b8 = lane & 8;
+  float u[KR], zp[KR];
+#pragma unroll
+  for (int k = 0; k < KR; k++) {
+    const int r = i + lane + 32 * k;
+    u[k] = (r < m) ? (r == i ? 1.f : uc[r] * sq) : 0.f;
+    zp[k] = 0.f;
+  }
+  for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
+    float a[4][KR];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = i + lane + 32 * k;
+        a[q][k] = (c0 + q < n && r < m) ? M[r + (size_t)(c0 + q) * ld] : 0.f;
+      }
+    if (tauq != 0.f) {
+      float w[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < KR; k++) s += u[k] * a[q][k];
+        w[q] = s;
+      }
+      float e2[2];
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        e2[q] = (b16 ? w[q + 2] : w[q]) + __shfl_xor_sync(0xffffffffu, b16 ? w[q] : w[q + 2], 16);
+      float g = (b8 ? e2[1] : e2[0]) + __shfl_xor_sync(0xffffffffu, b8 ? e2[0] : e2[1], 8);
+      g += __shfl_xor_sync(0xffffffffu, g, 4);
+      g += __shfl_xor_sync(0xffffffffu, g, 2);
+      g += __shfl_xor_sync(0xffffffffu, g, 1);
+      // lane l holds the sum of column 2 b16 + b8
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float f = __shfl_sync(0xffffffffu, g, ((q >> 1) & 1) * 16 + (q & 1) * 8) * tauq;
+#pragma unroll
+        for (int k = 0; k < KR; k++) a[q][k] -= f * u[k];
+        if (c0 + q < n) {
+          float* col = M + (size_t)(c0 + q) * ld;
+#pragma unroll
+          for (int k = 0; k < KR; k++) {
+            const int r = i + lane + 32 * k;
+            if (r < m) col[r] = a[q][k];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float wc = __shfl_sync(0xffffffffu, a[q][0], 0);  // new a_{i,c}
+      if (c0 + q >= i + 2 && c0 + q < n)
+#pragma unroll
+        for (int k = 0; k < KR; k++) zp[k] += a[q][k] * wc;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < KR; k++) zs[wid * 32 * kColRegs + lane + 32 * k] = zp[k];
+}
+
 // Unblocked Golub-Kahan bidiagonalisation of M (m x n, ld, m >= n) by one CTA
 // (the reference's bidiag_seq order, bidiag.c:33-186: left reflector and
 // rank-1 update, then right reflector and rank-1 update, per column).
@@ -114,60 +190,12 @@ __device__ void cta_bidiag(float* M, int ld, int m, int n, float* d, float* e, f
     const bool merged = m - i <= kZRows;
     const float* uc = M + (size_t)i * ld;
     if (merged) {
-      float u[kColRegs], zp[kColRegs];
-#pragma unroll
-      for (int k = 0; k < kColRegs; k++) {
-        const int r = i + lane + 32 * k;
-        u[k] = (r < m) ? (r == i ? 1.f : uc[r] * sq) : 0.f;
-        zp[k] = 0.f;
+      switch (row_slices(m - i)) {
+        case 1: left_pass<1>(M, ld, m, n, i, tauq, sq, zs, lane, wid, nw); break;
+        case 2: left_pass<2>(M, ld, m, n, i, tauq, sq, zs, lane, wid, nw); break;
+        case 4: left_pass<4>(M, ld, m, n, i, tauq, sq, zs, lane, wid, nw); break;
+        default: left_pass<8>(M, ld, m, n, i, tauq, sq, zs, lane, wid, nw); break;
       }
-      for (int c0 = i + 1 + 4 * wid; c0 < n; c0 += 4 * nw) {
-        float a[4][kColRegs];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-#pragma unroll
-          for (int k = 0; k < kColRegs; k++) {
-            const int r = i + lane + 32 * k;
-            a[q][k] = (c0 + q < n && r < m) ? M[r + (size_t)(c0 + q) * ld] : 0.f;
-          }
-        if (tauq != 0.f) {
-          float w[4];
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            float s = 0.f;
-#pragma unroll
-            for (int k = 0; k < kColRegs; k++) s += u[k] * a[q][k];
-            w[q] = s;
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-            for (int q = 0; q < 4; q++) w[q] += __shfl_xor_sync(0xffffffffu, w[q], o);
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const float f = w[q] * tauq;
-#pragma unroll
-            for (int k = 0; k < kColRegs; k++) a[q][k] -= f * u[k];
-            if (c0 + q < n) {
-              float* col = M + (size_t)(c0 + q) * ld;
-#pragma unroll
-              for (int k = 0; k < kColRegs; k++) {
-                const int r = i + lane + 32 * k;
-                if (r < m) col[r] = a[q][k];
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const float wc = __shfl_sync(0xffffffffu, a[q][0], 0);  // new a_{i,c}
-          if (c0 + q >= i + 2 && c0 + q < n)
-#pragma unroll
-            for (int k = 0; k < kColRegs; k++) zp[k] += a[q][k] * wc;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < kColRegs; k++) zs[wid * kZRows + lane + 32 * k] = zp[k];
     } else if (tauq != 0.f) {
       for (int c = i + 1 + wid; c < n; c += nw) {
         float* col = M + (size_t)c * ld;
@@ -446,8 +474,6 @@ __device__ void bx_right(float* Vc, int m, int n, const float* R, const float* t
       }
   }
 }
-
-__device__ __forceinline__ int row_slices(int rows) { return rows <= 32 ? 1 : rows <= 64 ? 2 : rows <= 128 ? 4 : 8; }
 
 // U_core = Q [Y; 0], V_core = P X for one problem per CTA (multU / multV).
 // Persistent CTAs take problems largest first from an atomic counter over the
