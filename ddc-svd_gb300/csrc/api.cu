@@ -242,6 +242,39 @@ static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda,
   return rc;
 }
 
+// Work forked onto the handle's side stream: fork() orders it after what the
+// main stream has queued, the work is launched with the side stream standing
+// in for the main one, and join() (at the latest when the object goes out of
+// scope, error returns included) orders the main stream after it.
+struct SideWork {
+  ddcsvd_context* c;
+  cudaStream_t main = nullptr;  // may be the legacy default stream (null)
+  bool swapped = false, forked = false, joined = false;
+  explicit SideWork(ddcsvd_context* ctx) : c(ctx) {}
+  int fork() {
+    DDC_CUDA_TRY(cudaEventRecord(c->fork_ev, c->stream));
+    DDC_CUDA_TRY(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+    forked = true;
+    main = c->stream;
+    c->stream = c->side;
+    swapped = true;
+    return DDCSVD_OK;
+  }
+  void back() {
+    if (swapped) c->stream = main;
+    swapped = false;
+  }
+  int join() {
+    back();
+    if (!forked || joined) return DDCSVD_OK;
+    joined = true;
+    DDC_CUDA_TRY(cudaEventRecord(c->join_ev, c->side));
+    DDC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
+    return DDCSVD_OK;
+  }
+  ~SideWork() { join(); }
+};
+
 static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int lda, float* dS, float* dU,
                          int ldu, float* dV, int ldv, int mode, bool check_finite) {
   const bool plain = (mode == DDCSVD_MODE_PLAIN_FP32);
@@ -249,6 +282,13 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   const int nctas = bidiag_coop_ctas(ctx, m, n);
   const int ldw = (int)round_up(m, 32);
   const size_t gsc = gemm_scratch_bytes(kind, m, n, 2 * kPanel);
+  // Tensor-core modes prepare the back-transformation's WY blocks on the
+  // side stream while stages 2-4 run (FP64-bound D&C, and a vector kernel
+  // that leaves most of the GPU idle); their buffers then get a region of
+  // their own instead of sharing the one that stages 2-4 use.  Stage timing
+  // keeps everything on one stream so that the stage events mean what they say.
+  const bool overlap = !plain && kind != GEMM_SIMT && !ctx->timing;
+  BxPrepared bxl, bxr;
   auto region_a = [&](Arena& a, Plan& pl) {
     pl.W = a.take<float>((size_t)ldw * n);
     pl.d = a.take<float>(n + 4);
@@ -258,6 +298,10 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     pl.sig_slot = a.take<double>(n + 4);
     pl.sig = a.take<double>(n + 4);
     pl.blob = a.take<char>(prep_bounds({n}).blob_bytes);
+    if (overlap) {
+      bx_plan(m, n, n, kind, a, &bxl);
+      bx_plan(n, std::max(0, n - 2), n, kind, a, &bxr);
+    }
   };
   // ---- size
   Plan pl;
@@ -272,10 +316,12 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     DDC_TRY(dc_sigma(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, b2, true));
     Arena b3 = a;
     DDC_TRY(bd_vectors(ctx, n, (long long)n * n, nullptr, nullptr, nullptr, nullptr, nullptr, b3, true));
-    Arena b4 = a;
-    DDC_TRY(apply_left_reflectors(ctx, m, n, nullptr, ldw, nullptr, dU, ldu, n, kind, plain, b4, true));
-    Arena b5 = a;
-    DDC_TRY(apply_right_reflectors(ctx, n, std::max(0, n - 2), nullptr, ldw, nullptr, dV, ldv, n, kind, plain, b5, true));
+    Arena b4 = a, b5 = a;  // stage 5 (its buffers are in region a when it overlaps stages 2-4)
+    if (!overlap) {
+      DDC_TRY(apply_left_reflectors(ctx, m, n, nullptr, ldw, nullptr, dU, ldu, n, kind, plain, b4, true));
+      DDC_TRY(apply_right_reflectors(ctx, n, std::max(0, n - 2), nullptr, ldw, nullptr, dV, ldv, n, kind, plain, b5,
+                                     true));
+    }
     need = std::max(std::max(b1.off, b2.off), std::max(std::max(b3.off, b4.off), b5.off));
   }
   DDC_TRY(ensure_workspace(ctx, need + 4096));
@@ -307,6 +353,14 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     else DDC_TRY(bidiag_blocked(ctx, m, n, pl.W, ldw, pl.d, pl.e, pl.tauq, pl.taup, pl.bw, kind, &sc));
   }
   DDC_TRY(stage_event(ctx, 1));
+  SideWork side(ctx);
+  if (overlap) {
+    DDC_TRY(side.fork());
+    int rc = bx_prepare(ctx, 0, m, n, pl.W, ldw, pl.tauq, bxl);
+    if (rc == DDCSVD_OK) rc = bx_prepare(ctx, 1, n, std::max(0, n - 2), pl.W, ldw, pl.taup, bxr);
+    side.back();
+    DDC_TRY(rc);
+  }
   // ---- bidiagonal read-back: split at negligible superdiagonal entries and
   //      build the D&C forest and vector layout on the host (2n floats down, one blob up)
   const PrepBounds PB = prep_bounds({n});
@@ -349,7 +403,13 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
   }
   DDC_TRY(stage_event(ctx, 3));
   // ---- stage 5
-  {
+  if (overlap) {
+    DDC_TRY(side.join());
+    ktimer_begin(ctx, KC_BACKXFORM);
+    DDC_TRY(bx_apply(ctx, m, n, bxl, dU, ldu, n, kind));
+    DDC_TRY(bx_apply(ctx, n, std::max(0, n - 2), bxr, dV, ldv, n, kind));
+    ktimer_end(ctx);
+  } else {
     Arena b = a;
     DDC_TRY(apply_left_reflectors(ctx, m, n, pl.W, ldw, pl.tauq, dU, ldu, n, kind, plain, b, false));
     Arena c = a;
@@ -504,6 +564,9 @@ static int create_ctx(ddcsvd_context** out, int device) {
   c->smem_optin = prop.sharedMemPerBlockOptin;
   DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->own_stream = true;
+  DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  DDC_CUDA_TRY(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+  DDC_CUDA_TRY(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
   {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
@@ -569,6 +632,12 @@ int ddcsvd_destroy(ddcsvd_handle_t h) {
   if (h->d_status) cudaFree(h->d_status);
   if (h->h_status) cudaFreeHost(h->h_status);
   for (int k = 0; k < 5; k++) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+  if (h->side) {
+    cudaStreamSynchronize(h->side);
+    cudaStreamDestroy(h->side);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   if (h->pool) cudaMemPoolDestroy(h->pool);
   delete h;

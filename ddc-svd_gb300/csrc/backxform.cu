@@ -350,41 +350,63 @@ int wy_prepare_wide(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int 
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
 // last first:  W1 = U_b^T C (stored K-major for the next product) and
 // C -= UT_b W1.
-static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw,
-                            const float* tau, float* C, int ldc, int ncols, GemmKind kind, Arena& a,
-                            bool plan_only) {
+void bx_plan(int rows_total, int nref, int ncols, GemmKind kind, Arena& a, BxPrepared* out) {
   constexpr int NB = kWYT;
-  const int ldu = (int)round_up(rows_total, 32);
+  BxPrepared& w = *out;
+  w.ldu = (int)round_up(rows_total, 32);
   const int nblk = ceil_div(std::max(nref, 1), NB);
-  float* Uc = a.take<float>((size_t)ldu * std::max(nref, 1));
-  float* UT = a.take<float>((size_t)ut_offset<NB>(nblk, rows_total) + 64);
-  float* W1s = a.take<float>((size_t)NB * ncols + 64);
-  float* wys = a.take<float>(wy_scratch_floats<NB>(rows_total, nref));
-  const size_t sbytes = gemm_scratch_bytes(kind, ncols, NB, rows_total);
-  char* sc = a.take<char>(sbytes);
-  if (plan_only || nref <= 0) return DDCSVD_OK;
-  Arena scratch;
-  scratch.base = sc;
-  scratch.plan = false;
-  scratch.cap = sbytes;
-  build_reflectors_kernel<<<dim3(ceil_div(ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
-      side, rows_total, nref, W, ldw, tau, Uc, ldu);
+  w.Uc = a.take<float>((size_t)w.ldu * std::max(nref, 1));
+  w.UT = a.take<float>((size_t)ut_offset<NB>(nblk, rows_total) + 64);
+  w.W1s = a.take<float>((size_t)NB * ncols + 64);
+  w.wys = a.take<float>(wy_scratch_floats<NB>(rows_total, nref));
+  w.sbytes = gemm_scratch_bytes(kind, ncols, NB, rows_total);
+  w.sc = a.take<char>(w.sbytes);
+}
+
+int bx_prepare(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw, const float* tau,
+               const BxPrepared& w) {
+  constexpr int NB = kWYT;
+  if (nref <= 0) return DDCSVD_OK;
+  build_reflectors_kernel<<<dim3(ceil_div(w.ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
+      side, rows_total, nref, W, ldw, tau, w.Uc, w.ldu);
   count_launch();
-  DDC_TRY(wy_prepare_all<NB>(ctx, rows_total, nref, Uc, ldu, tau, UT, false, wys));
+  DDC_TRY(wy_prepare_all<NB>(ctx, rows_total, nref, w.Uc, w.ldu, tau, w.UT, false, w.wys));
   DDC_CUDA_TRY(cudaGetLastError());
+  return DDCSVD_OK;
+}
+
+int bx_apply(ddcsvd_context* ctx, int rows_total, int nref, const BxPrepared& w, float* C, int ldc, int ncols,
+             GemmKind kind) {
+  constexpr int NB = kWYT;
+  if (nref <= 0) return DDCSVD_OK;
+  const int nblk = ceil_div(nref, NB);
+  Arena scratch;
+  scratch.base = w.sc;
+  scratch.plan = false;
+  scratch.cap = w.sbytes;
   for (int bi = nblk - 1; bi >= 0; bi--) {
     const int j0 = bi * NB;
     const int bs = std::min(NB, nref - j0);
     const int rows = rows_total - j0;
     if (rows <= 0 || bs <= 0) continue;
     // W1^T = C[j0:, :]^T U_b, stored as W1s[j + n * NB]
-    DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, Uc + (size_t)j0 * ldu, ldu, j0, W1s, NB, 1.f,
-                             0.f, &scratch));
+    DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, w.Uc + (size_t)j0 * w.ldu, w.ldu, j0, w.W1s,
+                             NB, 1.f, 0.f, &scratch));
     // C[j0:, :] -= UT_b W1
-    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, UT + ut_offset<NB>(bi, rows_total), NB, 0, W1s, NB, 0,
+    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, w.UT + ut_offset<NB>(bi, rows_total), NB, 0, w.W1s, NB, 0,
                            C + j0, ldc, -1.f, 1.f, &scratch));
   }
   return DDCSVD_OK;
+}
+
+static int apply_blocked_tc(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw,
+                            const float* tau, float* C, int ldc, int ncols, GemmKind kind, Arena& a,
+                            bool plan_only) {
+  BxPrepared w;
+  bx_plan(rows_total, nref, ncols, kind, a, &w);
+  if (plan_only) return DDCSVD_OK;
+  DDC_TRY(bx_prepare(ctx, side, rows_total, nref, W, ldw, tau, w));
+  return bx_apply(ctx, rows_total, nref, w, C, ldc, ncols, kind);
 }
 
 static int apply_blocked(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W,

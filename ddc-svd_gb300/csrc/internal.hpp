@@ -16,6 +16,11 @@ struct ddcsvd_context {
   int tail_cluster = -1;  // cluster size of the bidiagonalisation tail (0 = none, -1 = not yet probed)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // the handle's second stream: work that needs nothing from the stages
+  // running on `stream` meanwhile (the back-transformation's WY preparation
+  // runs there during stages 2-4), forked and joined through two events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // device workspace (grown on demand, reused across calls)
   void* ws = nullptr;
   size_t ws_bytes = 0;
@@ -212,6 +217,27 @@ int apply_left_reflectors(ddcsvd_context* ctx, int m, int nref, const float* W, 
 int apply_right_reflectors(ddcsvd_context* ctx, int n, int nref, const float* W, int ldw,
                            const float* taup, float* C, int ldc, int ncols, GemmKind kind,
                            bool plain, Arena& a, bool plan_only);
+
+// The tensor-core back-transformation in two halves: `bx_prepare` writes the
+// reflectors as an explicit masked matrix and every 128-reflector block's
+// T factor and U T (it reads only W and tau, so it may run on another stream
+// while the singular vectors are computed); `bx_apply` then updates C with
+// the prepared blocks, last block first.  side 0: left reflectors (columns
+// of W, rows_total = m), 1: right reflectors (rows of W, rows_total = n).
+struct BxPrepared {
+  float* Uc = nullptr;
+  float* UT = nullptr;
+  float* W1s = nullptr;
+  float* wys = nullptr;
+  char* sc = nullptr;
+  size_t sbytes = 0;
+  int ldu = 0;
+};
+void bx_plan(int rows_total, int nref, int ncols, GemmKind kind, Arena& a, BxPrepared* out);  // buffers from `a`
+int bx_prepare(ddcsvd_context* ctx, int side, int rows_total, int nref, const float* W, int ldw, const float* tau,
+               const BxPrepared& w);
+int bx_apply(ddcsvd_context* ctx, int rows_total, int nref, const BxPrepared& w, float* C, int ldc, int ncols,
+             GemmKind kind);
 
 // UT = Vp T (or Vp T^T) of one QR panel (nb <= kPanel reflectors), row-major with kPanel columns.
 int wy_prepare_block(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int ldv, const float* tau, float* UT,

@@ -568,3 +568,32 @@ def test_row_limits_report_arg(lib, cuda, mode, m, n, tall_qr):
     s, U, V = lib.svd_device(cuda.from_numpy(B).cuda(), mode=mode, handle=h)
     st = np.sort(np.linalg.svd(B.astype(np.float64), compute_uv=False))
     assert np.max(np.abs(s.double().cpu().numpy() - st)) <= TOL * st[-1]
+
+
+@pytest.mark.parametrize("stream_kind", ["legacy", "user"])
+def test_side_stream_overlap_keeps_stream_order(lib, cuda, orc, stream_kind):
+    """The tensor-core modes prepare the back-transformation on the handle's
+    second stream while stages 2-4 run and join it before stage 5.  On the
+    legacy default stream (a null stream handle) and on a user stream alike,
+    every later call of the handle must again run on the caller's stream:
+    a GEMM right after the SVD reads inputs that torch has only just queued
+    on that stream."""
+    if not _mode_available(lib, "tf32x6"):
+        pytest.skip("tf32x6 unavailable")
+    torch = cuda
+    s = torch.cuda.current_stream() if stream_kind == "legacy" else torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        h = lib.Handle(stream=s)
+        rng = np.random.default_rng(31)
+        A = rng.uniform(-1, 1, (700, 500)).astype(np.float32)
+        sv, U, V = lib.svd_device(torch.from_numpy(A).cuda(), mode="tf32x6", handle=h)
+        g = torch.Generator(device="cuda").manual_seed(5)
+        X = torch.rand((256, 2048), device="cuda", generator=g) * 2 - 1
+        Y = torch.rand((192, 2048), device="cuda", generator=g) * 2 - 1
+        C = lib.gemm_nt_device(X, Y, mode="tf32x6", handle=h)
+        ref = X.double() @ Y.double().T
+        err = float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref))
+        res = (sv.double().cpu().numpy(), U.double().cpu().numpy(), V.double().cpu().numpy())
+    s.synchronize()
+    assert err <= 1e-6, err
+    check_metrics(orc, A, *res)
