@@ -108,7 +108,9 @@ int ddcsvd_svd_f32(int m, int n, const float *A, int lda, float *sigma, float *U
 int ddcsvd_create(ddcsvd_handle_t *handle, int device);
 int ddcsvd_destroy(ddcsvd_handle_t handle);
 /* Work of this handle goes to `stream` (a cudaStream_t; NULL = the legacy default stream).
- * A new handle starts on a private non-blocking stream. */
+ * A new handle starts on a private non-blocking stream.  Part of an SVD in
+ * the tensor-core modes runs on the handle's own second stream, forked from
+ * and joined back to `stream` by events within the call. */
 int ddcsvd_set_stream(ddcsvd_handle_t handle, void *stream);
 /* Frees the cached device workspace and returns the memory that the
  * handle's own stream-ordered pool keeps between calls (per-call buffers of
