@@ -300,7 +300,7 @@ static size_t wy_scratch_floats(int rows_total, int nref) {
 
 template <int NB>
 static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const float* Uc, int ldu, const float* tau,
-                          float* UT, bool transT, float* scratch) {
+                          float* UT, bool transT, float* scratch, bool with_ut = true) {
   const int nblk = ceil_div(nref, NB);
   const int chunk = wy_chunk_rows(nblk);
   const int nchunk = ceil_div(rows_total, chunk);
@@ -317,8 +317,8 @@ static int wy_prepare_all(ddcsvd_context* ctx, int rows_total, int nref, const f
   wy_gsum_kernel<NB><<<dim3(ceil_div(NB * NB, 256), nblk), 256, 0, ctx->stream>>>(rows_total, nref, Gp, nchunk,
                                                                                   chunk, G);
   wy_tfactor_kernel<NB><<<nblk, 4 * NB, tf_smem, ctx->stream>>>(rows_total, nref, tau, G, T, transT ? 1 : 0);
-  wy_ut_kernel<NB><<<dim3(nblk, nchunk), 256, ut_smem, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT, chunk);
-  count_launch(4);
+  if (with_ut) wy_ut_kernel<NB><<<dim3(nblk, nchunk), 256, ut_smem, ctx->stream>>>(rows_total, nref, Uc, ldu, T, UT, chunk);
+  count_launch(with_ut ? 4 : 3);
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
 }
@@ -350,16 +350,244 @@ int wy_prepare_wide(ddcsvd_context* ctx, int rows, int nb, const float* Vp, int 
 // C (rows_total x ncols) := H_0 ... H_{nref-1} C on tensor cores.  Per block,
 // last first:  W1 = U_b^T C (stored K-major for the next product) and
 // C -= UT_b W1.
+// ---------------------------------------------------------------- 256-reflector blocks
+// The tensor-core back-transformation applies pairs of 128-reflector blocks
+// (a = reflectors j0 .. j0+127, b = the next 128) as one WY block of 256:
+//   Q_a Q_b = I - [U_a U_b] T [U_a U_b]^T,  T = [T_a, T_ab; 0, T_b],
+//   T_ab = -T_a (U_a^T U_b) T_b
+// (the standard concatenation of compact-WY factors), so that every pass
+// over C does twice the reflectors: K = 256 in C -= (U T) W1 and N = 256 in
+// W1^T = C^T U.  The 128-wide T factors come from wy_prepare_all; the kernels
+// below add the cross Gram matrix U_a^T U_b, T_ab, and U T row-major with 256
+// columns.
+constexpr int kPairNB = 2 * kWYT;
+
+__host__ __device__ inline long long ut2_offset(int p, int rows_total) {
+  return (long long)kPairNB * ((long long)p * rows_total - (long long)kPairNB * p * (p - 1) / 2);
+}
+
+__device__ __forceinline__ void pair_geom(int p, int nref, int& j0, int& bsa, int& bsb) {
+  j0 = p * kPairNB;
+  bsa = min(kWYT, nref - j0);
+  bsb = max(0, min(kWYT, nref - j0 - kWYT));
+}
+
+// Partial X = U_a^T U_b over a chunk of rows (grid (pair, chunk)); rows
+// below j0 + 128 contribute nothing (U_b is zero there).
+__global__ void __launch_bounds__(256) wy_xgram_kernel(int rows_total, int nref, const float* __restrict__ Uc,
+                                                       int ldu, float* Xp, int nchunk, int chunk) {
+  constexpr int NB = kWYT, R = NB / 16;
+  __shared__ float sA[kPrepRows][NB + 1];
+  __shared__ float sB[kPrepRows][NB + 1];
+  int j0, bsa, bsb;
+  pair_geom(blockIdx.x, nref, j0, bsa, bsb);
+  const int jb = j0 + kWYT;
+  const int c0 = jb + blockIdx.y * chunk;
+  const int t = threadIdx.x, ti = t & 15, tj = t >> 4;
+  float acc[R][R];
+#pragma unroll
+  for (int x = 0; x < R; x++)
+#pragma unroll
+    for (int y = 0; y < R; y++) acc[x][y] = 0.f;
+  if (bsb > 0 && c0 < rows_total) {
+    const int c1 = min(rows_total, c0 + chunk);
+    const float* Ua = Uc + (size_t)j0 * ldu;
+    const float* Ub = Uc + (size_t)jb * ldu;
+    for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
+      __syncthreads();
+      wy_load_tile<NB>(sA, Ua, ldu, r0, c1, bsa);
+      wy_load_tile<NB>(sB, Ub, ldu, r0, c1, bsb);
+      __syncthreads();
+#pragma unroll 4
+      for (int k = 0; k < kPrepRows; k++) {
+        float x[R], y[R];
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+          x[q] = sA[k][R * ti + q];
+          y[q] = sB[k][R * tj + q];
+        }
+#pragma unroll
+        for (int q = 0; q < R; q++)
+#pragma unroll
+          for (int c = 0; c < R; c++) acc[q][c] += x[q] * y[c];
+      }
+    }
+  }
+  float* X = Xp + ((size_t)blockIdx.x * nchunk + blockIdx.y) * NB * NB;
+#pragma unroll
+  for (int q = 0; q < R; q++)
+#pragma unroll
+    for (int c = 0; c < R; c++) X[(R * ti + q) + (size_t)(R * tj + c) * NB] = acc[q][c];
+}
+
+// X of every pair: the chunk partials added in chunk order (thread per entry).
+__global__ void __launch_bounds__(256) wy_xsum_kernel(const float* __restrict__ Xp, int nchunk, float* X) {
+  constexpr int NB = kWYT;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= NB * NB) return;
+  const float* src = Xp + (size_t)blockIdx.y * nchunk * NB * NB + idx;
+  float g = 0.f;
+  for (int c = 0; c < nchunk; c++) g += src[(size_t)c * NB * NB];
+  X[(size_t)blockIdx.y * NB * NB + idx] = g;
+}
+
+// T_ab = -T_a X T_b for one pair per CTA (256 threads, each an 8 x 8 tile of
+// the 128 x 128 result); sTa, sX and sTb in dynamic shared memory.
+__global__ void __launch_bounds__(256) wy_tmerge_kernel(int nref, const float* __restrict__ T, const float* __restrict__ X,
+                                                        float* Tab) {
+  constexpr int NB = kWYT, R = NB / 16;
+  extern __shared__ float wsm[];
+  float(*sTa)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm);
+  float(*sX)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + NB * (NB + 1));
+  float(*sTb)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(wsm + 2 * NB * (NB + 1));
+  const int p = blockIdx.x, t = threadIdx.x, ti = t & 15, tj = t >> 4;
+  int j0, bsa, bsb;
+  pair_geom(p, nref, j0, bsa, bsb);
+  float* out = Tab + (size_t)p * NB * NB;
+  if (bsb <= 0) {
+    for (int idx = t; idx < NB * NB; idx += blockDim.x) out[idx] = 0.f;
+    return;
+  }
+  const float* Ta = T + (size_t)(2 * p) * NB * NB;  // [r + c NB]
+  const float* Tb = T + (size_t)(2 * p + 1) * NB * NB;
+  const float* Xg = X + (size_t)p * NB * NB;
+  for (int idx = t; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx % NB, c = idx / NB;
+    sTa[r][c] = Ta[idx];
+    sX[r][c] = Xg[idx];
+    sTb[r][c] = Tb[idx];
+  }
+  __syncthreads();
+  float acc[R][R];
+  // Y = X T_b
+#pragma unroll
+  for (int q = 0; q < R; q++)
+#pragma unroll
+    for (int c = 0; c < R; c++) acc[q][c] = 0.f;
+  for (int k = 0; k < NB; k++) {
+    float x[R], y[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      x[q] = sX[R * ti + q][k];
+      y[q] = sTb[k][R * tj + q];
+    }
+#pragma unroll
+    for (int q = 0; q < R; q++)
+#pragma unroll
+      for (int c = 0; c < R; c++) acc[q][c] += x[q] * y[c];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < R; q++)
+#pragma unroll
+    for (int c = 0; c < R; c++) sX[R * ti + q][R * tj + c] = acc[q][c];
+  __syncthreads();
+  // T_ab = -T_a Y
+#pragma unroll
+  for (int q = 0; q < R; q++)
+#pragma unroll
+    for (int c = 0; c < R; c++) acc[q][c] = 0.f;
+  for (int k = 0; k < NB; k++) {
+    float x[R], y[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      x[q] = sTa[R * ti + q][k];
+      y[q] = sX[k][R * tj + q];
+    }
+#pragma unroll
+    for (int q = 0; q < R; q++)
+#pragma unroll
+      for (int c = 0; c < R; c++) acc[q][c] += x[q] * y[c];
+  }
+#pragma unroll
+  for (int q = 0; q < R; q++)
+#pragma unroll
+    for (int c = 0; c < R; c++) out[(R * ti + q) + (size_t)(R * tj + c) * NB] = -acc[q][c];
+}
+
+// UT of every pair, row-major with 256 columns over rows [j0, rows_total):
+// half 0 (columns 0-127) = U_a T_a, half 1 = U_a T_ab + U_b T_b, i.e. the
+// rows of [U_a U_b] times the half's 256 x 128 slice of the pair's T (grid
+// (pair, row chunk, half); sU [32][257] and the slice in dynamic shared
+// memory).  256 threads in 32 column groups of 4 columns and 8 row groups of
+// 4 rows of a 32-row tile, as wy_ut_kernel.
+__global__ void __launch_bounds__(256) wy_ut2_kernel(int rows_total, int nref, const float* __restrict__ Uc, int ldu,
+                                                     const float* __restrict__ T, const float* __restrict__ Tab,
+                                                     float* UT2, int chunk) {
+  constexpr int NB = kWYT, KP = kPairNB, CG = NB / 4, RPT = 4;
+  static_assert(256 / CG * RPT == kPrepRows, "row groups must cover the tile");
+  extern __shared__ __align__(16) float wsm[];
+  float(*sU)[KP + 1] = reinterpret_cast<float(*)[KP + 1]>(wsm);
+  float(*sT)[NB] = reinterpret_cast<float(*)[NB]>(wsm + kPrepRows * (KP + 1));
+  const int p = blockIdx.x, half = blockIdx.z, t = threadIdx.x;
+  int j0, bsa, bsb;
+  pair_geom(p, nref, j0, bsa, bsb);
+  if (half == 1 && bsb <= 0) return;
+  const int c0 = j0 + blockIdx.y * chunk;
+  if (c0 >= rows_total) return;
+  const int c1 = min(rows_total, c0 + chunk);
+  const int kin = (half == 0) ? NB : KP;  // inner dimension of this half
+  // the half's slice of T: rows 0-127 T_a (half 0) or T_ab (half 1), rows 128-255 T_b (half 1)
+  const float* Ta = T + (size_t)(2 * p) * NB * NB;
+  const float* Tb = T + (size_t)(2 * p + 1) * NB * NB;
+  const float* Tx = Tab + (size_t)p * NB * NB;
+  for (int idx = t; idx < kin * NB; idx += blockDim.x) {
+    const int k = idx % kin, c = idx / kin;
+    float v;
+    if (half == 0) v = Ta[k + (size_t)c * NB];
+    else v = (k < NB) ? Tx[k + (size_t)c * NB] : Tb[(k - NB) + (size_t)c * NB];
+    sT[k][c] = v;
+  }
+  const int cg = t % CG, rg = t / CG;
+  float* out = UT2 + ut2_offset(p, rows_total);
+  for (int r0 = c0; r0 < c1; r0 += kPrepRows) {
+    __syncthreads();
+    for (int idx = t; idx < kPrepRows * kin; idx += blockDim.x) {
+      const int rr = idx & (kPrepRows - 1), k = idx / kPrepRows;
+      const int r = r0 + rr;
+      const int bs = (k < NB) ? bsa : bsb;
+      const int col = j0 + k;  // reflector index (b's columns follow a's)
+      sU[rr][k] = (r < c1 && (k % NB) < bs) ? Uc[r + (size_t)col * ldu] : 0.f;
+    }
+    __syncthreads();
+    float4 acc[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; q++) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int k = 0; k < kin; k++) {
+      const float4 y = *reinterpret_cast<const float4*>(&sT[k][4 * cg]);
+#pragma unroll
+      for (int q = 0; q < RPT; q++) {
+        const float x = sU[rg * RPT + q][k];
+        acc[q].x += x * y.x;
+        acc[q].y += x * y.y;
+        acc[q].z += x * y.z;
+        acc[q].w += x * y.w;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; q++) {
+      const int r = r0 + rg * RPT + q;
+      if (r < c1) reinterpret_cast<float4*>(out + (size_t)(r - j0) * KP + half * NB)[cg] = acc[q];
+    }
+  }
+}
+
+static size_t ut2_smem_bytes() { return sizeof(float) * ((size_t)kPrepRows * (kPairNB + 1) + (size_t)kPairNB * kWYT); }
+
 void bx_plan(int rows_total, int nref, int ncols, GemmKind kind, Arena& a, BxPrepared* out) {
   constexpr int NB = kWYT;
   BxPrepared& w = *out;
   w.ldu = (int)round_up(rows_total, 32);
-  const int nblk = ceil_div(std::max(nref, 1), NB);
+  const int npair = ceil_div(std::max(nref, 1), kPairNB);
+  const int nchunk = ceil_div(std::max(rows_total, 1), kChunkRows);
   w.Uc = a.take<float>((size_t)w.ldu * std::max(nref, 1));
-  w.UT = a.take<float>((size_t)ut_offset<NB>(nblk, rows_total) + 64);
-  w.W1s = a.take<float>((size_t)NB * ncols + 64);
-  w.wys = a.take<float>(wy_scratch_floats<NB>(rows_total, nref));
-  w.sbytes = gemm_scratch_bytes(kind, ncols, NB, rows_total);
+  w.UT = a.take<float>((size_t)ut2_offset(npair, rows_total) + 64);
+  w.W1s = a.take<float>((size_t)kPairNB * ncols + 64);
+  // wy_prepare_all's scratch (Gram partials, G, T of the 128-blocks), then
+  // the pairs' cross-Gram partials, X and T_ab
+  w.wys = a.take<float>(wy_scratch_floats<NB>(rows_total, nref) + (size_t)npair * (nchunk + 2) * NB * NB + 64);
+  w.sbytes = gemm_scratch_bytes(kind, ncols, kPairNB, rows_total);
   w.sc = a.take<char>(w.sbytes);
 }
 
@@ -370,31 +598,52 @@ int bx_prepare(ddcsvd_context* ctx, int side, int rows_total, int nref, const fl
   build_reflectors_kernel<<<dim3(ceil_div(w.ldu, 32), ceil_div(nref, 32)), dim3(32, 8), 0, ctx->stream>>>(
       side, rows_total, nref, W, ldw, tau, w.Uc, w.ldu);
   count_launch();
-  DDC_TRY(wy_prepare_all<NB>(ctx, rows_total, nref, w.Uc, w.ldu, tau, w.UT, false, w.wys));
+  // T of every 128-block (wy_prepare_all's layout: Gram partials, G, then T)
+  DDC_TRY(wy_prepare_all<NB>(ctx, rows_total, nref, w.Uc, w.ldu, tau, nullptr, false, w.wys, false));
+  const int nblk = ceil_div(nref, NB);
+  const int nchunk_g = ceil_div(rows_total, wy_chunk_rows(nblk));
+  const float* T = w.wys + (size_t)nblk * nchunk_g * NB * NB + (size_t)nblk * NB * NB;
+  const int npair = ceil_div(nref, kPairNB);
+  const int nchunk = ceil_div(rows_total, kChunkRows);
+  float* Xp = w.wys + wy_scratch_floats<NB>(rows_total, nref);
+  float* X = Xp + (size_t)npair * nchunk * NB * NB;
+  float* Tab = X + (size_t)npair * NB * NB;
+  wy_xgram_kernel<<<dim3(npair, nchunk), 256, 0, ctx->stream>>>(rows_total, nref, w.Uc, w.ldu, Xp, nchunk,
+                                                                kChunkRows);
+  wy_xsum_kernel<<<dim3(ceil_div(NB * NB, 256), npair), 256, 0, ctx->stream>>>(Xp, nchunk, X);
+  const int tm_smem = 3 * NB * (NB + 1) * (int)sizeof(float);
+  DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_tmerge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    tm_smem));
+  wy_tmerge_kernel<<<npair, 256, tm_smem, ctx->stream>>>(nref, T, X, Tab);
+  const int ut_smem = (int)ut2_smem_bytes();
+  DDC_CUDA_TRY(cudaFuncSetAttribute((const void*)wy_ut2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    ut_smem));
+  wy_ut2_kernel<<<dim3(npair, nchunk, 2), 256, ut_smem, ctx->stream>>>(rows_total, nref, w.Uc, w.ldu, T, Tab, w.UT,
+                                                                      kChunkRows);
+  count_launch(4);
   DDC_CUDA_TRY(cudaGetLastError());
   return DDCSVD_OK;
 }
 
 int bx_apply(ddcsvd_context* ctx, int rows_total, int nref, const BxPrepared& w, float* C, int ldc, int ncols,
              GemmKind kind) {
-  constexpr int NB = kWYT;
   if (nref <= 0) return DDCSVD_OK;
-  const int nblk = ceil_div(nref, NB);
+  const int npair = ceil_div(nref, kPairNB);
   Arena scratch;
   scratch.base = w.sc;
   scratch.plan = false;
   scratch.cap = w.sbytes;
-  for (int bi = nblk - 1; bi >= 0; bi--) {
-    const int j0 = bi * NB;
-    const int bs = std::min(NB, nref - j0);
+  for (int p = npair - 1; p >= 0; p--) {
+    const int j0 = p * kPairNB;
+    const int bs = std::min(kPairNB, nref - j0);
     const int rows = rows_total - j0;
     if (rows <= 0 || bs <= 0) continue;
-    // W1^T = C[j0:, :]^T U_b, stored as W1s[j + n * NB]
+    // W1^T = C[j0:, :]^T U_p, stored as W1s[j + n * 256]
     DDC_TRY(gemm_tc_kmajor_t(ctx, kind, ncols, bs, rows, C, ldc, j0, w.Uc + (size_t)j0 * w.ldu, w.ldu, j0, w.W1s,
-                             NB, 1.f, 0.f, &scratch));
-    // C[j0:, :] -= UT_b W1
-    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, w.UT + ut_offset<NB>(bi, rows_total), NB, 0, w.W1s, NB, 0,
-                           C + j0, ldc, -1.f, 1.f, &scratch));
+                             kPairNB, 1.f, 0.f, &scratch));
+    // C[j0:, :] -= UT_p W1
+    DDC_TRY(gemm_tc_kmajor(ctx, kind, rows, ncols, bs, w.UT + ut2_offset(p, rows_total), kPairNB, 0, w.W1s, kPairNB,
+                           0, C + j0, ldc, -1.f, 1.f, &scratch));
   }
   return DDCSVD_OK;
 }
