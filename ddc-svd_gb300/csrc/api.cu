@@ -230,8 +230,11 @@ static int svd_core(ddcsvd_context* ctx, int m, int n, const float* dA, int lda,
   DDC_CUDA_TRY(pool_alloc(ctx, &buf, sizeof(float) * ((size_t)lu * n + (size_t)lv * n + 64)));
   float* Ui = buf;
   float* Vi = buf + (size_t)lu * n + 32;
+  auto v_copy = std::move(ctx->v_copy);  // the staged V is final only after the copy below
+  ctx->v_copy = nullptr;
   int rc = tall ? svd_tall_qr(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite)
                 : svd_core_impl(ctx, m, n, dA, lda, dS, Ui, lu, Vi, lv, mode, check_finite);
+  ctx->v_copy = std::move(v_copy);
   if (rc == DDCSVD_OK) {
     copy2d_kernel<<<dim3(ceil_div(m, 256), n), 256, 0, ctx->stream>>>(m, n, Ui, lu, dU, ldu);
     copy2d_kernel<<<dim3(ceil_div(n, 256), n), 256, 0, ctx->stream>>>(n, n, Vi, lv, dV, ldv);
@@ -402,18 +405,29 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     count_launch();
   }
   DDC_TRY(stage_event(ctx, 3));
-  // ---- stage 5
+  // ---- stage 5: V first (its host copy may then overlap U's products)
+  auto v_done = [&]() -> int {
+    if (ctx->v_copy && !ctx->v_copy_started) {
+      DDC_CUDA_TRY(cudaEventRecord(ctx->v_ready, ctx->stream));
+      DDC_CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->v_ready, 0));
+      ctx->v_copy_started = true;
+      DDC_CUDA_TRY(ctx->v_copy(ctx->side));
+    }
+    return DDCSVD_OK;
+  };
   if (overlap) {
     DDC_TRY(side.join());
     ktimer_begin(ctx, KC_BACKXFORM);
-    DDC_TRY(bx_apply(ctx, m, n, bxl, dU, ldu, n, kind));
     DDC_TRY(bx_apply(ctx, n, std::max(0, n - 2), bxr, dV, ldv, n, kind));
+    DDC_TRY(v_done());
+    DDC_TRY(bx_apply(ctx, m, n, bxl, dU, ldu, n, kind));
     ktimer_end(ctx);
   } else {
-    Arena b = a;
-    DDC_TRY(apply_left_reflectors(ctx, m, n, pl.W, ldw, pl.tauq, dU, ldu, n, kind, plain, b, false));
     Arena c = a;
     DDC_TRY(apply_right_reflectors(ctx, n, std::max(0, n - 2), pl.W, ldw, pl.taup, dV, ldv, n, kind, plain, c, false));
+    DDC_TRY(v_done());
+    Arena b = a;
+    DDC_TRY(apply_left_reflectors(ctx, m, n, pl.W, ldw, pl.tauq, dU, ldu, n, kind, plain, b, false));
   }
   sigma_out_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(n, pl.sig, dS);
   count_launch();
@@ -567,6 +581,7 @@ static int create_ctx(ddcsvd_context** out, int device) {
   DDC_CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
   DDC_CUDA_TRY(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
   DDC_CUDA_TRY(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
+  DDC_CUDA_TRY(cudaEventCreateWithFlags(&c->v_ready, cudaEventDisableTiming));
   {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
@@ -638,6 +653,7 @@ int ddcsvd_destroy(ddcsvd_handle_t h) {
   }
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
+  if (h->v_ready) cudaEventDestroy(h->v_ready);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   if (h->pool) cudaMemPoolDestroy(h->pool);
   delete h;
@@ -902,13 +918,24 @@ int ddcsvd_gemm_f32_device(ddcsvd_handle_t h, int mode, int M, int N, int K, con
 static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda, float* S, float* U, int ldu,
                         float* V, int ldv, int mode) {
   const int k = std::min(m, n);
+  // device copies with 16-byte aligned bases and leading dimensions (the
+  // tensor-core back-transformation then writes U and V in place)
+  const int lum = (int)round_up(m, 4), lvn = (int)round_up(n, 4);
+  const size_t na = (size_t)m * n, ns = round_up(k, 4), nu = (size_t)lum * k, nv = (size_t)lvn * k;
   float *dA = nullptr, *dS = nullptr, *dU = nullptr, *dV = nullptr;
-  const size_t na = (size_t)m * n, nu = (size_t)m * k, nv = (size_t)n * k;
-  DDC_CUDA_TRY(pool_alloc(h, &dA, sizeof(float) * (na + k + nu + nv + 64)));
-  dS = dA + na;
-  dU = dS + k;
+  DDC_CUDA_TRY(pool_alloc(h, &dA, sizeof(float) * (round_up(na, 4) + ns + nu + nv + 64)));
+  dS = dA + round_up(na, 4);
+  dU = dS + ns;
   dV = dU + nu;
+  // host copy of a device matrix (rows x k, device ld ldd) on stream st
+  auto out2d = [&](float* dst, int ld, const float* src, int ldd, int rows, cudaStream_t st) {
+    return (ld == rows && ldd == rows)
+               ? cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)rows * k, cudaMemcpyDeviceToHost, st)
+               : cudaMemcpy2DAsync(dst, sizeof(float) * ld, src, sizeof(float) * ldd, sizeof(float) * rows, k,
+                                   cudaMemcpyDeviceToHost, st);
+  };
   int rc = DDCSVD_OK;
+  bool side_used = false;
   do {
     if (lda == m) {
       if (cudaMemcpyAsync(dA, A, sizeof(float) * na, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
@@ -918,21 +945,34 @@ static int svd_host_f32(ddcsvd_context* h, int m, int n, const float* A, int lda
     }
     float* at = nullptr;
     if (m < n && pool_alloc(h, &at, sizeof(float) * na) != cudaSuccess) { rc = DDCSVD_ERR_ALLOC; break; }
-    rc = svd_device(h, m, n, dA, m, dS, dU, m, dV, n, mode, at);
+    // the pipeline finishes its second output first (V, or U of a wide
+    // input): the pipeline queues that copy on the side stream as soon as
+    // the output is final (before the other output's products)
+    const bool early_v = (m >= n);
+    h->v_copy = [&](cudaStream_t st) {
+      return early_v ? out2d(V, ldv, dV, lvn, n, st) : out2d(U, ldu, dU, lum, m, st);
+    };
+    h->v_copy_started = false;
+    rc = svd_device(h, m, n, dA, m, dS, dU, lum, dV, lvn, mode, at);
+    h->v_copy = nullptr;
+    side_used = h->v_copy_started;
     if (at) cudaFreeAsync(at, h->stream);
     if (rc != DDCSVD_OK) break;
+    if (!side_used) {
+      const cudaError_t e = early_v ? out2d(V, ldv, dV, lvn, n, h->stream) : out2d(U, ldu, dU, lum, m, h->stream);
+      if (e != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    }
     if (cudaMemcpyAsync(S, dS, sizeof(float) * k, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-    // packed host layouts leave as one contiguous copy each, strided ones row block by row block
-    auto out2d = [&](float* dst, int ld, const float* src, int rows) {
-      return ld == rows
-                 ? cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)rows * k, cudaMemcpyDeviceToHost, h->stream)
-                 : cudaMemcpy2DAsync(dst, sizeof(float) * ld, src, sizeof(float) * rows, sizeof(float) * rows, k,
-                                     cudaMemcpyDeviceToHost, h->stream);
-    };
-    if (out2d(U, ldu, dU, m) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-    if (out2d(V, ldv, dV, n) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
-    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    {
+      const cudaError_t e = early_v ? out2d(U, ldu, dU, lum, m, h->stream) : out2d(V, ldv, dV, lvn, n, h->stream);
+      if (e != cudaSuccess) { rc = DDCSVD_ERR_CUDA; break; }
+    }
   } while (0);
+  if (side_used) {  // the side stream's copy ends before the buffers are released
+    cudaEventRecord(h->join_ev, h->side);
+    cudaStreamWaitEvent(h->stream, h->join_ev, 0);
+  }
+  if (rc == DDCSVD_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = DDCSVD_ERR_CUDA;
   cudaFreeAsync(dA, h->stream);
   cudaStreamSynchronize(h->stream);
   if (rc == DDCSVD_ERR_CUDA && t_last_error.empty()) set_last_error("CUDA copy failed");

@@ -7,6 +7,8 @@
 #include <mutex>
 #include <vector>
 
+#include <functional>
+
 #include "common.cuh"
 
 struct ddcsvd_context {
@@ -21,6 +23,13 @@ struct ddcsvd_context {
   // runs there during stages 2-4), forked and joined through two events
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // set by the host-buffer API: once the pipeline's second output (V, or U
+  // of a wide input) is final it records v_ready, makes the side stream wait
+  // for it and calls v_copy to queue that output's copy to the host there,
+  // so the copy overlaps the rest of the back-transformation
+  cudaEvent_t v_ready = nullptr;
+  std::function<cudaError_t(cudaStream_t)> v_copy;
+  bool v_copy_started = false;
   // device workspace (grown on demand, reused across calls)
   void* ws = nullptr;
   size_t ws_bytes = 0;
