@@ -152,10 +152,16 @@ static int resolve_mode(int mode) {
 }
 
 // ---------------------------------------------------------------- small kernels
-__global__ void copy_pad_kernel(int m, int n, const float* __restrict__ A, int lda, float* W, int ldw) {
+// W = A with zero rows m .. ldw-1; with `st` set, a non-finite entry also
+// records DDCSVD_ERR_NONFINITE (the input check rides on the copy's read).
+__global__ void copy_pad_kernel(int m, int n, const float* __restrict__ A, int lda, float* W, int ldw,
+                                DevStatus* st = nullptr) {
   const int c = blockIdx.y;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ldw; r += gridDim.x * blockDim.x)
-    W[r + (size_t)c * ldw] = (r < m) ? A[r + (size_t)c * lda] : 0.f;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ldw; r += gridDim.x * blockDim.x) {
+    const float v = (r < m) ? A[r + (size_t)c * lda] : 0.f;
+    if (st && !isfinite(v)) set_error(st, DDCSVD_ERR_NONFINITE, (int)((r + (size_t)c * m) % 2147483647));
+    W[r + (size_t)c * ldw] = v;
+  }
 }
 
 __global__ void sigma_out_kernel(int n, const double* s, float* out) {
@@ -173,17 +179,6 @@ __global__ void triu_kernel(int n, const float* __restrict__ W, int ldw, float* 
   const int c = blockIdx.y;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ldr; r += gridDim.x * blockDim.x)
     R[r + (size_t)c * ldr] = (r <= c && r < n) ? W[r + (size_t)c * ldw] : 0.f;
-}
-
-__global__ void finite_check_kernel(int m, int n, const float* A, int lda, DevStatus* st) {
-  const size_t tot = (size_t)m * n;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
-    const float v = A[(i % m) + (i / m) * (size_t)lda];
-    if (!isfinite(v)) {
-      set_error(st, DDCSVD_ERR_NONFINITE, (int)(i % 2147483647));
-      return;
-    }
-  }
 }
 
 // ---------------------------------------------------------------- pipeline
@@ -338,11 +333,8 @@ static int svd_core_impl(ddcsvd_context* ctx, int m, int n, const float* dA, int
     ctx->kused = 0;
   }
   DDC_TRY(stage_event(ctx, 0));
-  if (check_finite) {
-    finite_check_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(m, n, dA, lda, ctx->d_status);
-    count_launch();
-  }
-  copy_pad_kernel<<<dim3(ceil_div(ldw, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, pl.W, ldw);
+  copy_pad_kernel<<<dim3(ceil_div(ldw, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, pl.W, ldw,
+                                                                      check_finite ? ctx->d_status : nullptr);
   count_launch();
   DDC_CUDA_TRY(cudaGetLastError());
   {
@@ -484,11 +476,8 @@ static int svd_tall_qr(ddcsvd_context* ctx, int m, int n, const float* dA, int l
   do {
     if ((rc = reset_status(ctx))) break;
     ctx->kused = 0;
-    if (check_finite) {
-      finite_check_kernel<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(m, n, dA, lda, ctx->d_status);
-      count_launch();
-    }
-    copy_pad_kernel<<<dim3(ceil_div(ldq, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, Wq, ldq);
+    copy_pad_kernel<<<dim3(ceil_div(ldq, 256), n), 256, 0, ctx->stream>>>(m, n, dA, lda, Wq, ldq,
+                                                                          check_finite ? ctx->d_status : nullptr);
     count_launch();
     if ((rc = range_scale_matrix(ctx, m, n, Wq, ldq, amax))) break;
     if ((rc = qr_blocked(ctx, m, n, Wq, ldq, tau, qw, kind))) break;

@@ -322,14 +322,23 @@ def test_form_factors_dropin(lib, cuda, m, n):
     assert np.linalg.norm(U @ B @ V.T - A32) / np.linalg.norm(A32) <= 1e-5
 
 
-def test_nonfinite_input_fails_loudly(lib, cuda):
-    A = np.ones((16, 8), dtype=np.float32)
-    A[3, 2] = np.nan
+@pytest.mark.parametrize("shape,bad,mode,tall_qr", [((16, 8), np.nan, "blocked", 0),
+                                                    ((300, 130), np.inf, "tf32x3", 1),
+                                                    ((40, 200), -np.inf, "tf32x3", 0)])
+def test_nonfinite_input_fails_loudly(lib, cuda, shape, bad, mode, tall_qr):
+    """A NaN or Inf entry is found while the input is copied into the working
+    matrix (the direct path, the QR-first path and a wide input alike)."""
+    if mode != "blocked" and not _mode_available(lib, mode):
+        pytest.skip(f"{mode} unavailable")
+    A = np.ones(shape, dtype=np.float32)
+    A[shape[0] // 2, shape[1] - 1] = bad
+    h = lib.Handle()
+    h.tuning = {"tall_qr": tall_qr}
     with pytest.raises(lib.DdcsvdError) as ei:
-        run(lib, cuda, A, "blocked")
+        lib.svd_device(cuda.from_numpy(A).cuda(), mode=mode, handle=h)
     assert ei.value.status == 7
-    s, U, V = run(lib, cuda, np.eye(8, dtype=np.float32), "blocked")  # handle still usable
-    assert np.allclose(s, 1.0)
+    s, U, V = lib.svd_device(cuda.from_numpy(np.eye(8, dtype=np.float32)).cuda(), mode=mode, handle=h)
+    assert np.allclose(s.cpu().numpy(), 1.0)  # handle still usable
 
 
 # ------------------------------------------------------------------ stage parity
