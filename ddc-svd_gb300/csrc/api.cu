@@ -978,6 +978,15 @@ int ddcsvd_svd_f32(int m, int n, const float* A, int lda, float* sigma, float* U
   return svd_host_f32(h, m, n, A, lda, sigma, U, ldu, V, ldv, mode);
 }
 
+int ddcsvd_svd_f32_host(ddcsvd_handle_t h, int m, int n, const float* A, int lda, float* sigma, float* U, int ldu,
+                        float* V, int ldv, int mode) {
+  t_last_error.clear();
+  if (!h || m <= 0 || n <= 0 || !A || !sigma || !U || !V || lda < m || ldu < m || ldv < n) return DDCSVD_ERR_ARG;
+  std::lock_guard<std::mutex> g(h->mu);
+  DDC_CUDA_TRY(cudaSetDevice(h->device));
+  return svd_host_f32(h, m, n, A, lda, sigma, U, ldu, V, ldv, mode);
+}
+
 int svd_gpu_ex(int m, int n, double* A, double* sigma, double* U, double* V, int mode) {
   t_last_error.clear();
   if (m <= 0 || n <= 0 || !A || !sigma || !U || !V) return DDCSVD_ERR_ARG;

@@ -27,6 +27,7 @@ _SIGS = {
     "form_v_par": (None, [c_int, c_int, P, P]),
     "svd_gpu_ex": (c_int, [c_int, c_int, P, P, P, P, c_int]),
     "ddcsvd_svd_f32": (c_int, [c_int, c_int, P, c_int, P, P, c_int, P, c_int, c_int]),
+    "ddcsvd_svd_f32_host": (c_int, [P, c_int, c_int, P, c_int, P, P, c_int, P, c_int, c_int]),
     "ddcsvd_create": (c_int, [P, c_int]),
     "ddcsvd_destroy": (c_int, [P]),
     "ddcsvd_set_stream": (c_int, [P, P]),

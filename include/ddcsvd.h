@@ -99,6 +99,10 @@ int svd_gpu_ex(int m, int n, double *A, double *sigma, double *U, double *V, int
 /* FP32 host buffers, A is not modified.  lda >= m, ldu >= m, ldv >= n. */
 int ddcsvd_svd_f32(int m, int n, const float *A, int lda, float *sigma, float *U, int ldu,
                    float *V, int ldv, int mode);
+/* The same on a handle (its launch knobs, limits and stream; the call
+ * returns after the results are in the host buffers). */
+int ddcsvd_svd_f32_host(ddcsvd_handle_t handle, int m, int n, const float *A, int lda, float *sigma, float *U,
+                        int ldu, float *V, int ldv, int mode);
 
 /* ---------------------------------------------------------------- handles and device API */
 

@@ -606,3 +606,27 @@ def test_side_stream_overlap_keeps_stream_order(lib, cuda, orc, stream_kind):
     s.synchronize()
     assert err <= 1e-6, err
     check_metrics(orc, A, *res)
+
+
+def test_host_f32_api_on_handle(lib, cuda, orc):
+    """ddcsvd_svd_f32_host: host buffers on a handle (its knobs and stream);
+    a strided host layout (ld larger than the rows) for every matrix."""
+    import ctypes
+    if not _mode_available(lib, "tf32x3"):
+        pytest.skip("tf32x3 unavailable")
+    rng = np.random.default_rng(41)
+    m, n = 333, 201
+    A = rng.uniform(-1, 1, (m, n)).astype(np.float32)
+    lda, ldu, ldv = m + 3, m + 5, n + 2
+    Ab = np.zeros((n, lda), dtype=np.float32)
+    Ab[:, :m] = A.T
+    s = np.zeros(n, dtype=np.float32)
+    Ub = np.zeros((n, ldu), dtype=np.float32)
+    Vb = np.zeros((n, ldv), dtype=np.float32)
+    h = lib.Handle()
+    h.tuning = {"splitk_max": 2}
+    addr = lambda x: x.ctypes.data
+    rc = lib.load().ddcsvd_svd_f32_host(h.ptr, m, n, addr(Ab), lda, addr(s), addr(Ub), ldu, addr(Vb), ldv,
+                                        lib.MODES["tf32x3"])
+    lib.check(rc, "ddcsvd_svd_f32_host")
+    check_metrics(orc, A, s.astype(np.float64), Ub[:, :m].T.astype(np.float64), Vb[:, :n].T.astype(np.float64))
