@@ -12,7 +12,12 @@
 // the reference (bidiag_par.c:310-397, left_update_mat.cl / right_update_mat.cl):
 // per column a left reflector and its rank-1 update, then a right reflector
 // and its rank-1 update, exchanged through distributed shared memory with
-// four hardware cluster barriers.  Reflector conventions, FP32 compensated
+// one hardware cluster barrier per column: the right reflector's products
+// x = A' v are gathered unscaled (v = e_1 + s * row, so x = A'(:, i+1) +
+// s * A'(:, i+2:) row(i+2:)) right after the left update, every CTA adds the
+// C partials for all rows itself, and since column i+1 after the right update
+// is A'(:, i+1) - tau * x, every CTA also forms the next left reflector
+// itself instead of waiting for the column's owner.  Reflector conventions, FP32 compensated
 // norms and the LAPACK-form storage are those of the panel kernel, so the
 // back-transformation reads the result unchanged.
 //
@@ -56,11 +61,13 @@ struct TailParams {
 };
 
 // Shared-memory layout (floats, every section 16-byte aligned): A [mt x ncb]
-// (column-major, ld mt), u, xp, xs, x [mt each], red [32 FF], scal [8],
-// nrm [1 FF].
+// (column-major, ld mt), u, x, xp[2], pc[2] [mt each; xp and pc, the ones
+// other CTAs read, double-buffered by column parity], vrow [ncb], red [32 FF],
+// scal [8], nrm [2 FF].
 __host__ __device__ inline size_t tail_vec_floats(int mt) { return (size_t)((mt + 4 + 3) & ~3); }
 __host__ __device__ inline size_t tail_smem_floats(int mt, int ncb) {
-  return (((size_t)mt * ncb + 3) & ~(size_t)3) + 4 * tail_vec_floats(mt) + 64 + 8 + 4;
+  return (((size_t)mt * ncb + 3) & ~(size_t)3) + 6 * tail_vec_floats(mt) + (((size_t)ncb + 3) & ~(size_t)3) +
+         64 + 8 + 4;
 }
 
 // CTA-wide compensated sum (fixed order: warp trees, then warps in order).
@@ -79,6 +86,45 @@ __device__ __forceinline__ FF tail_sum_ff(FF v, FF* red) {
   return red[0];
 }
 
+// Right update of the own columns l >= lr with (tp, x, row i of A) and then
+// their left update with (tq, u), rows > i, one warp per column: x and u for
+// the lane's rows (i + 1 + lane + 32 j) in registers, each column read and
+// written once.  Row i + 1 of the columns >= the local index lv is gathered
+// into vrow for the next step.  Needs mt - i - 1 <= 32 KR.
+template <int KR>
+__device__ __forceinline__ void tail_fused_update(float* A, int mt, int i, int lr, int nown, float tp, float tq,
+                                                  const float* x, const float* u, float* vrow, int lv) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int rb = i + 1 + lane;
+  float uc[KR], xc[KR];
+#pragma unroll
+  for (int j = 0; j < KR; j++) {
+    const int r = rb + 32 * j;
+    uc[j] = r < mt ? u[r] : 0.f;
+    xc[j] = (r < mt && tp != 0.f) ? x[r] : 0.f;  // x is not formed when tp = 0
+  }
+  for (int l = lr + wid; l < nown; l += nw) {
+    float* col = A + (size_t)l * mt;
+    const float f = tp * col[i];
+    float c[KR];
+    float y = 0.f;
+#pragma unroll
+    for (int j = 0; j < KR; j++) {
+      const int r = rb + 32 * j;
+      c[j] = r < mt ? col[r] - f * xc[j] : 0.f;
+      y += uc[j] * c[j];
+    }
+    y = warp_sum(y) * tq;
+#pragma unroll
+    for (int j = 0; j < KR; j++) {
+      const int r = rb + 32 * j;
+      c[j] -= y * uc[j];
+      if (r < mt) col[r] = c[j];
+    }
+    if (lane == 0 && l >= lv) vrow[l - lv] = c[0];
+  }
+}
+
 __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams p) {
   extern __shared__ __align__(16) float sm[];
   cg::cluster_group cluster = cg::this_cluster();
@@ -90,140 +136,203 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
   const int nown = rank < ncols ? (ncols - rank + C - 1) / C : 0;
   // first local index whose column is >= c
   auto lfirst = [&](int c) { return c <= rank ? 0 : (c - rank + C - 1) / C; };
+  const size_t vec = tail_vec_floats(mt);
   float* A = sm;
   float* u = A + (((size_t)mt * ncb + 3) & ~(size_t)3);
-  float* xp = u + tail_vec_floats(mt);
-  float* xs = xp + tail_vec_floats(mt);
-  float* x = xs + tail_vec_floats(mt);
-  FF* red = reinterpret_cast<FF*>(x + tail_vec_floats(mt));
+  float* x = u + vec;
+  float* xp = x + vec;      // [2][vec]
+  float* pc = xp + 2 * vec;  // [2][vec]
+  float* vrow = pc + 2 * vec;
+  FF* red = reinterpret_cast<FF*>(vrow + ((ncb + 3) & ~3));
   float* scal = reinterpret_cast<float*>(red + 32);
-  FF* nrm = reinterpret_cast<FF*>(scal + 8);
+  FF* nrm = reinterpret_cast<FF*>(scal + 8);  // [2]
 
-  // own columns into shared memory
+  // Left reflector of column j from u[j..mt) (the column after every earlier
+  // update).  Every CTA forms it from the same values in the same order, so
+  // all hold the same u; the owner of column j also stores it there.
+  auto form_left = [&](int j) {
+    FF s2{0.f, 0.f};
+    for (int r = j + 1 + t; r < mt; r += nt_) s2 = ff_add_sq(s2, u[r]);
+    s2 = tail_sum_ff(s2, red);
+    float alpha, tq, sq;
+    householder_ff(u[j], s2, &alpha, &tq, &sq);
+    __syncthreads();  // u[j] read by every thread before it is overwritten
+    const bool own = j % C == rank;
+    float* col = A + (size_t)(j / C) * mt;
+    for (int r = j + t; r < mt; r += nt_) {
+      const float v = (r == j) ? 1.f : u[r] * sq;
+      u[r] = v;
+      if (own) col[r] = v;
+    }
+    if (own && t == 0) {
+      p.d[j] = alpha;
+      p.tauq[j] = tq;
+    }
+    __syncthreads();
+    return tq;
+  };
+
+  // Left update of the own columns > j with u (warp per column, in shared
+  // memory); row j of the columns > j + 1 gathered into vrow.
+  auto left_update = [&](int j, float tq) {
+    const int l1 = lfirst(j + 1), l2 = lfirst(j + 2);
+    for (int l = l1 + wid; l < nown; l += nw) {
+      float* col = A + (size_t)l * mt;
+      if (tq != 0.f) {
+        float y = 0.f;
+        for (int r = j + lane; r < mt; r += 32) y += u[r] * col[r];
+        y = warp_sum(y) * tq;
+        for (int r = j + lane; r < mt; r += 32) col[r] -= y * u[r];
+      }
+      if (lane == 0 && l >= l2) vrow[l - l2] = col[j];
+    }
+    __syncthreads();
+  };
+
+  // own columns into shared memory; column 0 to every CTA
   for (int l = 0; l < nown; l++)
     for (int r = t; r < mt; r += nt_) A[r + (size_t)l * mt] = p.W[r + (size_t)(rank + l * C) * p.ldw];
+  for (int r = t; r < mt; r += nt_) u[r] = p.W[r];
   __syncthreads();
+  left_update(0, form_left(0));
   cluster.sync();
 
-  for (int i = 0; i < ncols; i++) {
-    const int own_i = i % C;  // rank owning column i (its local index i / C)
+  // step i: right reflector of row i, then the left reflector of column i + 1
+  for (int i = 0; i + 1 < ncols; i++) {
+    const int b = i & 1;
+    float* xpb = xp + b * vec;
+    float* pcb = pc + b * vec;
+    const int l1 = lfirst(i + 1), l2 = lfirst(i + 2);
+    const int own_next = (i + 1) % C;  // rank owning column i + 1
     TMARK(0);
-    // ---- A: left reflector from column i (its owner)
-    if (rank == own_i) {
-      float* col = A + (size_t)(i / C) * mt;
-      FF s2{0.f, 0.f};
-      for (int r = i + 1 + t; r < mt; r += nt_) s2 = ff_add_sq(s2, col[r]);
-      s2 = tail_sum_ff(s2, red);
-      float alpha, tq, sq;
-      householder_ff(col[i], s2, &alpha, &tq, &sq);
-      __syncthreads();  // col[i] read by every thread before it is overwritten
-      for (int r = i + t; r < mt; r += nt_) col[r] = (r == i) ? 1.f : col[r] * sq;
-      if (t == 0) {
-        p.d[i] = alpha;
-        p.tauq[i] = tq;
-        scal[0] = tq;
+    // ---- B: per row r > i the unscaled partial product of the right
+    // reflector's x over the own columns >= i + 2, the partial squared norm of
+    // row i over them, and column i + 1 copied (its owner replaces it in C
+    // while the other CTAs still read it)
+    {
+      const int nz = nown - l2;
+      const float* cnext = A + (size_t)((i + 1) / C) * mt;
+      for (int r = i + 1 + t; r < mt; r += nt_) {
+        const float* ar = A + r + (size_t)l2 * mt;
+        float z = 0.f;
+        for (int j = 0; j < nz; j++) z += ar[(size_t)j * mt] * vrow[j];
+        xpb[r] = z;
+      }
+      if (rank == own_next)
+        for (int r = i + t; r < mt; r += nt_) pcb[r] = cnext[r];
+      if (wid == nw - 1) {
+        FF s{0.f, 0.f};
+        for (int j = lane; j < nz; j += 32) s = ff_add_sq(s, vrow[j]);
+        s = warp_sum_ff(s);
+        if (lane == 0) nrm[b] = s;
       }
     }
     TMARK(1);
-    cluster.sync();  // #1: u and tau_q published
+    cluster.sync();  // partial norms, partial products and column i + 1 published
     TMARK(2);
-    // ---- B: left update of the own columns > i, partial norm of row i
-    {
-      const float* ucol = cluster.map_shared_rank(A + (size_t)(i / C) * mt, own_i);
-      const float tq = *cluster.map_shared_rank(scal, own_i);
-      for (int r = i + t; r < mt; r += nt_) u[r] = ucol[r];
-      __syncthreads();
-      if (tq != 0.f) {
-        for (int l = lfirst(i + 1) + wid; l < nown; l += nw) {  // warp per column
-          float* col = A + (size_t)l * mt;
-          float y = 0.f;
-          for (int r = i + lane; r < mt; r += 32) y += u[r] * col[r];
-          y = warp_sum(y) * tq;
-          for (int r = i + lane; r < mt; r += 32) col[r] -= y * u[r];
-        }
+    // ---- C: right reflector from row i (every CTA forms it)
+    if (t < 32) {
+      // the C partial norms fetched by lanes 0..C-1 at once, added by one shuffle tree
+      FF v = t < C ? cluster.map_shared_rank(nrm, t)[b] : FF{0.f, 0.f};
+      const FF tot = warp_sum_ff(v);
+      const float x0 = *cluster.map_shared_rank(pcb + i, own_next);
+      float beta, tpv, sp;
+      if (i < ncols - 2) {
+        householder_ff(x0, tot, &beta, &tpv, &sp);
+      } else {  // one element left: no reflection (bidiag.c:125-129)
+        beta = x0;
+        tpv = 0.f;
+        sp = 0.f;
       }
-      __syncthreads();
-      FF s{0.f, 0.f};
-      for (int l = lfirst(i + 2) + t; l < nown; l += nt_) s = ff_add_sq(s, A[i + (size_t)l * mt]);
-      s = tail_sum_ff(s, red);
       if (t == 0) {
-        *nrm = s;
-        // the row's first element, published before its owner overwrites it in C
-        if (i + 1 < ncols && (i + 1) % C == rank) scal[3] = A[i + (size_t)((i + 1) / C) * mt];
+        if (rank == 0) {
+          p.e[i] = beta;
+          p.taup[i] = tpv;
+        }
+        scal[1] = tpv;
+        scal[2] = sp;
       }
     }
-    if (i == ncols - 1) break;  // last column: no right reflector
+    __syncthreads();
     TMARK(3);
-    cluster.sync();  // #2: row-norm partials published
-    TMARK(4);
-    // ---- C: right reflector from row i (every CTA forms it), partial x
-    float tp;
+    const float tp = scal[1];
+    const float sp = scal[2];
+    for (int l = l1 + t; l < nown; l += nt_) {
+      float* a = A + i + (size_t)l * mt;
+      *a = (rank + l * C == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
+    }
+    // x = a'(:, i+1) + sp * (sum of the C partial products) and the next
+    // column a'(:, i+1) - tp * x, for all rows in every CTA: rows in aligned
+    // groups of four (the vectors are padded past mt), four lanes per group
+    // adding a quarter of the partials each
     {
-      if (t < 32) {
-        // the C partial norms fetched by lanes 0..C-1 at once, added by one shuffle tree
-        FF v = t < C ? *cluster.map_shared_rank(nrm, t) : FF{0.f, 0.f};
-        const FF tot = warp_sum_ff(v);
-        const float x0 = *cluster.map_shared_rank(scal + 3, (i + 1) % C);
-        float beta, tpv, sp;
-        if (i < ncols - 2) {
-          householder_ff(x0, tot, &beta, &tpv, &sp);
-        } else {  // one element left: no reflection (bidiag.c:125-129)
-          beta = x0;
-          tpv = 0.f;
-          sp = 0.f;
-        }
-        if (t == 0) {
-          if (rank == 0) {
-            p.e[i] = beta;
-            p.taup[i] = tpv;
+      const float* pn = cluster.map_shared_rank(pcb, own_next);
+      const int r0 = (i + 1) & ~3;
+      const int ngr = (mt - r0 + 3) >> 2;
+      const int part = t & 3;
+      for (int g0 = 0; g0 < ngr; g0 += nt_ >> 2) {
+        const int g = g0 + (t >> 2);
+        const bool act = g < ngr;
+        const int r = r0 + 4 * g;
+        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act && tp != 0.f) {
+          for (int k = part; k < C; k += 4) {
+            const float4 q = *reinterpret_cast<const float4*>(cluster.map_shared_rank(xpb, k) + r);
+            z.x += q.x;
+            z.y += q.y;
+            z.z += q.z;
+            z.w += q.w;
           }
-          scal[1] = tpv;
-          scal[2] = sp;
         }
-      }
-      __syncthreads();
-      TMARK(5);
-      tp = scal[1];
-      const float sp = scal[2];
-      const int lf = lfirst(i + 1);
-      for (int l = lf + t; l < nown; l += nt_) {
-        float* a = A + i + (size_t)l * mt;
-        *a = (rank + l * C == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
-      }
-      __syncthreads();
-      for (int r = i + 1 + t; r < mt; r += nt_) {
-        float s = 0.f;
-        for (int l = lf; l < nown; l++) s += A[r + (size_t)l * mt] * A[i + (size_t)l * mt];
-        xp[r] = s;
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {  // sums commute: the four lanes agree bit for bit
+          z.x += __shfl_xor_sync(0xffffffffu, z.x, o);
+          z.y += __shfl_xor_sync(0xffffffffu, z.y, o);
+          z.z += __shfl_xor_sync(0xffffffffu, z.z, o);
+          z.w += __shfl_xor_sync(0xffffffffu, z.w, o);
+        }
+        if (act && part == 0) {
+          const float4 a = *reinterpret_cast<const float4*>(pn + r);
+          if (tp != 0.f) {
+            const float4 xv = make_float4(a.x + sp * z.x, a.y + sp * z.y, a.z + sp * z.z, a.w + sp * z.w);
+            *reinterpret_cast<float4*>(x + r) = xv;
+            *reinterpret_cast<float4*>(u + r) =
+                make_float4(a.x - tp * xv.x, a.y - tp * xv.y, a.z - tp * xv.z, a.w - tp * xv.w);
+          } else {
+            *reinterpret_cast<float4*>(u + r) = a;
+          }
+        }
       }
     }
-    TMARK(6);
-    cluster.sync();  // #3: partial x published
-    TMARK(7);
-    // ---- D: x = sum of the C partials (reduce-scatter, all-gather), right update
-    {
-      const int len = ceil_div(mt - i - 1, C);
-      const int s0 = i + 1 + rank * len, s1 = min(mt, s0 + len);
-      for (int r = s0 + t; r < s1; r += nt_) {
-        float s = 0.f;
-        for (int k = 0; k < C; k++) s += cluster.map_shared_rank(xp, k)[r];
-        xs[r] = s;
-      }
-      TMARK(8);
-      cluster.sync();  // #4: slices of x published
-      TMARK(9);
-      for (int r = i + 1 + t; r < mt; r += nt_) x[r] = cluster.map_shared_rank(xs, (r - i - 1) / len)[r];
+    __syncthreads();
+    TMARK(4);
+    const float tq = form_left(i + 1);
+    TMARK(5);
+    // ---- D: right update of the own columns > i + 1 (column i + 1 now holds
+    // its left reflector), then their left update with it
+    const int lr = lfirst(i + 2);
+    const int rows = mt - i - 1;
+    if (rows <= 32 * 16) {
+      // one pass per column, x and u held in registers (the fewest per lane that hold the rows)
+      const int lv = lfirst(i + 3);
+      if (rows <= 32 * 4)
+        tail_fused_update<4>(A, mt, i, lr, nown, tp, tq, x, u, vrow, lv);
+      else if (rows <= 32 * 8)
+        tail_fused_update<8>(A, mt, i, lr, nown, tp, tq, x, u, vrow, lv);
+      else
+        tail_fused_update<16>(A, mt, i, lr, nown, tp, tq, x, u, vrow, lv);
       __syncthreads();
+    } else {
       if (tp != 0.f) {
-        const int lf = lfirst(i + 1);
         for (int r = i + 1 + t; r < mt; r += nt_) {
           const float f = tp * x[r];
-          for (int l = lf; l < nown; l++) A[r + (size_t)l * mt] -= f * A[i + (size_t)l * mt];
+          for (int l = lr; l < nown; l++) A[r + (size_t)l * mt] -= f * A[i + (size_t)l * mt];
         }
       }
       __syncthreads();
-      TMARK(10);
+      left_update(i + 1, tq);
     }
+    TMARK(6);
   }
   // reflectors and the bidiagonal's neighbourhood back to the working matrix
   cluster.sync();
