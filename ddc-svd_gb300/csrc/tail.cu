@@ -230,19 +230,24 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
     TMARK(1);
     cluster.sync();  // partial norms, partial products and column i + 1 published
     TMARK(2);
-    // ---- C: right reflector from row i (every CTA forms it)
-    if (t < 32) {
-      // the C partial norms fetched by lanes 0..C-1 at once, added by one shuffle tree
-      FF v = t < C ? cluster.map_shared_rank(nrm, t)[b] : FF{0.f, 0.f};
+    // ---- C: right reflector from row i (every CTA forms it; warp 0), and
+    // x = a'(:, i+1) + sp * (sum of the C partial products) with the next
+    // column a'(:, i+1) - tp * x, for all rows in every CTA: rows in aligned
+    // groups of four (the vectors are padded past mt), four lanes per group
+    // adding a quarter of the partials each
+    const float* pn = cluster.map_shared_rank(pcb, own_next);
+    const int r0 = (i + 1) & ~3;
+    const int ngr = (mt - r0 + 3) >> 2;
+    const int part = t & 3;
+    auto right_reflector = [&](FF v, float x0) {  // warp 0; v: lane t < C holds CTA t's norm partial
       const FF tot = warp_sum_ff(v);
-      const float x0 = *cluster.map_shared_rank(pcb + i, own_next);
-      float beta, tpv, sp;
+      float beta, tpv, spv;
       if (i < ncols - 2) {
-        householder_ff(x0, tot, &beta, &tpv, &sp);
+        householder_ff(x0, tot, &beta, &tpv, &spv);
       } else {  // one element left: no reflection (bidiag.c:125-129)
         beta = x0;
         tpv = 0.f;
-        sp = 0.f;
+        spv = 0.f;
       }
       if (t == 0) {
         if (rank == 0) {
@@ -250,62 +255,85 @@ __global__ void __launch_bounds__(kTailThreads, 1) bidiag_tail_kernel(TailParams
           p.taup[i] = tpv;
         }
         scal[1] = tpv;
-        scal[2] = sp;
+        scal[2] = spv;
       }
-    }
-    __syncthreads();
-    TMARK(3);
-    const float tp = scal[1];
-    const float sp = scal[2];
-    for (int l = l1 + t; l < nown; l += nt_) {
-      float* a = A + i + (size_t)l * mt;
-      *a = (rank + l * C == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
-    }
-    // x = a'(:, i+1) + sp * (sum of the C partial products) and the next
-    // column a'(:, i+1) - tp * x, for all rows in every CTA: rows in aligned
-    // groups of four (the vectors are padded past mt), four lanes per group
-    // adding a quarter of the partials each
-    {
-      const float* pn = cluster.map_shared_rank(pcb, own_next);
-      const int r0 = (i + 1) & ~3;
-      const int ngr = (mt - r0 + 3) >> 2;
-      const int part = t & 3;
+    };
+    auto zsum = [&](int r, bool load) {  // the group's rows summed over the C partials (all four lanes)
+      float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (load) {
+        for (int k = part; k < C; k += 4) {
+          const float4 q = *reinterpret_cast<const float4*>(cluster.map_shared_rank(xpb, k) + r);
+          z.x += q.x;
+          z.y += q.y;
+          z.z += q.z;
+          z.w += q.w;
+        }
+      }
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {  // sums commute: the four lanes agree bit for bit
+        z.x += __shfl_xor_sync(0xffffffffu, z.x, o);
+        z.y += __shfl_xor_sync(0xffffffffu, z.y, o);
+        z.z += __shfl_xor_sync(0xffffffffu, z.z, o);
+        z.w += __shfl_xor_sync(0xffffffffu, z.w, o);
+      }
+      return z;
+    };
+    auto finish = [&](int r, float4 a, float4 z, float tp, float sp) {  // x and the next column, rows r..r+3
+      if (tp != 0.f) {
+        const float4 xv = make_float4(a.x + sp * z.x, a.y + sp * z.y, a.z + sp * z.z, a.w + sp * z.w);
+        *reinterpret_cast<float4*>(x + r) = xv;
+        *reinterpret_cast<float4*>(u + r) =
+            make_float4(a.x - tp * xv.x, a.y - tp * xv.y, a.z - tp * xv.z, a.w - tp * xv.w);
+      } else {
+        *reinterpret_cast<float4*>(u + r) = a;
+      }
+    };
+    auto scale_row = [&](float tp, float sp) {  // row i of the own columns > i: the stored right reflector
+      for (int l = l1 + t; l < nown; l += nt_) {
+        float* a = A + i + (size_t)l * mt;
+        *a = (rank + l * C == i + 1) ? (tp != 0.f ? 1.f : 0.f) : *a * sp;
+      }
+    };
+    if (ngr <= (nt_ >> 2)) {
+      // one group per four lanes covers every row: the partial sums are loaded
+      // together with the reflector's inputs and wait in registers for tp and sp
+      FF v{0.f, 0.f};
+      float x0 = 0.f;
+      if (t < 32) {
+        if (t < C) v = cluster.map_shared_rank(nrm, t)[b];
+        x0 = *cluster.map_shared_rank(pcb + i, own_next);
+      }
+      const int g = t >> 2;
+      const bool act = g < ngr;
+      const int r = r0 + 4 * g;
+      const float4 z = zsum(r, act);
+      const float4 a = (act && part == 0) ? *reinterpret_cast<const float4*>(pn + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t < 32) right_reflector(v, x0);
+      __syncthreads();
+      TMARK(3);
+      const float tp = scal[1], sp = scal[2];
+      scale_row(tp, sp);
+      if (act && part == 0) finish(r, a, z, tp, sp);
+    } else {
+      if (t < 32) {
+        const FF v = t < C ? cluster.map_shared_rank(nrm, t)[b] : FF{0.f, 0.f};
+        right_reflector(v, *cluster.map_shared_rank(pcb + i, own_next));
+      }
+      __syncthreads();
+      TMARK(3);
+      const float tp = scal[1], sp = scal[2];
+      scale_row(tp, sp);
       for (int g0 = 0; g0 < ngr; g0 += nt_ >> 2) {
         const int g = g0 + (t >> 2);
         const bool act = g < ngr;
         const int r = r0 + 4 * g;
-        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (act && tp != 0.f) {
-          for (int k = part; k < C; k += 4) {
-            const float4 q = *reinterpret_cast<const float4*>(cluster.map_shared_rank(xpb, k) + r);
-            z.x += q.x;
-            z.y += q.y;
-            z.z += q.z;
-            z.w += q.w;
-          }
-        }
-#pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {  // sums commute: the four lanes agree bit for bit
-          z.x += __shfl_xor_sync(0xffffffffu, z.x, o);
-          z.y += __shfl_xor_sync(0xffffffffu, z.y, o);
-          z.z += __shfl_xor_sync(0xffffffffu, z.z, o);
-          z.w += __shfl_xor_sync(0xffffffffu, z.w, o);
-        }
-        if (act && part == 0) {
-          const float4 a = *reinterpret_cast<const float4*>(pn + r);
-          if (tp != 0.f) {
-            const float4 xv = make_float4(a.x + sp * z.x, a.y + sp * z.y, a.z + sp * z.z, a.w + sp * z.w);
-            *reinterpret_cast<float4*>(x + r) = xv;
-            *reinterpret_cast<float4*>(u + r) =
-                make_float4(a.x - tp * xv.x, a.y - tp * xv.y, a.z - tp * xv.z, a.w - tp * xv.w);
-          } else {
-            *reinterpret_cast<float4*>(u + r) = a;
-          }
-        }
+        const float4 z = zsum(r, act && tp != 0.f);
+        if (act && part == 0) finish(r, *reinterpret_cast<const float4*>(pn + r), z, tp, sp);
       }
     }
     __syncthreads();
     TMARK(4);
+    const float tp = scal[1];
     const float tq = form_left(i + 1);
     TMARK(5);
     // ---- D: right update of the own columns > i + 1 (column i + 1 now holds
